@@ -1,0 +1,63 @@
+"""Extract the golden vectors the tests replay from the reference's committed
+known-answer files.
+
+The reference pins its hot path with text fixtures generated against
+arkworks (ark-bn254 0.6) and Plonky3's Poseidon2; this script copies the
+lines the tests use into tests/golden/, trimming the two very large corpora
+(Fq and G1) to a deterministic prefix so the fixtures stay small. Run it from
+the repository root in a checkout that has the reference tree:
+
+    python tests/golden/make_golden.py /path/to/apogee-vm
+
+Every output file starts with a header naming its source file and the
+selection applied.
+"""
+import os
+import sys
+
+SOURCES = {
+    # name: (path inside the reference, line filter, max data lines or None)
+    "fr_kats.txt": ("crates/field/tests/vectors/fr_kats.txt", None, None),
+    "fq_kats.txt": ("crates/curve/tests/vectors/fq_kats.txt", ("fq_ops", "fq_pow", "fq_bytes", "fq_u64"), 400),
+    "g1_kats.txt": ("crates/curve/tests/vectors/g1_kats.txt", None, 120),
+    "msm_kats.txt": ("crates/curve/tests/vectors/msm_kats.txt", None, None),
+    "poly_kats.txt": ("crates/poly/tests/vectors/poly_kats.txt", None, None),
+    "poseidon2_perm.txt": ("crates/transcript/tests/vectors/poseidon2_perm.txt", None, None),
+    "transcript_cases.txt": ("crates/transcript/tests/vectors/transcript_cases.txt", None, None),
+    "g1_absorb_kats.txt": ("crates/pcs/tests/vectors/g1_absorb_kats.txt", None, None),
+    "mercury_proof.txt": ("crates/pcs/tests/vectors/mercury_proof.txt", None, None),
+    "mercury_batch.txt": ("crates/pcs/tests/vectors/mercury_batch.txt", None, None),
+    "accumulator.txt": ("crates/pcs/tests/vectors/accumulator.txt", None, None),
+}
+
+
+def main(ref_root: str) -> None:
+    out_dir = os.path.dirname(os.path.abspath(__file__))
+    for name, (rel, kinds, limit) in SOURCES.items():
+        src = os.path.join(ref_root, rel)
+        with open(src) as f:
+            lines = f.read().splitlines()
+        kept = []
+        counts = {}
+        for line in lines:
+            if not line or line.startswith("#"):
+                continue
+            kind = line.split()[0]
+            if kinds is not None and kind not in kinds:
+                continue
+            if limit is not None:
+                counts[kind] = counts.get(kind, 0) + 1
+                if counts[kind] > limit:
+                    continue
+            kept.append(line)
+        sel = "all data lines" if limit is None else f"first {limit} data lines of each record kind"
+        if kinds is not None:
+            sel += f" of kinds {', '.join(kinds)}"
+        header = [f"# golden vectors from the reference's {rel}", f"# selection: {sel}"]
+        with open(os.path.join(out_dir, name), "w") as f:
+            f.write("\n".join(header + kept) + "\n")
+        print(f"{name}: {len(kept)} lines")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,151 @@
+"""ctypes access to the CPU oracle (oracle/liboracle.so), plus the small
+field/RNG helpers the tests share.
+
+The oracle is test infrastructure: the tests use it to check the CUDA
+library, never the other way round.
+"""
+import ctypes
+import os
+import subprocess
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+P_R = 21888242871839275222246405745257275088548364400416034343698204186575808495617
+P_Q = 21888242871839275222246405745257275088696311157297823662689037894645226208583
+SNAP = 226
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        so = os.path.join(ORACLE_DIR, "liboracle.so")
+        srcs = [os.path.join(ORACLE_DIR, f) for f in os.listdir(ORACLE_DIR) if f.endswith((".cpp", ".hpp"))]
+        if not os.path.exists(so) or any(os.path.getmtime(s) > os.path.getmtime(so) for s in srcs):
+            subprocess.check_call(["make", "-s", "-C", ORACLE_DIR])
+        _lib = ctypes.CDLL(so)
+        _lib.oracle_time_msm.restype = ctypes.c_double
+    return _lib
+
+
+def fe(x: int) -> bytes:
+    return int(x).to_bytes(32, "little")
+
+
+def fe_int(b: bytes) -> int:
+    return int.from_bytes(b, "little")
+
+
+def hexb(s: str) -> bytes:
+    return bytes.fromhex(s)
+
+
+class Rng:
+    """splitmix64, as tools/test-support/src/lib.rs:26-66 defines it."""
+
+    def __init__(self, seed: int):
+        self.s = seed & 0xFFFFFFFFFFFFFFFF
+
+    def next_u64(self) -> int:
+        self.s = (self.s + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+        z = self.s
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+        return z ^ (z >> 31)
+
+    def next_le32(self) -> bytes:
+        return b"".join(self.next_u64().to_bytes(8, "little") for _ in range(4))
+
+    def next_fr(self) -> int:
+        """Rejection sampling with the top two bits cleared
+        (crates/curve/tests/common/mod.rs:33-41)."""
+        while True:
+            b = bytearray(self.next_le32())
+            b[31] &= 0x3F
+            v = int.from_bytes(b, "little")
+            if v < P_R:
+                return v
+
+
+def buf(n: int):
+    return ctypes.create_string_buffer(n)
+
+
+def new_snapshot() -> bytearray:
+    s = buf(SNAP)
+    lib().oracle_transcript_new(s)
+    return bytearray(s.raw)
+
+
+def transcript_op(snap: bytearray, op: int, tag: int = 0, data: bytes = b"", n: int = 0) -> bytes:
+    s = (ctypes.c_uint8 * SNAP).from_buffer(snap)
+    out = buf(32)
+    rc = lib().oracle_transcript_op(s, op, ctypes.c_uint64(tag), data, ctypes.c_size_t(n), out)
+    assert rc == 0, f"oracle transcript op {op} failed: {rc}"
+    return out.raw
+
+
+def g1_mul(point: bytes, k: int) -> bytes:
+    out = buf(64)
+    assert lib().oracle_g1_op(2, point, fe(k), out) == 0
+    return out.raw
+
+
+G1_GEN = fe(1) + fe(2)
+
+
+def msm(bases: bytes, scalars: bytes, n: int, threads: int = 4) -> bytes:
+    out = buf(64)
+    rc = lib().oracle_msm(bases, scalars, ctypes.c_size_t(n), ctypes.c_size_t(threads), out)
+    assert rc == 0, rc
+    return out.raw
+
+
+def toy_srs(tau: int, count: int, threads: int = 8) -> bytes:
+    out = buf(64 * count)
+    assert lib().oracle_toy_srs(fe(tau), ctypes.c_size_t(count), ctypes.c_size_t(threads), out) == 0
+    return out.raw
+
+
+def msm_case(pattern: str, n: int, seed: int):
+    """The input expansion of the MSM corpus (crates/curve/tests/msm.rs:41-69):
+    n bases k*G, then n scalars; 'infinity' zeroes every third base,
+    'zeros' and 'identical' rewrite the scalars after drawing them."""
+    rng = Rng(seed)
+    bases = []
+    for i in range(n):
+        k = rng.next_fr()
+        bases.append(b"\x00" * 64 if (pattern == "infinity" and i % 3 == 0) else g1_mul(G1_GEN, k))
+    draws = [rng.next_fr() for _ in range(n)]
+    if pattern == "zeros":
+        scalars = [0] * n
+    elif pattern == "identical":
+        scalars = [draws[0] if n else 0] * n
+    else:
+        scalars = draws
+    return b"".join(bases), b"".join(fe(s) for s in scalars)
+
+
+def golden_lines(name: str):
+    with open(os.path.join(GOLDEN, name)) as f:
+        for line in f:
+            line = line.rstrip("\n")
+            if line and not line.startswith("#"):
+                yield line
+
+
+TAG_NAMES = {
+    "PROTOCOL_SUITE": 1, "PUBLIC_INPUTS": 2, "COMMITMENT": 3, "SUMCHECK_ROUND": 4, "SUMCHECK_CHALLENGE": 5,
+    "EVALUATION_CLAIM": 6, "PCS_OPENING": 7, "WITNESS_DIGEST": 8, "SUMCHECK_FINAL_EVALS": 9,
+    "MERCURY_INSTANCE": 10, "MERCURY_ALPHA": 11, "MERCURY_GAMMA": 12, "MERCURY_Z": 13, "BDFG_BATCH": 14,
+    "BDFG_POINT": 15, "PAIRING_MERGE": 16, "MERCURY_BATCH": 17, "ACCUMULATOR_DIGEST": 18,
+    "ACCUMULATOR_MERGE": 19, "PUBLIC_INPUT_STREAM": 20, "PUBLIC_OUTPUT_STREAM": 21, "PROGRAM_IDENTITY": 22,
+    "VM_CONFIG": 23, "SHARD_COUNTS": 24, "GKR_OUTPUTS": 25, "GKR_OUTPUT_POINT": 26, "GKR_BATCH": 27,
+    "GKR_LAYER_CLAIMS": 28, "GKR_CHILD": 29, "MEMORY_WINDOWS": 30, "MEMORY_BOUNDARY": 31, "PROGRAM_ENTRY": 32,
+    "LOOKUP_CHALLENGE": 33, "SRS_DIGEST": 34, "SRS_VERIFIER": 35, "MEMORY_GROUP": 36, "MEMORY_CHALLENGE": 37,
+    "GLOBAL_STATE_DIGEST": 38, "SHARD_SEED": 39, "SHARD_TS_WINDOW": 40, "GENERIC_TABLE": 41,
+    "STACK_CHALLENGE": 42, "FOLD_STATE": 43, "FOLD_WEIGHT": 44, "FOLD_CHILD": 45,
+}

@@ -1,0 +1,318 @@
+"""Pin the CPU oracle against the reference's committed known-answer vectors
+(tests/golden/, extracted by tests/golden/make_golden.py).
+
+Each test replays one fixture the way the reference's own suite does:
+crates/field/tests, crates/curve/tests/{fq,g1,msm}.rs, crates/poly/tests,
+crates/transcript/tests/{poseidon2,cases}.rs and crates/pcs/tests/kats.rs.
+"""
+import ctypes
+
+import pytest
+
+import oracle_lib as O
+from oracle_lib import buf, fe, hexb
+
+
+def _field_kats(fn, fname, kinds):
+    n = 0
+    for line in O.golden_lines(fname):
+        f = line.split()
+        kind = f[0]
+        if kind not in kinds:
+            continue
+        n += 1
+        yield kind, f
+
+
+def test_fr_kats(oracle):
+    ops = {"add": 0, "sub": 1, "mul": 2}
+    checked = 0
+    for line in O.golden_lines("fr_kats.txt"):
+        f = line.split()
+        out = buf(32)
+        if f[0] in ops:
+            assert oracle.oracle_fr_op(ops[f[0]], hexb(f[1]), hexb(f[2]), out) == 0
+            assert out.raw.hex() == f[3], line
+        elif f[0] == "square":
+            assert oracle.oracle_fr_op(3, hexb(f[1]), None, out) == 0
+            assert out.raw.hex() == f[2]
+        elif f[0] == "inv":
+            rc = oracle.oracle_fr_op(4, hexb(f[1]), None, out)
+            if f[2] == "none":
+                assert rc == 1
+            else:
+                assert rc == 0 and out.raw.hex() == f[2]
+        elif f[0] == "pow":
+            assert oracle.oracle_fr_op(5, hexb(f[1]), hexb(f[2]), out) == 0
+            assert out.raw.hex() == f[3]
+        else:
+            continue
+        checked += 1
+    assert checked == 536
+
+
+def test_fq_kats(oracle):
+    checked = 0
+    for line in O.golden_lines("fq_kats.txt"):
+        f = line.split()
+        out = buf(32)
+        if f[0] == "fq_ops":
+            a, b = hexb(f[1]), hexb(f[2])
+            for op, want in ((0, f[3]), (1, f[4]), (2, f[5])):
+                assert oracle.oracle_fq_op(op, a, b, out) == 0
+                assert out.raw.hex() == want, line
+            assert oracle.oracle_fq_op(3, a, None, out) == 0 and out.raw.hex() == f[6]
+            rc = oracle.oracle_fq_op(4, a, None, out)
+            assert (rc == 1) if f[7] == "none" else (rc == 0 and out.raw.hex() == f[7])
+        elif f[0] == "fq_pow":
+            assert oracle.oracle_fq_op(5, hexb(f[1]), hexb(f[2]), out) == 0
+            assert out.raw.hex() == f[3]
+        elif f[0] == "fq_bytes":
+            v = int.from_bytes(hexb(f[1]), "little")
+            assert (v < O.P_Q) == (f[2] == "ok")
+        else:
+            continue
+        checked += 1
+    assert checked > 400
+
+
+def test_g1_kats(oracle):
+    checked = 0
+    for line in O.golden_lines("g1_kats.txt"):
+        f = line.split()
+        out = buf(64)
+        if f[0] == "g1_generator":
+            assert f[1] == O.G1_GEN.hex()
+        elif f[0] == "g1_ops":
+            p, q, k = hexb(f[1]), hexb(f[2]), hexb(f[3])
+            assert oracle.oracle_g1_op(0, p, q, out) == 0 and out.raw.hex() == f[4]
+            assert oracle.oracle_g1_op(1, p, None, out) == 0 and out.raw.hex() == f[5]
+            assert oracle.oracle_g1_op(2, p, k, out) == 0 and out.raw.hex() == f[6]
+            assert oracle.oracle_g1_op(3, p, None, out) == 0 and out.raw.hex() == f[7]
+        elif f[0] == "g1_add_edge":
+            assert oracle.oracle_g1_op(0, hexb(f[2]), hexb(f[3]), out) == 0
+            assert out.raw.hex() == f[4], line
+        elif f[0] == "g1_madd_edge":
+            # acc = 2P at Z != 1; acc + 2P through the mixed add is 4P and
+            # acc + (-2P) is infinity (crates/curve/tests/kats.rs:454-475).
+            p = hexb(f[1])
+            assert oracle.oracle_g1_op(1, p, None, out) == 0 and out.raw.hex() == f[2]
+            assert oracle.oracle_g1_op(4, p, hexb(f[2]), out) == 0 and out.raw.hex() == f[3]
+            assert oracle.oracle_g1_op(4, p, hexb(f[4]), out) == 0 and out.raw == bytes(64)
+        elif f[0] == "g1_scalar_edge":
+            assert oracle.oracle_g1_op(2, hexb(f[2]), hexb(f[3]), out) == 0
+            assert out.raw.hex() == f[4], line
+        elif f[0] == "g1_reject":
+            assert oracle.oracle_g1_check(hexb(f[1])) != 0
+        else:
+            continue
+        checked += 1
+    assert checked > 100
+
+
+def test_msm_kats(oracle):
+    checked = 0
+    for line in O.golden_lines("msm_kats.txt"):
+        f = line.split()
+        pattern, n, seed, want = f[1], int(f[2]), int(f[3]), f[4]
+        bases, scalars = O.msm_case(pattern, n, seed)
+        got = O.msm(bases, scalars, n, threads=8)
+        assert got.hex() == want, f"{pattern} n={n}"
+        checked += 1
+    assert checked == 13
+
+
+def test_msm_thread_count_independent(oracle):
+    bases, scalars = O.msm_case("random", 300, 7)
+    outs = {O.msm(bases, scalars, 300, threads=t) for t in (1, 3, 16)}
+    assert len(outs) == 1
+
+
+def test_poseidon2_perm(oracle):
+    checked = 0
+    for line in O.golden_lines("poseidon2_perm.txt"):
+        f = line.split()
+        out = buf(96)
+        assert oracle.oracle_poseidon2(b"".join(hexb(x) for x in f[1:4]), out) == 0
+        assert out.raw.hex() == "".join(f[4:7])
+        checked += 1
+    assert checked == 128
+
+
+def test_transcript_cases(oracle):
+    snap = None
+    cases = 0
+    for line in O.golden_lines("transcript_cases.txt"):
+        f = line.split()
+        if f[0] == "case":
+            snap = O.new_snapshot()
+        elif f[0] == "end":
+            cases += 1
+        elif f[0] == "observe":
+            O.transcript_op(snap, 0, data=hexb(f[1]))
+        elif f[0] == "sample":
+            assert O.transcript_op(snap, 1).hex() == f[1]
+        elif f[0] == "append_scalar":
+            O.transcript_op(snap, 2, O.TAG_NAMES[f[1]], hexb(f[2]), 1)
+        elif f[0] == "append_scalars":
+            n = int(f[2])
+            O.transcript_op(snap, 2, O.TAG_NAMES[f[1]], b"".join(hexb(x) for x in f[3:3 + n]), n)
+        elif f[0] == "append_bytes":
+            data = b"" if f[3] == "-" else hexb(f[3])
+            assert len(data) == int(f[2])
+            O.transcript_op(snap, 3, O.TAG_NAMES[f[1]], data, len(data))
+        elif f[0] == "challenge":
+            assert O.transcript_op(snap, 4, O.TAG_NAMES[f[1]]).hex() == f[2]
+        else:
+            raise AssertionError(line)
+    assert cases > 5
+
+
+def test_g1_absorb_kats(oracle):
+    for line in O.golden_lines("g1_absorb_kats.txt"):
+        f = line.split()
+        if f[0] == "single":
+            out = buf(128)
+            oracle.oracle_g1_limbs(hexb(f[1]), out)
+            assert out.raw.hex() == "".join(f[2:6])
+        elif f[0] == "pair":
+            for i, p in enumerate(f[1:3]):
+                out = buf(128)
+                oracle.oracle_g1_limbs(hexb(p), out)
+                assert out.raw.hex() == "".join(f[3 + 4 * i:7 + 4 * i])
+
+
+def test_poly_kats(oracle):
+    lines = [l.split() for l in O.golden_lines("poly_kats.txt")]
+    src = [l for l in lines if l[0] == "source"][0]
+    assert src[1] == "u32"
+    nv = int(src[2])
+    values = [int(l[2], 16) for l in lines if l[0] == "value"]
+    chals = [hexb(l[2]) for l in lines if l[0] == "challenge"]
+    table = bytearray(b"".join(fe(v) for v in values))
+    # bind k index value: the table after binding the first k challenges.
+    binds = {}
+    for l in lines:
+        if l[0] == "bind":
+            binds.setdefault(int(l[1]), {})[int(l[2])] = l[3]
+    for k, entries in binds.items():
+        t = (ctypes.c_uint8 * len(table)).from_buffer_copy(table)
+        assert oracle.oracle_bind(t, nv, b"".join(chals[:k]), k) == 0
+        raw = bytes(t)
+        for idx, want in entries.items():
+            assert raw[32 * idx:32 * idx + 32].hex() == want
+    # eq k index value: eq_table(challenges[..k]).
+    eqs = {}
+    for l in lines:
+        if l[0] == "eq":
+            eqs.setdefault(int(l[1]), {})[int(l[2])] = l[3]
+    for k, entries in eqs.items():
+        out = buf(32 << k)
+        assert oracle.oracle_eq_table(b"".join(chals[:k]), k, out) == 0
+        for idx, want in entries.items():
+            assert out.raw[32 * idx:32 * idx + 32].hex() == want
+    # point case index value / result case value.
+    points = {}
+    for l in lines:
+        if l[0] == "point":
+            points.setdefault(int(l[1]), {})[int(l[2])] = hexb(l[3])
+    results = {int(l[1]): l[2] for l in lines if l[0] == "result"}
+    for case, want in results.items():
+        pt = b"".join(points[case][i] for i in range(nv))
+        out = buf(32)
+        assert oracle.oracle_evaluate(bytes(table), nv, pt, out) == 0
+        assert out.raw.hex() == want
+    assert results and binds and eqs
+
+
+def _parse_proof_kat(name):
+    rec = {"value": {}, "point": {}}
+    for line in O.golden_lines(name):
+        f = line.split()
+        if f[0] in ("value", "point"):
+            rec[f[0]][int(f[1])] = hexb(f[2])
+        else:
+            rec[f[0]] = f[1]
+    nv = int(rec["numvars"])
+    evals = b"".join(rec["value"][i] for i in range(1 << nv))
+    u = b"".join(rec["point"][i] for i in range(nv))
+    return rec, nv, evals, u
+
+
+TOY_TAU = 0xABCDEF
+
+
+def test_mercury_proof_kat(oracle):
+    rec, nv, evals, u = _parse_proof_kat("mercury_proof.txt")
+    assert O.fe_int(hexb(rec["tau"])) == TOY_TAU
+    srs = O.toy_srs(TOY_TAU, 1 << nv)
+    cm = buf(64)
+    assert oracle.oracle_commit(srs, ctypes.c_size_t(1 << nv), evals, nv, 4, cm) == 0
+    assert cm.raw.hex() == rec["commitment"]
+    snap = O.new_snapshot()
+    s = (ctypes.c_uint8 * O.SNAP).from_buffer(snap)
+    v, proof = buf(32), buf(704)
+    rc = oracle.oracle_mercury_open(srs, ctypes.c_size_t(1 << nv), evals, nv, cm.raw, u, s, 4, v, proof)
+    assert rc == 0
+    assert v.raw.hex() == rec["claim"]
+    assert proof.raw.hex() == rec["proof"]
+    assert O.transcript_op(snap, 1).hex() == rec["probe"]
+
+
+def test_mercury_batch_kat(oracle):
+    rec, nv, evals, u = _parse_proof_kat("mercury_batch.txt")
+    srs = O.toy_srs(TOY_TAU, 1 << nv)
+    cm = buf(64)
+    assert oracle.oracle_commit(srs, ctypes.c_size_t(1 << nv), evals, nv, 4, cm) == 0
+    assert cm.raw.hex() == rec["commitment"]
+    snap = O.new_snapshot()
+    s = (ctypes.c_uint8 * O.SNAP).from_buffer(snap)
+    vs, proof = buf(32), buf(704)
+    rc = oracle.oracle_mercury_batch_open(srs, ctypes.c_size_t(1 << nv), evals, 1, nv, cm.raw, u, s, 4, vs, proof)
+    assert rc == 0
+    assert vs.raw.hex() == rec["claim"]
+    assert proof.raw.hex() == rec["proof"]
+    assert O.transcript_op(snap, 1).hex() == rec["probe"]
+
+
+def test_accumulator_batch_proof(oracle):
+    """The three-column batch opening recorded in accumulator.txt replays."""
+    rec = {"batch_value": {}, "batch_point": {}, "batch_claim": {}, "batch_cm": {}}
+    for line in O.golden_lines("accumulator.txt"):
+        f = line.split()
+        if f[0] == "batch_value":
+            rec["batch_value"][(int(f[1]), int(f[2]))] = hexb(f[3])
+        elif f[0] in ("batch_point", "batch_claim", "batch_cm"):
+            rec[f[0]][int(f[1])] = hexb(f[2])
+        elif f[0] in ("numvars", "batch_proof"):
+            rec[f[0]] = f[1]
+    nv = int(rec["numvars"])
+    k = len(rec["batch_cm"])
+    cols = b"".join(rec["batch_value"][(c, i)] for c in range(k) for i in range(1 << nv))
+    u = b"".join(rec["batch_point"][i] for i in range(nv))
+    srs = O.toy_srs(TOY_TAU, 1 << nv)
+    for c in range(k):
+        cm = buf(64)
+        assert oracle.oracle_commit(srs, ctypes.c_size_t(1 << nv), cols[32 * c << nv:32 * (c + 1) << nv], nv, 4, cm) == 0
+        assert cm.raw == rec["batch_cm"][c]
+    snap = O.new_snapshot()
+    s = (ctypes.c_uint8 * O.SNAP).from_buffer(snap)
+    vs, proof = buf(32 * k), buf(704)
+    cms = b"".join(rec["batch_cm"][c] for c in range(k))
+    rc = oracle.oracle_mercury_batch_open(srs, ctypes.c_size_t(1 << nv), cols, k, nv, cms, u, s, 4, vs, proof)
+    assert rc == 0
+    assert vs.raw == b"".join(rec["batch_claim"][c] for c in range(k))
+    assert proof.raw.hex() == rec["batch_proof"]
+
+
+def test_known_tau_commitment(oracle):
+    """cm == [f(tau)] G for a commitment over a seeded-tau SRS."""
+    rng = O.Rng(99)
+    nv = 6
+    tau = rng.next_fr()
+    srs = O.toy_srs(tau, 1 << nv)
+    coeffs = [rng.next_fr() for _ in range(1 << nv)]
+    cm = buf(64)
+    assert oracle.oracle_commit(srs, ctypes.c_size_t(1 << nv), b"".join(fe(c) for c in coeffs), nv, 4, cm) == 0
+    f_tau = sum(c * pow(tau, i, O.P_R) for i, c in enumerate(coeffs)) % O.P_R
+    assert cm.raw == O.g1_mul(O.G1_GEN, f_tau)
