@@ -1,0 +1,193 @@
+"""Python host mirror of the reference's hot-path interface over the C ABI
+(include/apogee_gpu.h, libapogee_gpu.so).
+
+Names and error behaviour follow the reference crates: `msm`/`msm_small_u32`
+(crates/curve/src/msm.rs:48,79) raise MsmError on a length mismatch; `commit`,
+`open`, `batch_open` (crates/pcs/src/lib.rs:237,313,688) raise PcsError with the
+reference's variant name. Field elements cross as Python ints (canonical) or as
+raw in-memory bytes; points as 64-byte canonical encodings.
+
+There is no CPU fallback: importing this module without the compiled library,
+or calling it without a CUDA device, raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libapogee_gpu.so")
+
+P_R = 21888242871839275222246405745257275088548364400416034343698204186575808495617
+P_Q = 21888242871839275222246405745257275088696311157297823662689037894645226208583
+R_MONT = pow(2, 256, P_R)
+R_MONT_INV = pow(R_MONT, -1, P_R)
+TRANSCRIPT_BYTES = 226
+PROOF_BYTES = 704
+
+STATUS = {
+    0: "Ok", 1: "LengthMismatch", 2: "UnsupportedNumVars", 3: "PointLengthMismatch", 4: "SrsTooSmall",
+    5: "DegenerateChallenge", 6: "EmptyBatch", 7: "BatchLengthMismatch", 8: "MixedColumnSizes",
+    9: "InvalidPoint", 20: "NonCanonical", 21: "InvalidArgument", 22: "BadCircuit", 23: "NoSrs",
+    24: "Internal", 100: "Cuda", 101: "OutOfMemory", 103: "NoDevice",
+}
+PCS_CODES = {2, 3, 4, 5, 6, 7, 8, 9}
+
+
+class ApogeeError(RuntimeError):
+    def __init__(self, status: int, message: str = ""):
+        self.status = status
+        self.variant = STATUS.get(status, f"status {status}")
+        super().__init__(f"{self.variant}: {message}" if message else self.variant)
+
+
+class MsmError(ApogeeError):
+    """curve::msm::MsmError."""
+
+
+class PcsError(ApogeeError):
+    """pcs_verify::PcsError."""
+
+
+_lib = None
+
+
+def lib():
+    """The loaded library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = ctypes.CDLL(LIB_PATH)
+        L.apg_last_error.restype = ctypes.c_char_p
+        L.apg_ctx_stream.restype = ctypes.c_void_p
+        L.apg_srs_len.restype = ctypes.c_size_t
+        for name in ("apg_srs_len", "apg_last_error", "apg_ctx_stream"):
+            getattr(L, name).argtypes = [ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+# ---------------------------------------------------------------------------
+# Encodings
+# ---------------------------------------------------------------------------
+
+def to_mont_bytes(xs) -> bytes:
+    """Canonical ints -> Fr in-memory (Montgomery) bytes, 32 per element."""
+    return b"".join(((int(x) * R_MONT) % P_R).to_bytes(32, "little") for x in xs)
+
+
+def from_mont_bytes(b: bytes):
+    return [(int.from_bytes(b[i:i + 32], "little") * R_MONT_INV) % P_R for i in range(0, len(b), 32)]
+
+
+def fe(x: int) -> bytes:
+    return int(x).to_bytes(32, "little")
+
+
+# ---------------------------------------------------------------------------
+# Context
+# ---------------------------------------------------------------------------
+
+class Context:
+    """One device context: a CUDA stream, scratch memory and a resident SRS."""
+
+    def __init__(self, device: int = 0):
+        self._h = ctypes.c_void_p()
+        st = lib().apg_ctx_create(device, ctypes.byref(self._h))
+        if st != 0:
+            raise ApogeeError(st, "apg_ctx_create")
+
+    def close(self):
+        if self._h:
+            lib().apg_ctx_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return lib().apg_ctx_stream(self._h) or 0
+
+    def _check(self, st: int, cls=ApogeeError):
+        if st != 0:
+            msg = lib().apg_last_error(self._h).decode(errors="replace")
+            if st == 1:
+                raise MsmError(st, msg)
+            if st in PCS_CODES:
+                raise PcsError(st, msg)
+            raise cls(st, msg)
+
+    def synchronize(self):
+        self._check(lib().apg_ctx_synchronize(self._h))
+
+    # ---- SRS --------------------------------------------------------------
+    def srs_upload(self, points: bytes):
+        assert len(points) % 64 == 0
+        self._check(lib().apg_srs_upload(self._h, points, ctypes.c_size_t(len(points) // 64)))
+
+    def srs_generate(self, tau: int, n: int):
+        self._check(lib().apg_srs_generate(self._h, fe(tau), ctypes.c_size_t(n)))
+
+    def srs_download(self, n: int) -> bytes:
+        out = ctypes.create_string_buffer(64 * n)
+        self._check(lib().apg_srs_download(self._h, out, ctypes.c_size_t(n)))
+        return out.raw
+
+    def srs_len(self) -> int:
+        return lib().apg_srs_len(self._h)
+
+    def srs_prepare(self, cbits: int = 0):
+        self._check(lib().apg_srs_prepare(self._h, cbits))
+
+    # ---- MSM ----------------------------------------------------------------
+    def msm(self, bases: bytes, scalars: bytes) -> bytes:
+        """curve::msm::msm: bases 64-byte canonical points, scalars Fr in-memory bytes."""
+        out = ctypes.create_string_buffer(64)
+        self._check(lib().apg_msm(self._h, bases, ctypes.c_size_t(len(bases) // 64), scalars,
+                                  ctypes.c_size_t(len(scalars) // 32), out))
+        return out.raw
+
+    def msm_small_u32(self, bases: bytes, scalars) -> bytes:
+        arr = (ctypes.c_uint32 * len(scalars))(*scalars)
+        out = ctypes.create_string_buffer(64)
+        self._check(lib().apg_msm_small_u32(self._h, bases, ctypes.c_size_t(len(bases) // 64), arr,
+                                            ctypes.c_size_t(len(scalars)), out))
+        return out.raw
+
+    # ---- commit -------------------------------------------------------------
+    def commit(self, evals: bytes, num_vars: int) -> bytes:
+        """pcs::commit over the resident SRS; evals are Fr in-memory bytes."""
+        out = ctypes.create_string_buffer(64)
+        self._check(lib().apg_commit(self._h, evals, ctypes.c_size_t(num_vars), out))
+        return out.raw
+
+    def commit_u32(self, evals, num_vars: int) -> bytes:
+        arr = (ctypes.c_uint32 * len(evals))(*evals)
+        out = ctypes.create_string_buffer(64)
+        self._check(lib().apg_commit_u32(self._h, arr, ctypes.c_size_t(num_vars), out))
+        return out.raw
+
+    def commit_batch(self, cols, num_vars: int) -> list:
+        k = len(cols)
+        ptrs = (ctypes.c_char_p * k)(*cols)
+        out = ctypes.create_string_buffer(64 * k)
+        self._check(lib().apg_commit_batch(self._h, ptrs, ctypes.c_size_t(k), ctypes.c_size_t(num_vars), out))
+        return [out.raw[64 * j:64 * j + 64] for j in range(k)]
+
+    def commit_device(self, d_ptr: int, num_vars: int) -> bytes:
+        out = ctypes.create_string_buffer(64)
+        self._check(lib().apg_commit_device(self._h, ctypes.c_void_p(d_ptr), ctypes.c_size_t(num_vars), out))
+        return out.raw

@@ -1,0 +1,249 @@
+// The C ABI boundary (include/apogee_gpu.h): argument checks in the
+// reference's refusal order, context locking, and the mapping of every
+// failure to an apg_status. No exception crosses this file's functions.
+#include "common.cuh"
+
+using namespace apg;
+
+struct apg_ctx {
+  Ctx c;
+};
+
+namespace {
+
+template <class F>
+int guarded(apg_ctx* ctx, F&& f) {
+  if (!ctx) return APG_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(ctx->c.mu);
+  try {
+    APG_CUDA(cudaSetDevice(ctx->c.device));
+    int st = f(ctx->c);
+    if (st == APG_OK) ctx->c.last_error.clear();
+    return st;
+  } catch (const Error& e) {
+    ctx->c.last_error = e.what();
+    return e.status;
+  } catch (const std::exception& e) {
+    ctx->c.last_error = e.what();
+    return APG_ERR_INTERNAL;
+  }
+}
+
+// Mercury's instance rule (crates/pcs-verify/src/lib.rs:97-102).
+bool mercury_num_vars_ok(size_t nv) { return nv >= 2 && nv <= 54 && nv % 2 == 0; }
+
+// The table a commit of n points reads: a narrow-window one for small
+// instances (cheap bucket reduction), the wide one otherwise.
+const SrsTable* commit_table(Ctx& c, size_t n) {
+  if (n <= ((size_t)1 << 14)) {
+    const SrsTable* t = srs_table(c, 8, n);
+    if (t) return t;
+  }
+  return srs_table(c, 16, n);
+}
+
+int commit_common(Ctx& c, const void* evals, bool on_device, bool small, size_t num_vars, uint8_t* out) {
+  if (!out || (!evals && num_vars > 0)) return APG_ERR_INVALID_ARGUMENT;
+  if (!mercury_num_vars_ok(num_vars)) {
+    c.last_error = "unsupported num_vars";
+    return APG_ERR_UNSUPPORTED_NUM_VARS;
+  }
+  if (!c.srs) return APG_ERR_NO_SRS;
+  size_t n = (size_t)1 << num_vars;
+  if (c.srs_n < n) {
+    c.last_error = "the SRS holds fewer powers than the column has evaluations";
+    return APG_ERR_SRS_TOO_SMALL;
+  }
+  const size_t elem = small ? 4 : 32;
+  const void* d = evals;
+  if (!on_device) {
+    void* buf = c.scratch[S_SCALARS].get(n * elem);
+    APG_CUDA(cudaMemcpyAsync(buf, evals, n * elem, cudaMemcpyHostToDevice, c.stream));
+    d = buf;
+  }
+  const SrsTable* t = commit_table(c, n);
+  if (!t) throw Error(APG_ERR_INTERNAL, "no SRS window table");
+  msm_device(c, nullptr, t, d, small, false, n, nullptr, out);
+  return APG_OK;
+}
+
+int msm_common(Ctx& c, const uint8_t* bases, size_t nb, const void* scalars, size_t ns, bool small, uint8_t* out) {
+  if (!out) return APG_ERR_INVALID_ARGUMENT;
+  if (nb != ns) {
+    c.last_error = "one scalar per base";
+    return APG_ERR_LENGTH_MISMATCH;
+  }
+  if (nb == 0) {
+    memset(out, 0, 64);
+    return APG_OK;
+  }
+  if (!bases || !scalars) return APG_ERR_INVALID_ARGUMENT;
+  Affine* d_bases = c.scratch[S_BASES].as<Affine>(nb);
+  upload_points(c, bases, nb, d_bases);
+  const size_t elem = small ? 4 : 32;
+  void* d_s = c.scratch[S_SCALARS].get(ns * elem);
+  APG_CUDA(cudaMemcpyAsync(d_s, scalars, ns * elem, cudaMemcpyHostToDevice, c.stream));
+  msm_device(c, d_bases, nullptr, d_s, small, false, nb, nullptr, out);
+  return APG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int apg_ctx_create(int device, apg_ctx** out) {
+  if (!out) return APG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= device || device < 0) return APG_ERR_NO_DEVICE;
+  apg_ctx* ctx = new apg_ctx();
+  ctx->c.device = device;
+  try {
+    APG_CUDA(cudaSetDevice(device));
+    APG_CUDA(cudaDeviceGetAttribute(&ctx->c.sm_count, cudaDevAttrMultiProcessorCount, device));
+    APG_CUDA(cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking));
+    APG_CUDA(cudaMalloc(&ctx->c.d_flags, 4));
+    APG_CUDA(cudaMemset(ctx->c.d_flags, 0, 4));
+  } catch (const Error& e) {
+    delete ctx;
+    return e.status;
+  }
+  *out = ctx;
+  return APG_OK;
+}
+
+void apg_ctx_destroy(apg_ctx* ctx) {
+  if (!ctx) return;
+  {
+    std::lock_guard<std::mutex> lock(ctx->c.mu);
+    Ctx& c = ctx->c;
+    cudaSetDevice(c.device);
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    for (auto& b : c.scratch) b.release();
+    for (auto& t : c.tables) cudaFree(t.tab);
+    if (c.srs) cudaFree(c.srs);
+    if (c.d_flags) cudaFree(c.d_flags);
+    if (c.stream) cudaStreamDestroy(c.stream);
+  }
+  delete ctx;
+}
+
+const char* apg_last_error(apg_ctx* ctx) { return ctx ? ctx->c.last_error.c_str() : "null context"; }
+
+void* apg_ctx_stream(apg_ctx* ctx) { return ctx ? (void*)ctx->c.stream : nullptr; }
+
+int apg_ctx_synchronize(apg_ctx* ctx) {
+  return guarded(ctx, [&](Ctx& c) {
+    APG_CUDA(cudaStreamSynchronize(c.stream));
+    return APG_OK;
+  });
+}
+
+static void drop_srs(Ctx& c) {
+  APG_CUDA(cudaStreamSynchronize(c.stream));
+  for (auto& t : c.tables) cudaFree(t.tab);
+  c.tables.clear();
+  if (c.srs) cudaFree(c.srs);
+  c.srs = nullptr;
+  c.srs_n = 0;
+}
+
+int apg_srs_upload(apg_ctx* ctx, const uint8_t* g1_points, size_t n) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (!g1_points || n == 0) return (int)APG_ERR_INVALID_ARGUMENT;
+    drop_srs(c);
+    Affine* d = nullptr;
+    APG_CUDA(cudaMalloc(&d, n * sizeof(Affine)));
+    try {
+      upload_points(c, g1_points, n, d);
+    } catch (...) {
+      cudaFree(d);
+      throw;
+    }
+    c.srs = d;
+    c.srs_n = n;
+    return (int)APG_OK;
+  });
+}
+
+int apg_srs_generate(apg_ctx* ctx, const uint8_t tau[32], size_t n) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (!tau || n == 0) return (int)APG_ERR_INVALID_ARGUMENT;
+    drop_srs(c);
+    Affine* d = nullptr;
+    APG_CUDA(cudaMalloc(&d, n * sizeof(Affine)));
+    try {
+      generate_srs(c, tau, n, d);
+    } catch (...) {
+      cudaFree(d);
+      throw;
+    }
+    c.srs = d;
+    c.srs_n = n;
+    return (int)APG_OK;
+  });
+}
+
+int apg_srs_download(apg_ctx* ctx, uint8_t* g1_points, size_t n) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (!c.srs) return (int)APG_ERR_NO_SRS;
+    if (!g1_points || n > c.srs_n) return (int)APG_ERR_INVALID_ARGUMENT;
+    download_points(c, c.srs, n, g1_points);
+    return (int)APG_OK;
+  });
+}
+
+size_t apg_srs_len(apg_ctx* ctx) {
+  if (!ctx) return 0;
+  std::lock_guard<std::mutex> lock(ctx->c.mu);
+  return ctx->c.srs_n;
+}
+
+int apg_srs_prepare(apg_ctx* ctx, int cbits) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (!c.srs) return (int)APG_ERR_NO_SRS;
+    if (cbits == 0) {
+      srs_table(c, 8, std::min(c.srs_n, (size_t)1 << 14));
+      srs_table(c, 16, c.srs_n);
+    } else {
+      if (cbits < 2 || cbits > 20) return (int)APG_ERR_INVALID_ARGUMENT;
+      srs_table(c, cbits, c.srs_n);
+    }
+    return (int)APG_OK;
+  });
+}
+
+int apg_msm(apg_ctx* ctx, const uint8_t* bases, size_t n_bases, const uint8_t* scalars, size_t n_scalars,
+            uint8_t out[64]) {
+  return guarded(ctx, [&](Ctx& c) { return msm_common(c, bases, n_bases, scalars, n_scalars, false, out); });
+}
+
+int apg_msm_small_u32(apg_ctx* ctx, const uint8_t* bases, size_t n_bases, const uint32_t* scalars,
+                      size_t n_scalars, uint8_t out[64]) {
+  return guarded(ctx, [&](Ctx& c) { return msm_common(c, bases, n_bases, scalars, n_scalars, true, out); });
+}
+
+int apg_commit(apg_ctx* ctx, const uint8_t* evals, size_t num_vars, uint8_t out[64]) {
+  return guarded(ctx, [&](Ctx& c) { return commit_common(c, evals, false, false, num_vars, out); });
+}
+
+int apg_commit_u32(apg_ctx* ctx, const uint32_t* evals, size_t num_vars, uint8_t out[64]) {
+  return guarded(ctx, [&](Ctx& c) { return commit_common(c, evals, false, true, num_vars, out); });
+}
+
+int apg_commit_device(apg_ctx* ctx, const void* d_evals, size_t num_vars, uint8_t out[64]) {
+  return guarded(ctx, [&](Ctx& c) { return commit_common(c, d_evals, true, false, num_vars, out); });
+}
+
+int apg_commit_batch(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_t num_vars, uint8_t* out) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (!cols || !out) return (int)APG_ERR_INVALID_ARGUMENT;
+    for (size_t j = 0; j < k; ++j) {
+      int st = commit_common(c, cols[j], false, false, num_vars, out + 64 * j);
+      if (st) return st;
+    }
+    return (int)APG_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,139 @@
+// Library-internal plumbing: the device context behind an apg_ctx handle,
+// status propagation and scratch memory.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/apogee_gpu.h"
+#include "curve.cuh"
+
+namespace apg {
+
+// A failure carrying the C ABI status it maps to. Every entry point catches
+// it at the boundary; nothing escapes into the caller's process as a throw.
+struct Error : std::runtime_error {
+  int status;
+  Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define APG_CUDA(call)                                                                                      \
+  do {                                                                                                      \
+    cudaError_t e_ = (call);                                                                                \
+    if (e_ != cudaSuccess)                                                                                  \
+      throw ::apg::Error(e_ == cudaErrorMemoryAllocation ? APG_ERR_OUT_OF_MEMORY : APG_ERR_CUDA,          \
+                         std::string(#call) + ": " + cudaGetErrorString(e_));                              \
+  } while (0)
+
+#define APG_LAUNCH_CHECK() APG_CUDA(cudaGetLastError())
+
+// Device-side error flags a kernel may raise; read back after a sync.
+enum DeviceFlag : uint32_t {
+  DEV_NONCANONICAL = 1u,   // an input coordinate or scalar was >= its modulus
+  DEV_OFF_CURVE = 2u,      // an input point failed y^2 = x^3 + 3
+  DEV_TRANSCRIPT = 4u,     // a transcript invariant was broken
+  DEV_DEGENERATE = 8u,     // Mercury's {z, 1/z, alpha} had a repeat
+  DEV_NONZERO_REM = 16u,   // a division that must be exact left a remainder
+};
+
+// A grow-only device buffer.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  void* get(size_t bytes) {
+    if (bytes > cap) {
+      if (p) cudaFree(p);
+      p = nullptr;
+      cap = 0;
+      size_t want = bytes + bytes / 8 + 256;
+      APG_CUDA(cudaMalloc(&p, want));
+      cap = want;
+    }
+    return p;
+  }
+  template <class T>
+  T* as(size_t count) {
+    return reinterpret_cast<T*>(get(count * sizeof(T)));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// The precomputed window table of the resident SRS for one window width:
+// tab[w * n + i] = 2^(c*w) * P_i, affine Montgomery.
+struct SrsTable {
+  int c = 0, windows = 0;
+  size_t n = 0;
+  Affine* tab = nullptr;
+};
+
+enum ScratchSlot {
+  S_ENTRIES, S_SORTED, S_COUNTS, S_OFFSETS, S_SCANBLK, S_BUCKETS, S_HEAD, S_TAIL, S_FLAGS, S_LEVEL_A,
+  S_LEVEL_B, S_LEVEL_T, S_TSUM, S_RESULT, S_BASES, S_SCALARS, S_TMP0, S_TMP1, S_TMP2, S_TMP3, S_TMP4,
+  S_TMP5, S_TMP6, S_TMP7, S_COUNT
+};
+
+struct Ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  std::string last_error;
+  Affine* srs = nullptr;
+  size_t srs_n = 0;
+  std::vector<SrsTable> tables;
+  DevBuf scratch[S_COUNT];
+  uint32_t* d_flags = nullptr;  // device error flags (DeviceFlag bits)
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  void check_flags() {
+    uint32_t f = 0;
+    APG_CUDA(cudaMemcpyAsync(&f, d_flags, 4, cudaMemcpyDeviceToHost, stream));
+    APG_CUDA(cudaStreamSynchronize(stream));
+    if (f) {
+      APG_CUDA(cudaMemsetAsync(d_flags, 0, 4, stream));
+      if (f & DEV_NONCANONICAL) throw Error(APG_ERR_NONCANONICAL, "an input value is not below its modulus");
+      if (f & DEV_OFF_CURVE) throw Error(APG_ERR_INVALID_POINT, "an input point is not on the curve");
+      if (f & DEV_DEGENERATE) throw Error(APG_ERR_DEGENERATE_CHALLENGE, "degenerate Mercury challenge set");
+      if (f & DEV_NONZERO_REM) throw Error(APG_ERR_INTERNAL, "an exact division left a remainder");
+      throw Error(APG_ERR_INTERNAL, "device invariant failed");
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Entry points implemented in the .cu files.
+// ---------------------------------------------------------------------------
+
+// Canonical Fr -> Montgomery in place, raising DEV_NONCANONICAL for values >= p.
+__global__ void k_fr_to_mont(Fr* v, size_t n, uint32_t* flags);
+
+// Canonical 64-byte points (host) -> device affine Montgomery, validated.
+void upload_points(Ctx& c, const uint8_t* host, size_t n, Affine* dst);
+// Device affine Montgomery -> canonical 64-byte points (host).
+void download_points(Ctx& c, const Affine* src, size_t n, uint8_t* host);
+// SRS [tau^i]G for i < n, generated on the device.
+void generate_srs(Ctx& c, const uint8_t tau_canonical[32], size_t n, Affine* dst);
+
+// Pippenger over device inputs; the result (canonical affine bytes, 64) is
+// written to device memory `out64` when non-null and returned to `host_out`
+// when non-null.
+struct MsmPlan {
+  int c;         // window width
+  int windows;   // signed-digit windows
+  bool precomp;  // read bases from an SRS window table
+};
+MsmPlan msm_plan(size_t n, bool small_scalars, const SrsTable* table);
+void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* scalars, bool small_scalars,
+                bool scalars_canonical, size_t n, uint8_t* out64_device, uint8_t* host_out);
+const SrsTable* srs_table(Ctx& c, int cbits, size_t need);
+
+}  // namespace apg

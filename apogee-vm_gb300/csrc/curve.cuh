@@ -1,0 +1,173 @@
+// BN254 G1 (y^2 = x^3 + 3 over Fq) for the MSM: affine bases and XYZZ
+// accumulators.
+//
+// XYZZ coordinates (X, Y, ZZ, ZZZ) stand for (X/ZZ, Y/ZZZ) with ZZ^3 = ZZZ^2;
+// ZZ = 0 is the point at infinity. The formulas are the published ones for
+// a = 0 short Weierstrass curves: madd-2008-s (8M + 2S, the bucket hot path),
+// add-2008-s (12M + 2S), dbl-2008-s-1 and mdbl-2008-s-1. The reference keeps
+// Jacobian coordinates (crates/curve/src/g1.rs:155-277); an MSM's value does
+// not depend on the coordinates, and every result leaves the device as the
+// canonical affine encoding (g1.rs:92-100), so parity is compared there.
+//
+// Device affine points carry Montgomery coordinates; (0, 0), which is not on
+// the curve, encodes infinity.
+#pragma once
+#include "field.cuh"
+
+namespace apg {
+
+struct Affine {
+  Fq x, y;
+};
+
+struct Xyzz {
+  Fq x, y, zz, zzz;
+};
+
+__device__ __forceinline__ bool aff_is_inf(const Affine& p) { return fe_is_zero(p.x) && fe_is_zero(p.y); }
+
+__device__ __forceinline__ Xyzz xyzz_inf() {
+  Xyzz r;
+  r.x = fe_zero<FqConsts>();
+  r.y = fe_zero<FqConsts>();
+  r.zz = fe_zero<FqConsts>();
+  r.zzz = fe_zero<FqConsts>();
+  return r;
+}
+
+__device__ __forceinline__ bool xyzz_is_inf(const Xyzz& p) { return fe_is_zero(p.zz); }
+
+__device__ __forceinline__ Xyzz xyzz_from_affine(const Affine& a) {
+  if (aff_is_inf(a)) return xyzz_inf();
+  Xyzz r;
+  r.x = a.x;
+  r.y = a.y;
+  r.zz = fe_one<FqConsts>();
+  r.zzz = fe_one<FqConsts>();
+  return r;
+}
+
+// mdbl-2008-s-1: 2 * (x, y) for an affine finite point.
+__device__ __forceinline__ Xyzz xyzz_dbl_affine(const Affine& a) {
+  Fq u = fe_dbl(a.y);
+  Fq v = fe_sqr(u);
+  Fq w = fe_mul(u, v);
+  Fq s = fe_mul(a.x, v);
+  Fq x2 = fe_sqr(a.x);
+  Fq m = fe_add(fe_dbl(x2), x2);
+  Xyzz r;
+  r.x = fe_sub(fe_sub(fe_sqr(m), s), s);
+  r.y = fe_sub(fe_mul(m, fe_sub(s, r.x)), fe_mul(w, a.y));
+  r.zz = v;
+  r.zzz = w;
+  return r;
+}
+
+// dbl-2008-s-1.
+__device__ __forceinline__ Xyzz xyzz_dbl(const Xyzz& p) {
+  if (xyzz_is_inf(p)) return p;
+  Fq u = fe_dbl(p.y);
+  Fq v = fe_sqr(u);
+  Fq w = fe_mul(u, v);
+  Fq s = fe_mul(p.x, v);
+  Fq x2 = fe_sqr(p.x);
+  Fq m = fe_add(fe_dbl(x2), x2);
+  Xyzz r;
+  r.x = fe_sub(fe_sub(fe_sqr(m), s), s);
+  r.y = fe_sub(fe_mul(m, fe_sub(s, r.x)), fe_mul(w, p.y));
+  r.zz = fe_mul(v, p.zz);
+  r.zzz = fe_mul(w, p.zzz);
+  return r;
+}
+
+// madd-2008-s: acc + (x2, y2), the affine point assumed finite.
+__device__ __forceinline__ Xyzz xyzz_add_affine(const Xyzz& p, const Affine& a) {
+  if (xyzz_is_inf(p)) return xyzz_from_affine(a);
+  Fq u2 = fe_mul(a.x, p.zz);
+  Fq s2 = fe_mul(a.y, p.zzz);
+  Fq pp_ = fe_sub(u2, p.x);
+  Fq r = fe_sub(s2, p.y);
+  if (fe_is_zero(pp_)) {
+    if (fe_is_zero(r)) return xyzz_dbl_affine(a);
+    return xyzz_inf();
+  }
+  Fq pp = fe_sqr(pp_);
+  Fq ppp = fe_mul(pp_, pp);
+  Fq q = fe_mul(p.x, pp);
+  Xyzz o;
+  o.x = fe_sub(fe_sub(fe_sub(fe_sqr(r), ppp), q), q);
+  o.y = fe_sub(fe_mul(r, fe_sub(q, o.x)), fe_mul(p.y, ppp));
+  o.zz = fe_mul(p.zz, pp);
+  o.zzz = fe_mul(p.zzz, ppp);
+  return o;
+}
+
+// add-2008-s.
+__device__ __forceinline__ Xyzz xyzz_add(const Xyzz& p, const Xyzz& q) {
+  if (xyzz_is_inf(p)) return q;
+  if (xyzz_is_inf(q)) return p;
+  Fq u1 = fe_mul(p.x, q.zz);
+  Fq u2 = fe_mul(q.x, p.zz);
+  Fq s1 = fe_mul(p.y, q.zzz);
+  Fq s2 = fe_mul(q.y, p.zzz);
+  Fq pp_ = fe_sub(u2, u1);
+  Fq r = fe_sub(s2, s1);
+  if (fe_is_zero(pp_)) {
+    if (fe_is_zero(r)) return xyzz_dbl(p);
+    return xyzz_inf();
+  }
+  Fq pp = fe_sqr(pp_);
+  Fq ppp = fe_mul(pp_, pp);
+  Fq qq = fe_mul(u1, pp);
+  Xyzz o;
+  o.x = fe_sub(fe_sub(fe_sub(fe_sqr(r), ppp), qq), qq);
+  o.y = fe_sub(fe_mul(r, fe_sub(qq, o.x)), fe_mul(s1, ppp));
+  o.zz = fe_mul(fe_mul(p.zz, q.zz), pp);
+  o.zzz = fe_mul(fe_mul(p.zzz, q.zzz), ppp);
+  return o;
+}
+
+__device__ __forceinline__ Xyzz xyzz_neg(const Xyzz& p) {
+  Xyzz r = p;
+  r.y = fe_neg(p.y);
+  return r;
+}
+
+// XYZZ -> affine (Montgomery); infinity -> (0, 0). One inversion.
+__device__ __forceinline__ Affine xyzz_to_affine(const Xyzz& p) {
+  Affine a;
+  if (xyzz_is_inf(p)) {
+    a.x = fe_zero<FqConsts>();
+    a.y = fe_zero<FqConsts>();
+    return a;
+  }
+  Fq t = fe_inverse(fe_mul(p.zz, p.zzz));
+  a.x = fe_mul(p.x, fe_mul(t, p.zzz));
+  a.y = fe_mul(p.y, fe_mul(t, p.zz));
+  return a;
+}
+
+__device__ __forceinline__ Affine ld_affine(const Affine* p) {
+  Affine a;
+  a.x = ld_fe(&p->x);
+  a.y = ld_fe(&p->y);
+  return a;
+}
+
+__device__ __forceinline__ Xyzz ld_xyzz(const Xyzz* p) {
+  Xyzz a;
+  a.x = ld_fe(&p->x);
+  a.y = ld_fe(&p->y);
+  a.zz = ld_fe(&p->zz);
+  a.zzz = ld_fe(&p->zzz);
+  return a;
+}
+
+__device__ __forceinline__ void st_xyzz(Xyzz* p, const Xyzz& a) {
+  st_fe(&p->x, a.x);
+  st_fe(&p->y, a.y);
+  st_fe(&p->zz, a.zz);
+  st_fe(&p->zzz, a.zzz);
+}
+
+}  // namespace apg

@@ -1,0 +1,323 @@
+// BN254 Fr / Fq arithmetic for sm_103a: 8 x 32-bit little-endian limbs in
+// Montgomery form with R = 2^256, byte-identical to the reference's in-memory
+// 4 x 64-bit representation (crates/field/src/lib.rs:30-36, 321), so a
+// caller's `&[Fr]` crosses the C ABI with no conversion.
+//
+// The multiply is CIOS on the integer multiply pipe: per limb of b, one
+// mad.lo / mad.hi carry chain accumulates a*b_i and one accumulates m*p,
+// 35 IMADs a limb, 280 a product, then one conditional subtraction. With
+// a, b < m < 2^254 the accumulator stays below 2m < 2^255 between limbs and
+// below 2^288 inside one, so nine 32-bit words always hold it.
+#pragma once
+#include <cstdint>
+
+namespace apg {
+
+struct FrConsts {
+  static constexpr uint32_t P0 = 0xf0000001u, P1 = 0x43e1f593u, P2 = 0x79b97091u, P3 = 0x2833e848u,
+                            P4 = 0x8181585du, P5 = 0xb85045b6u, P6 = 0xe131a029u, P7 = 0x30644e72u;
+  static constexpr uint32_t INV = 0xefffffffu;  // -p^-1 mod 2^32
+  __host__ __device__ static constexpr uint32_t R(int i) {
+    return (const uint32_t[8]){0x4ffffffbu, 0xac96341cu, 0x9f60cd29u, 0x36fc7695u,
+                               0x7879462eu, 0x666ea36fu, 0x9a07df2fu, 0x0e0a77c1u}[i];
+  }
+  __host__ __device__ static constexpr uint32_t R2(int i) {
+    return (const uint32_t[8]){0xae216da7u, 0x1bb8e645u, 0xe35c59e3u, 0x53fe3ab1u,
+                               0x53bb8085u, 0x8c49833du, 0x7f4e44a5u, 0x0216d0b1u}[i];
+  }
+};
+
+struct FqConsts {
+  static constexpr uint32_t P0 = 0xd87cfd47u, P1 = 0x3c208c16u, P2 = 0x6871ca8du, P3 = 0x97816a91u,
+                            P4 = 0x8181585du, P5 = 0xb85045b6u, P6 = 0xe131a029u, P7 = 0x30644e72u;
+  static constexpr uint32_t INV = 0xe4866389u;  // -q^-1 mod 2^32
+  __host__ __device__ static constexpr uint32_t R(int i) {
+    return (const uint32_t[8]){0xc58f0d9du, 0xd35d438du, 0xf5c70b3du, 0x0a78eb28u,
+                               0x7879462cu, 0x666ea36fu, 0x9a07df2fu, 0x0e0a77c1u}[i];
+  }
+  __host__ __device__ static constexpr uint32_t R2(int i) {
+    return (const uint32_t[8]){0x538afa89u, 0xf32cfc5bu, 0xd44501fbu, 0xb5e71911u,
+                               0x0a417ff6u, 0x47ab1effu, 0xcab8351fu, 0x06d89f71u}[i];
+  }
+};
+
+template <class C>
+struct Fe {
+  uint32_t v[8];
+};
+
+typedef Fe<FrConsts> Fr;
+typedef Fe<FqConsts> Fq;
+
+template <class C>
+__host__ __device__ __forceinline__ Fe<C> fe_zero() {
+  Fe<C> r;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.v[i] = 0;
+  return r;
+}
+
+template <class C>
+__host__ __device__ __forceinline__ Fe<C> fe_one() {
+  Fe<C> r;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.v[i] = C::R(i);
+  return r;
+}
+
+template <class C>
+__device__ __forceinline__ bool fe_is_zero(const Fe<C>& a) {
+  return (a.v[0] | a.v[1] | a.v[2] | a.v[3] | a.v[4] | a.v[5] | a.v[6] | a.v[7]) == 0;
+}
+
+template <class C>
+__device__ __forceinline__ bool fe_eq(const Fe<C>& a, const Fe<C>& b) {
+  uint32_t d = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) d |= a.v[i] ^ b.v[i];
+  return d == 0;
+}
+
+// r = a - m if a >= m (a < 2m): subtract, keep the difference unless it borrowed.
+template <class C>
+__device__ __forceinline__ void fe_reduce_once(uint32_t r[8]) {
+  uint32_t s0, s1, s2, s3, s4, s5, s6, s7, br;
+  asm("sub.cc.u32  %0, %9, %17;\n\t"
+      "subc.cc.u32 %1, %10, %18;\n\t"
+      "subc.cc.u32 %2, %11, %19;\n\t"
+      "subc.cc.u32 %3, %12, %20;\n\t"
+      "subc.cc.u32 %4, %13, %21;\n\t"
+      "subc.cc.u32 %5, %14, %22;\n\t"
+      "subc.cc.u32 %6, %15, %23;\n\t"
+      "subc.cc.u32 %7, %16, %24;\n\t"
+      "subc.u32    %8, 0, 0;"
+      : "=r"(s0), "=r"(s1), "=r"(s2), "=r"(s3), "=r"(s4), "=r"(s5), "=r"(s6), "=r"(s7), "=r"(br)
+      : "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+        "n"(C::P0), "n"(C::P1), "n"(C::P2), "n"(C::P3), "n"(C::P4), "n"(C::P5), "n"(C::P6), "n"(C::P7));
+  const bool keep = br != 0;
+  r[0] = keep ? r[0] : s0;
+  r[1] = keep ? r[1] : s1;
+  r[2] = keep ? r[2] : s2;
+  r[3] = keep ? r[3] : s3;
+  r[4] = keep ? r[4] : s4;
+  r[5] = keep ? r[5] : s5;
+  r[6] = keep ? r[6] : s6;
+  r[7] = keep ? r[7] : s7;
+}
+
+template <class C>
+__device__ __forceinline__ Fe<C> fe_add(const Fe<C>& a, const Fe<C>& b) {
+  Fe<C> r;
+  asm("add.cc.u32  %0, %8, %16;\n\t"
+      "addc.cc.u32 %1, %9, %17;\n\t"
+      "addc.cc.u32 %2, %10, %18;\n\t"
+      "addc.cc.u32 %3, %11, %19;\n\t"
+      "addc.cc.u32 %4, %12, %20;\n\t"
+      "addc.cc.u32 %5, %13, %21;\n\t"
+      "addc.cc.u32 %6, %14, %22;\n\t"
+      "addc.u32    %7, %15, %23;"
+      : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3]), "=r"(r.v[4]), "=r"(r.v[5]), "=r"(r.v[6]),
+        "=r"(r.v[7])
+      : "r"(a.v[0]), "r"(a.v[1]), "r"(a.v[2]), "r"(a.v[3]), "r"(a.v[4]), "r"(a.v[5]), "r"(a.v[6]), "r"(a.v[7]),
+        "r"(b.v[0]), "r"(b.v[1]), "r"(b.v[2]), "r"(b.v[3]), "r"(b.v[4]), "r"(b.v[5]), "r"(b.v[6]), "r"(b.v[7]));
+  fe_reduce_once<C>(r.v);
+  return r;
+}
+
+template <class C>
+__device__ __forceinline__ Fe<C> fe_sub(const Fe<C>& a, const Fe<C>& b) {
+  Fe<C> r;
+  uint32_t br;
+  asm("sub.cc.u32  %0, %9, %17;\n\t"
+      "subc.cc.u32 %1, %10, %18;\n\t"
+      "subc.cc.u32 %2, %11, %19;\n\t"
+      "subc.cc.u32 %3, %12, %20;\n\t"
+      "subc.cc.u32 %4, %13, %21;\n\t"
+      "subc.cc.u32 %5, %14, %22;\n\t"
+      "subc.cc.u32 %6, %15, %23;\n\t"
+      "subc.cc.u32 %7, %16, %24;\n\t"
+      "subc.u32    %8, 0, 0;"
+      : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3]), "=r"(r.v[4]), "=r"(r.v[5]), "=r"(r.v[6]),
+        "=r"(r.v[7]), "=r"(br)
+      : "r"(a.v[0]), "r"(a.v[1]), "r"(a.v[2]), "r"(a.v[3]), "r"(a.v[4]), "r"(a.v[5]), "r"(a.v[6]), "r"(a.v[7]),
+        "r"(b.v[0]), "r"(b.v[1]), "r"(b.v[2]), "r"(b.v[3]), "r"(b.v[4]), "r"(b.v[5]), "r"(b.v[6]), "r"(b.v[7]));
+  // On borrow add the modulus back (masked add: br is 0 or all ones).
+  asm("add.cc.u32  %0, %0, %8;\n\t"
+      "addc.cc.u32 %1, %1, %9;\n\t"
+      "addc.cc.u32 %2, %2, %10;\n\t"
+      "addc.cc.u32 %3, %3, %11;\n\t"
+      "addc.cc.u32 %4, %4, %12;\n\t"
+      "addc.cc.u32 %5, %5, %13;\n\t"
+      "addc.cc.u32 %6, %6, %14;\n\t"
+      "addc.u32    %7, %7, %15;"
+      : "+r"(r.v[0]), "+r"(r.v[1]), "+r"(r.v[2]), "+r"(r.v[3]), "+r"(r.v[4]), "+r"(r.v[5]), "+r"(r.v[6]),
+        "+r"(r.v[7])
+      : "r"(br & C::P0), "r"(br & C::P1), "r"(br & C::P2), "r"(br & C::P3), "r"(br & C::P4), "r"(br & C::P5),
+        "r"(br & C::P6), "r"(br & C::P7));
+  return r;
+}
+
+template <class C>
+__device__ __forceinline__ Fe<C> fe_neg(const Fe<C>& a) {
+  return fe_is_zero(a) ? a : fe_sub(fe_zero<C>(), a);
+}
+
+template <class C>
+__device__ __forceinline__ Fe<C> fe_dbl(const Fe<C>& a) {
+  return fe_add(a, a);
+}
+
+// One CIOS step: t += a * bi; m = t0 * inv; t += m * p; t >>= 32.
+#define APG_CIOS_STEP(BI)                                                                                    \
+  asm("{\n\t"                                                                                              \
+      ".reg .u32 m;\n\t"                                                                                   \
+      "mad.lo.cc.u32  %0, %9, %17, %0;\n\t"                                                                \
+      "madc.lo.cc.u32 %1, %10, %17, %1;\n\t"                                                               \
+      "madc.lo.cc.u32 %2, %11, %17, %2;\n\t"                                                               \
+      "madc.lo.cc.u32 %3, %12, %17, %3;\n\t"                                                               \
+      "madc.lo.cc.u32 %4, %13, %17, %4;\n\t"                                                               \
+      "madc.lo.cc.u32 %5, %14, %17, %5;\n\t"                                                               \
+      "madc.lo.cc.u32 %6, %15, %17, %6;\n\t"                                                               \
+      "madc.lo.cc.u32 %7, %16, %17, %7;\n\t"                                                               \
+      "addc.u32       %8, %8, 0;\n\t"                                                                      \
+      "mad.hi.cc.u32  %1, %9, %17, %1;\n\t"                                                                \
+      "madc.hi.cc.u32 %2, %10, %17, %2;\n\t"                                                               \
+      "madc.hi.cc.u32 %3, %11, %17, %3;\n\t"                                                               \
+      "madc.hi.cc.u32 %4, %12, %17, %4;\n\t"                                                               \
+      "madc.hi.cc.u32 %5, %13, %17, %5;\n\t"                                                               \
+      "madc.hi.cc.u32 %6, %14, %17, %6;\n\t"                                                               \
+      "madc.hi.cc.u32 %7, %15, %17, %7;\n\t"                                                               \
+      "madc.hi.u32    %8, %16, %17, %8;\n\t"                                                               \
+      "mul.lo.u32     m, %0, %18;\n\t"                                                                     \
+      "mad.lo.cc.u32  %0, m, %19, %0;\n\t"                                                                 \
+      "madc.lo.cc.u32 %1, m, %20, %1;\n\t"                                                                 \
+      "madc.lo.cc.u32 %2, m, %21, %2;\n\t"                                                                 \
+      "madc.lo.cc.u32 %3, m, %22, %3;\n\t"                                                                 \
+      "madc.lo.cc.u32 %4, m, %23, %4;\n\t"                                                                 \
+      "madc.lo.cc.u32 %5, m, %24, %5;\n\t"                                                                 \
+      "madc.lo.cc.u32 %6, m, %25, %6;\n\t"                                                                 \
+      "madc.lo.cc.u32 %7, m, %26, %7;\n\t"                                                                 \
+      "addc.u32       %8, %8, 0;\n\t"                                                                      \
+      "mad.hi.cc.u32  %1, m, %19, %1;\n\t"                                                                 \
+      "madc.hi.cc.u32 %2, m, %20, %2;\n\t"                                                                 \
+      "madc.hi.cc.u32 %3, m, %21, %3;\n\t"                                                                 \
+      "madc.hi.cc.u32 %4, m, %22, %4;\n\t"                                                                 \
+      "madc.hi.cc.u32 %5, m, %23, %5;\n\t"                                                                 \
+      "madc.hi.cc.u32 %6, m, %24, %6;\n\t"                                                                 \
+      "madc.hi.cc.u32 %7, m, %25, %7;\n\t"                                                                 \
+      "madc.hi.u32    %8, m, %26, %8;\n\t"                                                                 \
+      "}"                                                                                                  \
+      : "+r"(t0), "+r"(t1), "+r"(t2), "+r"(t3), "+r"(t4), "+r"(t5), "+r"(t6), "+r"(t7), "+r"(t8)            \
+      : "r"(a.v[0]), "r"(a.v[1]), "r"(a.v[2]), "r"(a.v[3]), "r"(a.v[4]), "r"(a.v[5]), "r"(a.v[6]),          \
+        "r"(a.v[7]), "r"(BI), "n"(C::INV), "n"(C::P0), "n"(C::P1), "n"(C::P2), "n"(C::P3), "n"(C::P4),      \
+        "n"(C::P5), "n"(C::P6), "n"(C::P7));                                                               \
+  t0 = t1;                                                                                                 \
+  t1 = t2;                                                                                                 \
+  t2 = t3;                                                                                                 \
+  t3 = t4;                                                                                                 \
+  t4 = t5;                                                                                                 \
+  t5 = t6;                                                                                                 \
+  t6 = t7;                                                                                                 \
+  t7 = t8;                                                                                                 \
+  t8 = 0;
+
+template <class C>
+__device__ __forceinline__ Fe<C> fe_mul(const Fe<C>& a, const Fe<C>& b) {
+  uint32_t t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, t5 = 0, t6 = 0, t7 = 0, t8 = 0;
+  APG_CIOS_STEP(b.v[0])
+  APG_CIOS_STEP(b.v[1])
+  APG_CIOS_STEP(b.v[2])
+  APG_CIOS_STEP(b.v[3])
+  APG_CIOS_STEP(b.v[4])
+  APG_CIOS_STEP(b.v[5])
+  APG_CIOS_STEP(b.v[6])
+  APG_CIOS_STEP(b.v[7])
+  Fe<C> r;
+  r.v[0] = t0;
+  r.v[1] = t1;
+  r.v[2] = t2;
+  r.v[3] = t3;
+  r.v[4] = t4;
+  r.v[5] = t5;
+  r.v[6] = t6;
+  r.v[7] = t7;
+  fe_reduce_once<C>(r.v);
+  return r;
+}
+
+template <class C>
+__device__ __forceinline__ Fe<C> fe_sqr(const Fe<C>& a) {
+  return fe_mul(a, a);
+}
+
+// Montgomery form -> canonical limbs (multiply by 1), and back (multiply by R^2).
+template <class C>
+__device__ __forceinline__ Fe<C> fe_from_mont(const Fe<C>& a) {
+  Fe<C> one = fe_zero<C>();
+  one.v[0] = 1;
+  return fe_mul(a, one);
+}
+
+template <class C>
+__device__ __forceinline__ Fe<C> fe_to_mont(const Fe<C>& a) {
+  Fe<C> r2;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r2.v[i] = C::R2(i);
+  return fe_mul(a, r2);
+}
+
+template <class C>
+__device__ __forceinline__ Fe<C> fe_from_u64(uint64_t x) {
+  Fe<C> a = fe_zero<C>();
+  a.v[0] = (uint32_t)x;
+  a.v[1] = (uint32_t)(x >> 32);
+  return fe_to_mont(a);
+}
+
+// Canonical value < m? (used to validate inputs arriving in canonical form)
+template <class C>
+__device__ __forceinline__ bool fe_lt_mod(const uint32_t a[8]) {
+  const uint32_t p[8] = {C::P0, C::P1, C::P2, C::P3, C::P4, C::P5, C::P6, C::P7};
+#pragma unroll
+  for (int i = 7; i >= 0; --i) {
+    if (a[i] != p[i]) return a[i] < p[i];
+  }
+  return false;
+}
+
+// a^(m-2) by a fixed square-and-multiply over the exponent's bits.
+template <class C>
+__device__ __noinline__ Fe<C> fe_inverse(const Fe<C>& a) {
+  const uint32_t p[8] = {C::P0, C::P1, C::P2, C::P3, C::P4, C::P5, C::P6, C::P7};
+  uint32_t e[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) e[i] = p[i];
+  e[0] -= 2;  // P0 is odd and > 2 for both moduli: no borrow
+  Fe<C> acc = fe_one<C>();
+  for (int i = 7; i >= 0; --i) {
+    for (int b = 31; b >= 0; --b) {
+      acc = fe_sqr(acc);
+      if ((e[i] >> b) & 1) acc = fe_mul(acc, a);
+    }
+  }
+  return acc;
+}
+
+template <class C>
+__device__ __forceinline__ Fe<C> ld_fe(const Fe<C>* p) {
+  const uint4* q = reinterpret_cast<const uint4*>(p);
+  uint4 x = q[0], y = q[1];
+  Fe<C> r;
+  r.v[0] = x.x; r.v[1] = x.y; r.v[2] = x.z; r.v[3] = x.w;
+  r.v[4] = y.x; r.v[5] = y.y; r.v[6] = y.z; r.v[7] = y.w;
+  return r;
+}
+
+template <class C>
+__device__ __forceinline__ void st_fe(Fe<C>* p, const Fe<C>& a) {
+  uint4* q = reinterpret_cast<uint4*>(p);
+  q[0] = make_uint4(a.v[0], a.v[1], a.v[2], a.v[3]);
+  q[1] = make_uint4(a.v[4], a.v[5], a.v[6], a.v[7]);
+}
+
+}  // namespace apg

@@ -1,0 +1,581 @@
+// Pippenger MSM on sm_103a (replaces crates/curve/src/msm.rs:48-311).
+//
+// Pipeline, all on the context's stream:
+//  1. k_recode      one thread per scalar: Montgomery -> canonical, signed
+//                   c-bit digits in [-2^(c-1), 2^(c-1)] (the reference's
+//                   recoding rule, msm.rs:180-198), one packed entry per
+//                   nonzero digit and a histogram of bucket occupancy.
+//  2. scan+scatter  a counting sort of the entries by bucket.
+//  3. k_accumulate  load-balanced bucket accumulation: every thread owns a
+//                   fixed-length segment of the sorted list and folds each run
+//                   of equal buckets into an XYZZ accumulator with mixed adds;
+//                   runs cut by a segment edge are stitched by k_fixup.
+//  4. k_level/k_sum bucket reduction sum_k k*B_k as a tree of running sums.
+//  5. k_finish      combine windows (Horner) or, with a precomputed SRS window
+//                   table, nothing: there every window shares one bucket set
+//                   because the table already holds 2^(c*w) * P_i.
+//  6. normalise to the canonical affine encoding.
+#include "common.cuh"
+
+namespace apg {
+
+namespace {
+
+constexpr int kLevelFan = 8;  // buckets folded per thread in one reduction level
+
+__device__ __forceinline__ void raise_flag(uint32_t* flags, uint32_t f) { atomicOr(flags, f); }
+
+__device__ __forceinline__ Fq fq_const_u32(uint32_t v) {
+  Fq a = fe_zero<FqConsts>();
+  a.v[0] = v;
+  return fe_to_mont(a);
+}
+
+__device__ __forceinline__ Affine generator_affine() {
+  Affine g;
+  g.x = fe_one<FqConsts>();
+  g.y = fq_const_u32(2);
+  return g;
+}
+
+__device__ __forceinline__ bool on_curve(const Affine& p) {
+  Fq rhs = fe_add(fe_mul(fe_sqr(p.x), p.x), fq_const_u32(3));
+  return fe_eq(fe_sqr(p.y), rhs);
+}
+
+// ---- point conversion -------------------------------------------------------
+
+__global__ void k_points_in(const uint4* raw, size_t n, Affine* dst, uint32_t* flags) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint4 q0 = raw[4 * i], q1 = raw[4 * i + 1], q2 = raw[4 * i + 2], q3 = raw[4 * i + 3];
+  uint32_t w[16] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w,
+                    q2.x, q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w};
+  uint32_t any = 0;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) any |= w[k];
+  Affine a;
+  if (any == 0) {
+    a.x = fe_zero<FqConsts>();
+    a.y = fe_zero<FqConsts>();
+  } else {
+    if (!fe_lt_mod<FqConsts>(w) || !fe_lt_mod<FqConsts>(w + 8)) raise_flag(flags, DEV_NONCANONICAL);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      a.x.v[k] = w[k];
+      a.y.v[k] = w[8 + k];
+    }
+    a.x = fe_to_mont(a.x);
+    a.y = fe_to_mont(a.y);
+    if (!on_curve(a)) raise_flag(flags, DEV_OFF_CURVE);
+  }
+  st_fe(&dst[i].x, a.x);
+  st_fe(&dst[i].y, a.y);
+}
+
+__global__ void k_points_out(const Affine* src, size_t n, uint4* raw) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Affine a = ld_affine(&src[i]);
+  Fq x = fe_from_mont(a.x), y = fe_from_mont(a.y);
+  raw[4 * i] = make_uint4(x.v[0], x.v[1], x.v[2], x.v[3]);
+  raw[4 * i + 1] = make_uint4(x.v[4], x.v[5], x.v[6], x.v[7]);
+  raw[4 * i + 2] = make_uint4(y.v[0], y.v[1], y.v[2], y.v[3]);
+  raw[4 * i + 3] = make_uint4(y.v[4], y.v[5], y.v[6], y.v[7]);
+}
+
+}  // namespace
+
+// Canonical Fr -> Montgomery in place, flagging values >= p.
+__global__ void k_fr_to_mont(Fr* v, size_t n, uint32_t* flags) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Fr a = ld_fe(&v[i]);
+  if (!fe_lt_mod<FrConsts>(a.v)) atomicOr(flags, (uint32_t)DEV_NONCANONICAL);
+  st_fe(&v[i], fe_to_mont(a));
+}
+
+namespace {
+
+// [tau^i] G by double-and-add over the canonical bits of tau^i.
+__global__ void k_srs_powers(Fr tau, size_t n, Affine* dst) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Fr s = fe_one<FrConsts>(), base = tau;
+  for (size_t e = i; e; e >>= 1) {
+    if (e & 1) s = fe_mul(s, base);
+    base = fe_sqr(base);
+  }
+  Fr sc = fe_from_mont(s);
+  const Affine g = generator_affine();
+  Xyzz acc = xyzz_inf();
+  for (int bit = 253; bit >= 0; --bit) {
+    acc = xyzz_dbl(acc);
+    if ((sc.v[bit >> 5] >> (bit & 31)) & 1) acc = xyzz_add_affine(acc, g);
+  }
+  Affine a = xyzz_to_affine(acc);
+  st_fe(&dst[i].x, a.x);
+  st_fe(&dst[i].y, a.y);
+}
+
+// tab[w*n + i] = 2^(c*w) * base[i].
+__global__ void k_window_table(const Affine* base, size_t n, int c, int windows, Affine* tab) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Affine cur = ld_affine(&base[i]);
+  st_fe(&tab[i].x, cur.x);
+  st_fe(&tab[i].y, cur.y);
+  for (int w = 1; w < windows; ++w) {
+    if (!aff_is_inf(cur)) {
+      Xyzz acc = xyzz_from_affine(cur);
+      for (int j = 0; j < c; ++j) acc = xyzz_dbl(acc);
+      cur = xyzz_to_affine(acc);
+    }
+    st_fe(&tab[(size_t)w * n + i].x, cur.x);
+    st_fe(&tab[(size_t)w * n + i].y, cur.y);
+  }
+}
+
+// ---- recode + histogram -------------------------------------------------------
+
+// Entry layout: bits 63..32 bucket (space*K + |d|-1), bit 31 negate, bits 30..0
+// base index. A zero digit writes kSkip and is not counted.
+constexpr uint64_t kSkip = ~0ull;
+
+template <bool SMALL>
+__global__ void k_recode(const void* scalars, size_t n, int c, int windows, int precomp, size_t tab_n,
+                         int canonical_in, uint64_t* entries, uint32_t* counts, uint32_t* flags) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t limbs[8];
+  if (SMALL) {
+    limbs[0] = reinterpret_cast<const uint32_t*>(scalars)[i];
+#pragma unroll
+    for (int k = 1; k < 8; ++k) limbs[k] = 0;
+  } else {
+    Fr s = ld_fe(reinterpret_cast<const Fr*>(scalars) + i);
+    if (!fe_lt_mod<FrConsts>(s.v)) raise_flag(flags, DEV_NONCANONICAL);
+    if (!canonical_in) s = fe_from_mont(s);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) limbs[k] = s.v[k];
+  }
+  const uint32_t K = 1u << (c - 1);
+  const uint32_t mask = (1u << c) - 1;
+  uint32_t carry = 0;
+  for (int w = 0; w < windows; ++w) {
+    int off = w * c;
+    uint32_t raw = 0;
+    if (off < 256) {
+      int limb = off >> 5, sh = off & 31;
+      uint64_t v = limbs[limb] >> sh;
+      if (limb + 1 < 8) v |= (uint64_t)limbs[limb + 1] << (32 - sh);
+      raw = (uint32_t)v & mask;
+    }
+    uint32_t coef = raw + carry;
+    uint32_t mag;
+    uint32_t neg = 0;
+    if (w == windows - 1 || coef < K) {
+      mag = coef;
+      carry = 0;
+    } else {
+      mag = (1u << c) - coef;  // digit coef - 2^c < 0
+      neg = 1;
+      carry = 1;
+    }
+    uint64_t e = kSkip;
+    if (mag) {
+      uint32_t space = precomp ? 0u : (uint32_t)w;
+      uint32_t bucket = space * K + (mag - 1);
+      uint64_t pidx = precomp ? (uint64_t)w * tab_n + i : i;
+      e = ((uint64_t)bucket << 32) | ((uint64_t)neg << 31) | pidx;
+      atomicAdd(&counts[bucket], 1u);
+    }
+    entries[(size_t)w * n + i] = e;
+  }
+}
+
+// ---- exclusive scan (u32), three passes ------------------------------------
+
+constexpr int kScanBlock = 1024;
+constexpr int kScanItems = 4;  // per thread
+
+__global__ void k_scan_local(uint32_t* data, size_t n, uint32_t* block_sums) {
+  __shared__ uint32_t sh[kScanBlock];
+  size_t base = (size_t)blockIdx.x * kScanBlock * kScanItems + (size_t)threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    v[k] = (base + k < n) ? data[base + k] : 0;
+    sum += v[k];
+  }
+  sh[threadIdx.x] = sum;
+  __syncthreads();
+  for (int off = 1; off < kScanBlock; off <<= 1) {
+    uint32_t t = threadIdx.x >= (unsigned)off ? sh[threadIdx.x - off] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += t;
+    __syncthreads();
+  }
+  uint32_t run = sh[threadIdx.x] - sum;  // exclusive prefix of this thread
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    if (base + k < n) data[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = sh[threadIdx.x];
+}
+
+// Exclusive scan of up to kScanBlock block sums in one block; total at [nb].
+__global__ void k_scan_blocks(uint32_t* block_sums, int nb) {
+  __shared__ uint32_t sh[kScanBlock];
+  uint32_t v = threadIdx.x < (unsigned)nb ? block_sums[threadIdx.x] : 0;
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int off = 1; off < kScanBlock; off <<= 1) {
+    uint32_t t = threadIdx.x >= (unsigned)off ? sh[threadIdx.x - off] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += t;
+    __syncthreads();
+  }
+  if (threadIdx.x < (unsigned)nb) block_sums[threadIdx.x] = sh[threadIdx.x] - v;
+  if (threadIdx.x == kScanBlock - 1) block_sums[nb] = sh[threadIdx.x];
+}
+
+__global__ void k_scan_add(uint32_t* data, size_t n, const uint32_t* block_sums, uint32_t* total_out) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) data[i] += block_sums[i / (kScanBlock * kScanItems)];
+  if (i == 0) *total_out = block_sums[(n + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems)];
+}
+
+__global__ void k_scatter(const uint64_t* entries, size_t e_count, uint32_t* cursor, uint64_t* sorted) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= e_count) return;
+  uint64_t e = entries[i];
+  if (e == kSkip) return;
+  uint32_t pos = atomicAdd(&cursor[e >> 32], 1u);
+  sorted[pos] = e;
+}
+
+// ---- accumulation -----------------------------------------------------------
+
+__device__ __forceinline__ Affine load_base(const Affine* bases, uint64_t e) {
+  Affine a = ld_affine(&bases[e & 0x7fffffffu]);
+  if ((e >> 31) & 1) a.y = fe_neg(a.y);
+  return a;
+}
+
+enum SegFlag : uint8_t { SEG_STARTS_BEFORE = 1, SEG_CONTINUES = 2, SEG_SINGLE_RUN = 4 };
+
+__global__ void __launch_bounds__(128) k_accumulate(const uint64_t* sorted, const uint32_t* total, int seg_len,
+                                                    size_t nseg, const Affine* bases, Xyzz* buckets, Xyzz* head,
+                                                    Xyzz* tail, uint8_t* seg_flags) {
+  size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const size_t E = *total;
+  const size_t lo = s * (size_t)seg_len;
+  if (lo >= E) {
+    seg_flags[s] = 0;
+    return;
+  }
+  const size_t hi = min(lo + (size_t)seg_len, E);
+  uint32_t cur = (uint32_t)(sorted[lo] >> 32);
+  const bool starts_before = lo > 0 && (uint32_t)(sorted[lo - 1] >> 32) == cur;
+  const bool continues = hi < E && (uint32_t)(sorted[hi] >> 32) == (uint32_t)(sorted[hi - 1] >> 32);
+  bool first_run = true;
+  Xyzz acc = xyzz_inf();
+  for (size_t i = lo; i < hi; ++i) {
+    uint64_t e = sorted[i];
+    uint32_t b = (uint32_t)(e >> 32);
+    if (b != cur) {
+      if (first_run && starts_before) st_xyzz(&head[s], acc);
+      else st_xyzz(&buckets[cur], acc);
+      first_run = false;
+      cur = b;
+      acc = xyzz_inf();
+    }
+    Affine p = load_base(bases, e);
+    if (!aff_is_inf(p)) acc = xyzz_add_affine(acc, p);
+  }
+  if (continues) {
+    if (first_run && starts_before) st_xyzz(&head[s], acc);
+    else st_xyzz(&tail[s], acc);
+  } else {
+    if (first_run && starts_before) st_xyzz(&head[s], acc);
+    else st_xyzz(&buckets[cur], acc);
+  }
+  seg_flags[s] = (starts_before ? SEG_STARTS_BEFORE : 0) | (continues ? SEG_CONTINUES : 0) |
+                 (first_run ? SEG_SINGLE_RUN : 0);
+}
+
+// A bucket whose run crosses segment edges: the segment where it starts sums
+// its tail with the heads of the segments it spills into.
+__global__ void k_fixup(const uint64_t* sorted, const uint32_t* total, int seg_len, size_t nseg,
+                        const uint8_t* seg_flags, const Xyzz* head, const Xyzz* tail, Xyzz* buckets) {
+  size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const size_t E = *total;
+  if (s * (size_t)seg_len >= E) return;
+  uint8_t f = seg_flags[s];
+  if (!(f & SEG_CONTINUES)) return;
+  if ((f & SEG_SINGLE_RUN) && (f & SEG_STARTS_BEFORE)) return;  // a middle piece
+  const size_t hi = min((s + 1) * (size_t)seg_len, E);
+  const uint32_t b = (uint32_t)(sorted[hi - 1] >> 32);
+  Xyzz acc = ld_xyzz(&tail[s]);
+  for (size_t t = s + 1; t < nseg; ++t) {
+    acc = xyzz_add(acc, ld_xyzz(&head[t]));
+    uint8_t g = seg_flags[t];
+    if ((g & SEG_SINGLE_RUN) && (g & SEG_CONTINUES)) continue;
+    break;
+  }
+  st_xyzz(&buckets[b], acc);
+}
+
+// ---- bucket reduction -------------------------------------------------------
+
+// in[space*M + k] has weight k+1. Group g of `fan` buckets yields
+// T_g = sum_j (j+1) in[g*fan + j] and R_g = sum_j in[g*fan + j]; the next
+// level takes R_1..R_{G-1} (weights 1..G-1) and an identity pad at weight G:
+//   sum_k k B_k = sum_g T_g + fan * sum_g g R_g.
+__global__ void k_level(const Xyzz* in, int M, int spaces, int fan, Xyzz* outT, Xyzz* outR) {
+  int G = (M + fan - 1) / fan;
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= spaces * G) return;
+  int sp = idx / G, g = idx % G;
+  int lo = g * fan, hi = min(lo + fan, M);
+  Xyzz run = xyzz_inf(), tot = xyzz_inf();
+  for (int k = hi - 1; k >= lo; --k) {
+    run = xyzz_add(run, ld_xyzz(&in[(size_t)sp * M + k]));
+    tot = xyzz_add(tot, run);
+  }
+  st_xyzz(&outT[(size_t)sp * G + g], tot);
+  if (g > 0) st_xyzz(&outR[(size_t)sp * G + g - 1], run);
+  else st_xyzz(&outR[(size_t)sp * G + G - 1], xyzz_inf());
+}
+
+// out[space] = sum of in[space*M .. space*M + M).
+__global__ void k_sum(const Xyzz* in, int M, Xyzz* out) {
+  __shared__ Xyzz sh[128];
+  int sp = blockIdx.x;
+  Xyzz acc = xyzz_inf();
+  for (int k = threadIdx.x; k < M; k += blockDim.x) acc = xyzz_add(acc, ld_xyzz(&in[(size_t)sp * M + k]));
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < (unsigned)off) sh[threadIdx.x] = xyzz_add(sh[threadIdx.x], sh[threadIdx.x + off]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) st_xyzz(&out[sp], sh[0]);
+}
+
+// tsum[level*spaces + sp] holds level sums; combine by Horner in `fan`, then
+// combine spaces (windows) by Horner in 2^c, normalise and write 64 bytes.
+__global__ void k_finish(const Xyzz* tsum, int levels, int spaces, int fan_log, int c, uint32_t* out64) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  Xyzz total = xyzz_inf();
+  for (int sp = spaces - 1; sp >= 0; --sp) {
+    for (int j = 0; j < c && sp != spaces - 1; ++j) total = xyzz_dbl(total);
+    Xyzz s = xyzz_inf();
+    for (int l = levels - 1; l >= 0; --l) {
+      for (int j = 0; j < fan_log && l != levels - 1; ++j) s = xyzz_dbl(s);
+      s = xyzz_add(s, ld_xyzz(&tsum[(size_t)l * spaces + sp]));
+    }
+    total = xyzz_add(total, s);
+  }
+  Affine a = xyzz_to_affine(total);
+  Fq x = fe_from_mont(a.x), y = fe_from_mont(a.y);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    out64[k] = x.v[k];
+    out64[8 + k] = y.v[k];
+  }
+}
+
+template <class T>
+inline unsigned blocks_for(size_t n, int threads) {
+  return (unsigned)((n + threads - 1) / threads);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+
+void upload_points(Ctx& c, const uint8_t* host, size_t n, Affine* dst) {
+  if (n == 0) return;
+  uint4* raw = c.scratch[S_TMP7].as<uint4>(4 * n);
+  APG_CUDA(cudaMemcpyAsync(raw, host, 64 * n, cudaMemcpyHostToDevice, c.stream));
+  k_points_in<<<blocks_for<int>(n, 256), 256, 0, c.stream>>>(raw, n, dst, c.d_flags);
+  APG_LAUNCH_CHECK();
+  c.check_flags();
+}
+
+void download_points(Ctx& c, const Affine* src, size_t n, uint8_t* host) {
+  if (n == 0) return;
+  uint4* raw = c.scratch[S_TMP7].as<uint4>(4 * n);
+  k_points_out<<<blocks_for<int>(n, 256), 256, 0, c.stream>>>(src, n, raw);
+  APG_LAUNCH_CHECK();
+  APG_CUDA(cudaMemcpyAsync(host, raw, 64 * n, cudaMemcpyDeviceToHost, c.stream));
+  APG_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+void generate_srs(Ctx& c, const uint8_t tau_canonical[32], size_t n, Affine* dst) {
+  Fr* d_tau = c.scratch[S_TMP6].as<Fr>(1);
+  APG_CUDA(cudaMemcpyAsync(d_tau, tau_canonical, 32, cudaMemcpyHostToDevice, c.stream));
+  k_fr_to_mont<<<1, 1, 0, c.stream>>>(d_tau, 1, c.d_flags);
+  APG_LAUNCH_CHECK();
+  c.check_flags();
+  Fr tau_mont;
+  APG_CUDA(cudaMemcpyAsync(&tau_mont, d_tau, 32, cudaMemcpyDeviceToHost, c.stream));
+  APG_CUDA(cudaStreamSynchronize(c.stream));
+  k_srs_powers<<<blocks_for<int>(n, 128), 128, 0, c.stream>>>(tau_mont, n, dst);
+  APG_LAUNCH_CHECK();
+  APG_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+static int default_window(size_t n, bool small) {
+  int lg = 0;
+  while (((size_t)1 << (lg + 1)) <= n) ++lg;
+  int cb;
+  if (lg <= 4) cb = 3;
+  else if (lg <= 8) cb = 5;
+  else if (lg <= 12) cb = 9;
+  else if (lg <= 16) cb = 12;
+  else if (lg <= 20) cb = 15;
+  else cb = 16;
+  if (small && cb > 11) cb = 11;  // 32-bit scalars: three windows
+  return cb;
+}
+
+static int window_count(int bits, int cb) { return (bits + 1 + cb - 1) / cb; }
+
+const SrsTable* srs_table(Ctx& c, int cbits, size_t need) {
+  for (auto& t : c.tables)
+    if (t.c == cbits && t.n >= need) return &t;
+  if (!c.srs || c.srs_n < need) return nullptr;
+  // Build over the whole SRS for the wide table, over a prefix for narrow ones.
+  size_t n = cbits >= 12 ? c.srs_n : std::min(c.srs_n, (size_t)1 << 16);
+  if (n < need) n = c.srs_n;
+  for (auto it = c.tables.begin(); it != c.tables.end(); ++it)
+    if (it->c == cbits) {
+      cudaFree(it->tab);
+      c.tables.erase(it);
+      break;
+    }
+  SrsTable t;
+  t.c = cbits;
+  t.windows = window_count(254, cbits);
+  t.n = n;
+  APG_CUDA(cudaMalloc(&t.tab, (size_t)t.windows * n * sizeof(Affine)));
+  k_window_table<<<blocks_for<int>(n, 128), 128, 0, c.stream>>>(c.srs, n, cbits, t.windows, t.tab);
+  APG_LAUNCH_CHECK();
+  APG_CUDA(cudaStreamSynchronize(c.stream));
+  c.tables.push_back(t);
+  return &c.tables.back();
+}
+
+MsmPlan msm_plan(size_t n, bool small_scalars, const SrsTable* table) {
+  MsmPlan p;
+  if (table) {
+    p.c = table->c;
+    p.windows = small_scalars ? window_count(32, table->c) : table->windows;
+    p.precomp = true;
+  } else {
+    p.c = default_window(n, small_scalars);
+    p.windows = window_count(small_scalars ? 32 : 254, p.c);
+    p.precomp = false;
+  }
+  return p;
+}
+
+void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* scalars, bool small_scalars,
+                bool scalars_canonical, size_t n, uint8_t* out64_device, uint8_t* host_out) {
+  if (n == 0) {
+    if (out64_device) APG_CUDA(cudaMemsetAsync(out64_device, 0, 64, c.stream));
+    if (host_out) memset(host_out, 0, 64);
+    return;
+  }
+  MsmPlan p = msm_plan(n, small_scalars, table);
+  const int K = 1 << (p.c - 1);
+  const int spaces = p.precomp ? 1 : p.windows;
+  const size_t nbins = (size_t)spaces * K;
+  const size_t E = (size_t)p.windows * n;
+  const Affine* src = p.precomp ? table->tab : bases;
+  const size_t tab_n = p.precomp ? table->n : 0;
+
+  uint64_t* entries = c.scratch[S_ENTRIES].as<uint64_t>(E);
+  uint64_t* sorted = c.scratch[S_SORTED].as<uint64_t>(E);
+  uint32_t* counts = c.scratch[S_COUNTS].as<uint32_t>(nbins + 1);
+  const size_t scan_blocks = (nbins + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems);
+  if (scan_blocks > (size_t)kScanBlock - 1) throw Error(APG_ERR_INVALID_ARGUMENT, "too many buckets");
+  uint32_t* blk = c.scratch[S_SCANBLK].as<uint32_t>(kScanBlock + 1);
+  uint32_t* total = c.scratch[S_OFFSETS].as<uint32_t>(1);
+  Xyzz* buckets = c.scratch[S_BUCKETS].as<Xyzz>(nbins);
+
+  APG_CUDA(cudaMemsetAsync(counts, 0, (nbins + 1) * sizeof(uint32_t), c.stream));
+  APG_CUDA(cudaMemsetAsync(buckets, 0, nbins * sizeof(Xyzz), c.stream));
+  if (small_scalars)
+    k_recode<true><<<blocks_for<int>(n, 256), 256, 0, c.stream>>>(scalars, n, p.c, p.windows, p.precomp, tab_n,
+                                                                   1, entries, counts, c.d_flags);
+  else
+    k_recode<false><<<blocks_for<int>(n, 256), 256, 0, c.stream>>>(scalars, n, p.c, p.windows, p.precomp, tab_n,
+                                                                    scalars_canonical ? 1 : 0, entries, counts,
+                                                                    c.d_flags);
+  APG_LAUNCH_CHECK();
+  k_scan_local<<<(unsigned)scan_blocks, kScanBlock, 0, c.stream>>>(counts, nbins, blk);
+  k_scan_blocks<<<1, kScanBlock, 0, c.stream>>>(blk, (int)scan_blocks);
+  k_scan_add<<<blocks_for<int>(nbins, 256), 256, 0, c.stream>>>(counts, nbins, blk, total);
+  k_scatter<<<blocks_for<int>(E, 256), 256, 0, c.stream>>>(entries, E, counts, sorted);
+  APG_LAUNCH_CHECK();
+
+  // Segments: enough threads to fill the chip several times over.
+  size_t target_threads = (size_t)c.sm_count * 1024;
+  int seg_len = (int)std::max<size_t>(4, std::min<size_t>(256, E / std::max<size_t>(target_threads, 1)));
+  size_t nseg = (E + seg_len - 1) / seg_len;
+  Xyzz* head = c.scratch[S_HEAD].as<Xyzz>(nseg);
+  Xyzz* tail = c.scratch[S_TAIL].as<Xyzz>(nseg);
+  uint8_t* flags = c.scratch[S_FLAGS].as<uint8_t>(nseg);
+  k_accumulate<<<blocks_for<int>(nseg, 128), 128, 0, c.stream>>>(sorted, total, seg_len, nseg, src, buckets, head,
+                                                                  tail, flags);
+  APG_LAUNCH_CHECK();
+  k_fixup<<<blocks_for<int>(nseg, 128), 128, 0, c.stream>>>(sorted, total, seg_len, nseg, flags, head, tail,
+                                                             buckets);
+  APG_LAUNCH_CHECK();
+
+  // Reduction levels.
+  int fan_log = 0;
+  while ((1 << fan_log) < kLevelFan) ++fan_log;
+  int levels = 0;
+  {
+    int M = K;
+    while (true) {
+      ++levels;
+      if (M <= kLevelFan) break;
+      M = (M + kLevelFan - 1) / kLevelFan;
+    }
+  }
+  Xyzz* tsum = c.scratch[S_TSUM].as<Xyzz>((size_t)levels * spaces);
+  Xyzz* lvl_in = buckets;
+  int M = K;
+  for (int l = 0; l < levels; ++l) {
+    int G = (M + kLevelFan - 1) / kLevelFan;
+    Xyzz* outT = c.scratch[S_LEVEL_T].as<Xyzz>((size_t)spaces * G);
+    Xyzz* outR = c.scratch[(l & 1) ? S_LEVEL_B : S_LEVEL_A].as<Xyzz>((size_t)spaces * G);
+    k_level<<<blocks_for<int>((size_t)spaces * G, 64), 64, 0, c.stream>>>(lvl_in, M, spaces, kLevelFan, outT, outR);
+    k_sum<<<spaces, 128, 0, c.stream>>>(outT, G, tsum + (size_t)l * spaces);
+    APG_LAUNCH_CHECK();
+    lvl_in = outR;
+    M = G;
+  }
+  uint32_t* res = c.scratch[S_RESULT].as<uint32_t>(16);
+  k_finish<<<1, 32, 0, c.stream>>>(tsum, levels, spaces, fan_log, p.c, out64_device ? (uint32_t*)out64_device : res);
+  APG_LAUNCH_CHECK();
+  if (host_out) {
+    APG_CUDA(cudaMemcpyAsync(host_out, out64_device ? (void*)out64_device : (void*)res, 64, cudaMemcpyDeviceToHost,
+                             c.stream));
+    c.check_flags();
+  }
+}
+
+}  // namespace apg

@@ -1,0 +1,126 @@
+/*
+ * apogee_gpu.h — the C ABI of the GB300 shard-proving hot path.
+ *
+ * A drop-in for the commit/open and sumcheck-prover interfaces that the
+ * reference's crates/prover calls: crates/curve (msm), crates/pcs (commit,
+ * open, batch_open), crates/sumcheck (prove_zerocheck) and crates/gkr
+ * (forward, prove). Each entry point below names the reference function it
+ * replaces (file:line, paths inside the reference project).
+ *
+ * Conventions (the reference's own, so a binding converts nothing):
+ *  - Fr in memory: 32 bytes, the four 64-bit Montgomery limbs little-endian,
+ *    exactly Fr::to_memory_bytes (crates/field/src/lib.rs:321); a `&[Fr]`
+ *    slice is passed as its data pointer.
+ *  - Fr on the wire (proof values, challenges, claims): 32 canonical
+ *    little-endian bytes, Fr::to_bytes (lib.rs:252).
+ *  - G1: 64 bytes x || y canonical little-endian, all-zero = infinity,
+ *    G1Affine::to_bytes (crates/curve/src/g1.rs:92-100).
+ *  - A transcript crosses as its 226-byte TranscriptSnapshot tuple
+ *    (state[3], input[2], input_len:u8, output[2], output_len:u8; Fr
+ *    canonical), in/out (crates/transcript/src/lib.rs:188-194, 353-376).
+ *  - Every function returns an apg_status; 0 is success. Nothing aborts the
+ *    caller's process; apg_last_error() describes the last failure.
+ *  - A context is thread-safe (calls on one context serialise); use one
+ *    context per concurrent caller to overlap work.
+ */
+#ifndef APOGEE_GPU_H
+#define APOGEE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct apg_ctx apg_ctx;
+
+/* Status codes. 1..9 mirror MsmError / PcsError variants
+ * (crates/curve/src/msm.rs:29-33, crates/pcs-verify/src/lib.rs:40-86). */
+enum apg_status {
+  APG_OK = 0,
+  APG_ERR_LENGTH_MISMATCH = 1,        /* MsmError::LengthMismatch */
+  APG_ERR_UNSUPPORTED_NUM_VARS = 2,   /* PcsError::UnsupportedNumVars */
+  APG_ERR_POINT_LENGTH_MISMATCH = 3,  /* PcsError::PointLengthMismatch */
+  APG_ERR_SRS_TOO_SMALL = 4,          /* PcsError::SrsTooSmall */
+  APG_ERR_DEGENERATE_CHALLENGE = 5,   /* PcsError::DegenerateChallenge */
+  APG_ERR_EMPTY_BATCH = 6,            /* PcsError::EmptyBatch */
+  APG_ERR_BATCH_LENGTH_MISMATCH = 7,  /* PcsError::BatchLengthMismatch */
+  APG_ERR_MIXED_COLUMN_SIZES = 8,     /* PcsError::MixedColumnSizes */
+  APG_ERR_INVALID_POINT = 9,          /* PcsError::InvalidPoint / off-curve input */
+  APG_ERR_NONCANONICAL = 20,          /* an input value is >= its modulus */
+  APG_ERR_INVALID_ARGUMENT = 21,      /* null pointer, bad shape */
+  APG_ERR_BAD_CIRCUIT = 22,           /* malformed circuit blob */
+  APG_ERR_NO_SRS = 23,                /* no SRS resident on the context */
+  APG_ERR_INTERNAL = 24,              /* a device invariant failed */
+  APG_ERR_CUDA = 100,                 /* a CUDA call failed */
+  APG_ERR_OUT_OF_MEMORY = 101,        /* device allocation refused */
+  APG_ERR_NO_DEVICE = 103             /* no usable CUDA device */
+};
+
+#define APG_TRANSCRIPT_BYTES 226
+#define APG_PROOF_BYTES 704
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Create a context on CUDA device `device` (one stream, its own scratch). */
+int apg_ctx_create(int device, apg_ctx** out);
+void apg_ctx_destroy(apg_ctx* ctx);
+/* The last failure's message on this context ("" if none). */
+const char* apg_last_error(apg_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that time or
+ * order work against it. */
+void* apg_ctx_stream(apg_ctx* ctx);
+/* Block until all work queued on the context has finished. */
+int apg_ctx_synchronize(apg_ctx* ctx);
+
+/* ---- SRS (crates/srs/src/lib.rs:96-100, 244: Srs::g1) ------------------- */
+
+/* Make `n` G1 powers resident on the device (canonical 64-byte points, each
+ * validated). Replaces handing `srs.g1()` to every commit. */
+int apg_srs_upload(apg_ctx* ctx, const uint8_t* g1_points, size_t n);
+/* Benchmark-only setup: [tau^i]G for i < n from a given tau (canonical Fr),
+ * computed on the device. Not a secure setup. */
+int apg_srs_generate(apg_ctx* ctx, const uint8_t tau[32], size_t n);
+/* Copy the first n resident powers out (canonical 64-byte points). */
+int apg_srs_download(apg_ctx* ctx, uint8_t* g1_points, size_t n);
+/* Number of resident powers. */
+size_t apg_srs_len(apg_ctx* ctx);
+/* Precompute the window table that commits over the resident SRS read
+ * (window width `cbits`, 0 = the library's choice). Optional: the first
+ * commit builds it. Costs windows x n x 64 bytes of device memory. */
+int apg_srs_prepare(apg_ctx* ctx, int cbits);
+
+/* ---- MSM (crates/curve/src/msm.rs) ------------------------------------- */
+
+/* msm::msm (msm.rs:48): sum scalars[i] * bases[i]. bases: canonical 64-byte
+ * points; scalars: Fr in memory (Montgomery). Lengths must match
+ * (APG_ERR_LENGTH_MISMATCH); empty input is the identity (64 zero bytes). */
+int apg_msm(apg_ctx* ctx, const uint8_t* bases, size_t n_bases, const uint8_t* scalars, size_t n_scalars,
+            uint8_t out[64]);
+/* msm::msm_small_u32 (msm.rs:79): the same over u32 scalars. */
+int apg_msm_small_u32(apg_ctx* ctx, const uint8_t* bases, size_t n_bases, const uint32_t* scalars,
+                      size_t n_scalars, uint8_t out[64]);
+
+/* ---- commit (crates/pcs/src/lib.rs:237-298) ---------------------------- */
+
+/* pcs::commit over the resident SRS: the KZG commitment to the 2^num_vars
+ * evaluations read as coefficients. evals: Fr in memory (Montgomery).
+ * Errors: APG_ERR_UNSUPPORTED_NUM_VARS (odd or out of 2..54),
+ * APG_ERR_SRS_TOO_SMALL, APG_ERR_NO_SRS. */
+int apg_commit(apg_ctx* ctx, const uint8_t* evals, size_t num_vars, uint8_t out[64]);
+/* pcs::commit of a narrow column (column_msm's U1/U8/U16/U32 arms,
+ * lib.rs:280-298): u32 values through the small-scalar path. */
+int apg_commit_u32(apg_ctx* ctx, const uint32_t* evals, size_t num_vars, uint8_t out[64]);
+/* commit_all (crates/prover/src/lib.rs:444-471): k columns of one size,
+ * cols[j] pointing at column j's evaluations (Fr in memory); out: k x 64. */
+int apg_commit_batch(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_t num_vars, uint8_t* out);
+/* As apg_commit, with the evaluations already in device memory (a pointer
+ * the caller allocated on this context's device). */
+int apg_commit_device(apg_ctx* ctx, const void* d_evals, size_t num_vars, uint8_t out[64]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* APOGEE_GPU_H */

@@ -1,0 +1,168 @@
+"""GPU parity of the MSM and commit paths against the oracle and the
+reference's committed MSM corpus (crates/curve/tests/vectors/msm_kats.txt).
+
+Every comparison is on the canonical affine bytes, which are
+representation-independent, so the device's XYZZ buckets and windows need
+not match the reference's Jacobian ones.
+"""
+import random
+
+import pytest
+
+import oracle_lib as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import apogee_gpu as A
+
+    with A.Context(0) as c:
+        yield c
+
+
+def mont(scalars_bytes: bytes) -> bytes:
+    import apogee_gpu as A
+
+    xs = [int.from_bytes(scalars_bytes[i:i + 32], "little") for i in range(0, len(scalars_bytes), 32)]
+    return A.to_mont_bytes(xs)
+
+
+def test_msm_kats(ctx):
+    checked = 0
+    for line in O.golden_lines("msm_kats.txt"):
+        f = line.split()
+        pattern, n, seed, want = f[1], int(f[2]), int(f[3]), f[4]
+        bases, scalars = O.msm_case(pattern, n, seed)
+        assert ctx.msm(bases, mont(scalars)).hex() == want, f"{pattern} n={n}"
+        checked += 1
+    assert checked == 13
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 32, 33, 100, 257, 1025, 5000])
+def test_msm_random_sizes_against_oracle(ctx, n):
+    bases, scalars = O.msm_case("random", n, 1000 + n)
+    assert ctx.msm(bases, mont(scalars)) == O.msm(bases, scalars, n, threads=8)
+
+
+def test_msm_length_mismatch_and_empty(ctx):
+    import apogee_gpu as A
+
+    bases, scalars = O.msm_case("random", 4, 5)
+    with pytest.raises(A.MsmError):
+        ctx.msm(bases, mont(scalars)[:96])
+    assert ctx.msm(b"", b"") == bytes(64)
+
+
+def test_msm_edge_scalars(ctx):
+    """0, 1, p-1 and top-window carries: scalars just below 2^254 and
+    values whose every window reaches the signed-digit threshold."""
+    n = 64
+    bases, _ = O.msm_case("random", n, 77)
+    edge = [0, 1, 2, O.P_R - 1, O.P_R - 2, (1 << 253), (1 << 253) + (1 << 252)]
+    edge += [int("8" * 63, 16) % O.P_R, int("7fff" * 16, 16) % O.P_R, int("ffff" * 15 + "0fff", 16) % O.P_R]
+    rng = random.Random(3)
+    scalars = edge + [rng.randrange(O.P_R) for _ in range(n - len(edge))]
+    sb = b"".join(O.fe(s) for s in scalars)
+    assert ctx.msm(bases, mont(sb)) == O.msm(bases, sb, n)
+
+
+def test_msm_rejects_noncanonical(ctx):
+    import apogee_gpu as A
+
+    bases, scalars = O.msm_case("random", 4, 6)
+    bad = bytearray(bases)
+    bad[64:96] = O.fe(O.P_Q)  # x = q is not a canonical coordinate
+    with pytest.raises(A.ApogeeError):
+        ctx.msm(bytes(bad), mont(scalars))
+    off = bytearray(bases)
+    off[0] ^= 1  # breaks the curve equation
+    with pytest.raises(A.PcsError):
+        ctx.msm(bytes(off), mont(scalars))
+    # and the context stays usable afterwards
+    assert ctx.msm(bases, mont(scalars)) == O.msm(bases, scalars, 4)
+
+
+def test_msm_small_u32(ctx):
+    n = 3000
+    bases, _ = O.msm_case("random", n, 8)
+    rng = random.Random(9)
+    vals = [rng.choice([0, 1, rng.getrandbits(8), rng.getrandbits(16), rng.getrandbits(32)]) for _ in range(n)]
+    vals[:4] = [0xFFFFFFFF, 0x80000000, 0x7FFFFFFF, 0]
+    sb = b"".join(O.fe(v) for v in vals)
+    assert ctx.msm_small_u32(bases, vals) == O.msm(bases, sb, n)
+
+
+def test_srs_generate_matches_oracle(ctx):
+    tau = 0xABCDEF
+    n = 300
+    ctx.srs_generate(tau, n)
+    assert ctx.srs_download(n) == O.toy_srs(tau, n)
+
+
+def test_commit_against_oracle_and_known_tau(ctx):
+    import ctypes
+
+    rng = O.Rng(2026)
+    tau = rng.next_fr()
+    nv = 10
+    n = 1 << nv
+    srs = O.toy_srs(tau, n)
+    ctx.srs_upload(srs)
+    coeffs = [rng.next_fr() for _ in range(n)]
+    cb = b"".join(O.fe(c) for c in coeffs)
+    cm = ctx.commit(mont(cb), nv)
+    want = O.buf(64)
+    assert O.lib().oracle_commit(srs, ctypes.c_size_t(n), cb, nv, 8, want) == 0
+    assert cm == want.raw
+    f_tau = sum(c * pow(tau, i, O.P_R) for i, c in enumerate(coeffs)) % O.P_R
+    assert cm == O.g1_mul(O.G1_GEN, f_tau)
+
+
+def test_commit_shape_errors(ctx):
+    import apogee_gpu as A
+
+    ctx.srs_generate(5, 64)
+    with pytest.raises(A.PcsError) as e:
+        ctx.commit(bytes(32 * 8), 3)
+    assert e.value.variant == "UnsupportedNumVars"
+    with pytest.raises(A.PcsError) as e:
+        ctx.commit(bytes(32 * 256), 8)
+    assert e.value.variant == "SrsTooSmall"
+
+
+def test_commit_u32_and_batch(ctx):
+    tau = 0x1234567
+    nv = 8
+    n = 1 << nv
+    ctx.srs_generate(tau, n)
+    rng = random.Random(11)
+    vals = [rng.getrandbits(32) for _ in range(n)]
+    f_tau = sum(v * pow(tau, i, O.P_R) for i, v in enumerate(vals)) % O.P_R
+    assert ctx.commit_u32(vals, nv) == O.g1_mul(O.G1_GEN, f_tau)
+    cols = [[rng.randrange(O.P_R) for _ in range(n)] for _ in range(3)]
+    import apogee_gpu as A
+
+    cms = ctx.commit_batch([A.to_mont_bytes(c) for c in cols], nv)
+    for c, cm in zip(cols, cms):
+        f_tau = sum(v * pow(tau, i, O.P_R) for i, v in enumerate(c)) % O.P_R
+        assert cm == O.g1_mul(O.G1_GEN, f_tau)
+
+
+def test_commit_large_known_tau(ctx):
+    """2^16 points through the wide-window table: the known-tau identity."""
+    import apogee_gpu as A
+
+    tau = 0x5EED
+    nv = 16
+    n = 1 << nv
+    ctx.srs_generate(tau, n)
+    rng = random.Random(12)
+    coeffs = [rng.randrange(O.P_R) for _ in range(n)]
+    cm = ctx.commit(A.to_mont_bytes(coeffs), nv)
+    # f(tau) by Horner
+    acc = 0
+    for c in reversed(coeffs):
+        acc = (acc * tau + c) % O.P_R
+    assert cm == O.g1_mul(O.G1_GEN, acc)
