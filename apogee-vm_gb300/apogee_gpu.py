@@ -191,3 +191,42 @@ class Context:
         out = ctypes.create_string_buffer(64)
         self._check(lib().apg_commit_device(self._h, ctypes.c_void_p(d_ptr), ctypes.c_size_t(num_vars), out))
         return out.raw
+
+    def commit_batch_device(self, d_ptrs, num_vars: int) -> list:
+        k = len(d_ptrs)
+        arr = (ctypes.c_void_p * k)(*d_ptrs)
+        out = ctypes.create_string_buffer(64 * k)
+        self._check(lib().apg_commit_batch_device(self._h, arr, ctypes.c_size_t(k), ctypes.c_size_t(num_vars), out))
+        return [out.raw[64 * j:64 * j + 64] for j in range(k)]
+
+    def commit_batch_host(self, host_ptrs, num_vars: int) -> list:
+        """apg_commit_batch over raw host pointers (e.g. pinned tensors)."""
+        k = len(host_ptrs)
+        arr = (ctypes.c_void_p * k)(*host_ptrs)
+        out = ctypes.create_string_buffer(64 * k)
+        self._check(lib().apg_commit_batch(self._h, arr, ctypes.c_size_t(k), ctypes.c_size_t(num_vars), out))
+        return [out.raw[64 * j:64 * j + 64] for j in range(k)]
+
+    def fr_to_mont_device(self, d_ptr: int, n: int):
+        self._check(lib().apg_fr_to_mont_device(self._h, ctypes.c_void_p(d_ptr), ctypes.c_size_t(n)))
+
+    def launch_count(self) -> int:
+        f = lib().apg_ctx_launch_count
+        f.restype = ctypes.c_uint64
+        return f(self._h)
+
+    TIMER_MSM_ACCUMULATE, TIMER_MSM_TOTAL, TIMER_SUMCHECK_ROUND, TIMER_GKR_FORWARD, TIMER_MERCURY_PASS = range(5)
+
+    def set_timing(self, on: bool):
+        self._check(lib().apg_ctx_set_timing(self._h, 1 if on else 0))
+
+    def timer(self, which: int):
+        ms = ctypes.c_double()
+        n = ctypes.c_uint64()
+        self._check(lib().apg_ctx_timer(self._h, which, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def probe_fq_mul_rate(self, ms: float = 200.0) -> float:
+        r = ctypes.c_double()
+        self._check(lib().apg_probe_fq_mul_rate(self._h, ctypes.c_double(ms), ctypes.byref(r)))
+        return r.value

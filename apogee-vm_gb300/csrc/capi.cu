@@ -235,6 +235,68 @@ int apg_commit_device(apg_ctx* ctx, const void* d_evals, size_t num_vars, uint8_
   return guarded(ctx, [&](Ctx& c) { return commit_common(c, d_evals, true, false, num_vars, out); });
 }
 
+int apg_commit_batch_device(apg_ctx* ctx, const void* const* d_cols, size_t k, size_t num_vars, uint8_t* out) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (!d_cols || !out) return (int)APG_ERR_INVALID_ARGUMENT;
+    if (!mercury_num_vars_ok(num_vars)) return (int)APG_ERR_UNSUPPORTED_NUM_VARS;
+    if (!c.srs) return (int)APG_ERR_NO_SRS;
+    size_t n = (size_t)1 << num_vars;
+    if (c.srs_n < n) return (int)APG_ERR_SRS_TOO_SMALL;
+    const SrsTable* t = commit_table(c, n);
+    if (!t) throw Error(APG_ERR_INTERNAL, "no SRS window table");
+    uint8_t* d_out = c.scratch[S_TMP5].as<uint8_t>(64 * k);
+    for (size_t j = 0; j < k; ++j) msm_device(c, nullptr, t, d_cols[j], false, false, n, d_out + 64 * j, nullptr);
+    APG_CUDA(cudaMemcpyAsync(out, d_out, 64 * k, cudaMemcpyDeviceToHost, c.stream));
+    c.check_flags();
+    return (int)APG_OK;
+  });
+}
+
+int apg_fr_to_mont_device(apg_ctx* ctx, void* d_vals, size_t n) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (!d_vals && n) return (int)APG_ERR_INVALID_ARGUMENT;
+    if (n) launch(c, k_fr_to_mont, (unsigned)((n + 255) / 256), 256, 0, (Fr*)d_vals, n, c.d_flags);
+    c.check_flags();
+    return (int)APG_OK;
+  });
+}
+
+int apg_ctx_set_timing(apg_ctx* ctx, int on) {
+  return guarded(ctx, [&](Ctx& c) {
+    c.timers.flush();
+    c.timers.on = on != 0;
+    for (int i = 0; i < Timers::N; ++i) {
+      c.timers.ms[i] = 0;
+      c.timers.count[i] = 0;
+    }
+    return (int)APG_OK;
+  });
+}
+
+int apg_ctx_timer(apg_ctx* ctx, int timer, double* ms, uint64_t* launches) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (timer < 0 || timer >= Timers::N || !ms || !launches) return (int)APG_ERR_INVALID_ARGUMENT;
+    c.timers.flush();
+    *ms = c.timers.ms[timer];
+    *launches = c.timers.count[timer];
+    return (int)APG_OK;
+  });
+}
+
+int apg_probe_fq_mul_rate(apg_ctx* ctx, double ms, double* fq_mul_per_s) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (!fq_mul_per_s || ms <= 0) return (int)APG_ERR_INVALID_ARGUMENT;
+    *fq_mul_per_s = probe_fq_mul_rate(c, ms);
+    return (int)APG_OK;
+  });
+}
+
+uint64_t apg_ctx_launch_count(apg_ctx* ctx) {
+  if (!ctx) return 0;
+  std::lock_guard<std::mutex> lock(ctx->c.mu);
+  return ctx->c.launches;
+}
+
 int apg_commit_batch(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_t num_vars, uint8_t* out) {
   return guarded(ctx, [&](Ctx& c) {
     if (!cols || !out) return (int)APG_ERR_INVALID_ARGUMENT;

@@ -81,6 +81,38 @@ enum ScratchSlot {
   S_TMP5, S_TMP6, S_TMP7, S_COUNT
 };
 
+// Per-kernel CUDA-event timers (ids are public: APG_TIMER_* in the header).
+struct Timers {
+  static constexpr int N = 8;
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  double ms[N] = {0};
+  uint64_t count[N] = {0};
+  cudaEvent_t get() {
+    if (pool.empty()) {
+      cudaEvent_t e;
+      APG_CUDA(cudaEventCreate(&e));
+      return e;
+    }
+    cudaEvent_t e = pool.back();
+    pool.pop_back();
+    return e;
+  }
+  void flush() {
+    for (auto& p : pending) {
+      APG_CUDA(cudaEventSynchronize(p.second.second));
+      float t = 0;
+      APG_CUDA(cudaEventElapsedTime(&t, p.second.first, p.second.second));
+      ms[p.first] += t;
+      count[p.first] += 1;
+      pool.push_back(p.second.first);
+      pool.push_back(p.second.second);
+    }
+    pending.clear();
+  }
+};
+
 struct Ctx {
   int device = 0;
   int sm_count = 0;
@@ -92,7 +124,22 @@ struct Ctx {
   std::vector<SrsTable> tables;
   DevBuf scratch[S_COUNT];
   uint32_t* d_flags = nullptr;  // device error flags (DeviceFlag bits)
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  uint64_t launches = 0;        // kernels launched on this context
+  Timers timers;
+
+  // Bracket work on the stream with a timer's events (no-op unless enabled).
+  cudaEvent_t timer_begin() {
+    if (!timers.on) return nullptr;
+    cudaEvent_t e = timers.get();
+    APG_CUDA(cudaEventRecord(e, stream));
+    return e;
+  }
+  void timer_end(int id, cudaEvent_t begin) {
+    if (!timers.on || !begin) return;
+    cudaEvent_t e = timers.get();
+    APG_CUDA(cudaEventRecord(e, stream));
+    timers.pending.push_back({id, {begin, e}});
+  }
 
   void check_flags() {
     uint32_t f = 0;
@@ -108,6 +155,14 @@ struct Ctx {
     }
   }
 };
+
+// Launch a kernel on the context's stream, check the launch and count it.
+template <class... KArgs, class... Args>
+inline void launch(Ctx& c, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, Args... args) {
+  kernel<<<grid, block, smem, c.stream>>>(args...);
+  APG_CUDA(cudaGetLastError());
+  ++c.launches;
+}
 
 // ---------------------------------------------------------------------------
 // Entry points implemented in the .cu files.
@@ -135,5 +190,6 @@ MsmPlan msm_plan(size_t n, bool small_scalars, const SrsTable* table);
 void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* scalars, bool small_scalars,
                 bool scalars_canonical, size_t n, uint8_t* out64_device, uint8_t* host_out);
 const SrsTable* srs_table(Ctx& c, int cbits, size_t need);
+double probe_fq_mul_rate(Ctx& c, double target_ms);
 
 }  // namespace apg

@@ -406,16 +406,14 @@ void upload_points(Ctx& c, const uint8_t* host, size_t n, Affine* dst) {
   if (n == 0) return;
   uint4* raw = c.scratch[S_TMP7].as<uint4>(4 * n);
   APG_CUDA(cudaMemcpyAsync(raw, host, 64 * n, cudaMemcpyHostToDevice, c.stream));
-  k_points_in<<<blocks_for<int>(n, 256), 256, 0, c.stream>>>(raw, n, dst, c.d_flags);
-  APG_LAUNCH_CHECK();
+  launch(c, k_points_in, blocks_for<int>(n, 256), 256, 0, (const uint4*)raw, n, dst, c.d_flags);
   c.check_flags();
 }
 
 void download_points(Ctx& c, const Affine* src, size_t n, uint8_t* host) {
   if (n == 0) return;
   uint4* raw = c.scratch[S_TMP7].as<uint4>(4 * n);
-  k_points_out<<<blocks_for<int>(n, 256), 256, 0, c.stream>>>(src, n, raw);
-  APG_LAUNCH_CHECK();
+  launch(c, k_points_out, blocks_for<int>(n, 256), 256, 0, src, n, raw);
   APG_CUDA(cudaMemcpyAsync(host, raw, 64 * n, cudaMemcpyDeviceToHost, c.stream));
   APG_CUDA(cudaStreamSynchronize(c.stream));
 }
@@ -423,14 +421,12 @@ void download_points(Ctx& c, const Affine* src, size_t n, uint8_t* host) {
 void generate_srs(Ctx& c, const uint8_t tau_canonical[32], size_t n, Affine* dst) {
   Fr* d_tau = c.scratch[S_TMP6].as<Fr>(1);
   APG_CUDA(cudaMemcpyAsync(d_tau, tau_canonical, 32, cudaMemcpyHostToDevice, c.stream));
-  k_fr_to_mont<<<1, 1, 0, c.stream>>>(d_tau, 1, c.d_flags);
-  APG_LAUNCH_CHECK();
+  launch(c, k_fr_to_mont, 1, 1, 0, d_tau, (size_t)1, c.d_flags);
   c.check_flags();
   Fr tau_mont;
   APG_CUDA(cudaMemcpyAsync(&tau_mont, d_tau, 32, cudaMemcpyDeviceToHost, c.stream));
   APG_CUDA(cudaStreamSynchronize(c.stream));
-  k_srs_powers<<<blocks_for<int>(n, 128), 128, 0, c.stream>>>(tau_mont, n, dst);
-  APG_LAUNCH_CHECK();
+  launch(c, k_srs_powers, blocks_for<int>(n, 128), 128, 0, tau_mont, n, dst);
   APG_CUDA(cudaStreamSynchronize(c.stream));
 }
 
@@ -454,11 +450,12 @@ const SrsTable* srs_table(Ctx& c, int cbits, size_t need) {
   for (auto& t : c.tables)
     if (t.c == cbits && t.n >= need) return &t;
   if (!c.srs || c.srs_n < need) return nullptr;
-  // Build over the whole SRS for the wide table, over a prefix for narrow ones.
+  // The wide table covers the whole SRS, a narrow one a 2^16 prefix.
   size_t n = cbits >= 12 ? c.srs_n : std::min(c.srs_n, (size_t)1 << 16);
   if (n < need) n = c.srs_n;
   for (auto it = c.tables.begin(); it != c.tables.end(); ++it)
     if (it->c == cbits) {
+      APG_CUDA(cudaStreamSynchronize(c.stream));
       cudaFree(it->tab);
       c.tables.erase(it);
       break;
@@ -468,8 +465,7 @@ const SrsTable* srs_table(Ctx& c, int cbits, size_t need) {
   t.windows = window_count(254, cbits);
   t.n = n;
   APG_CUDA(cudaMalloc(&t.tab, (size_t)t.windows * n * sizeof(Affine)));
-  k_window_table<<<blocks_for<int>(n, 128), 128, 0, c.stream>>>(c.srs, n, cbits, t.windows, t.tab);
-  APG_LAUNCH_CHECK();
+  launch(c, k_window_table, blocks_for<int>(n, 128), 128, 0, (const Affine*)c.srs, n, cbits, t.windows, t.tab);
   APG_CUDA(cudaStreamSynchronize(c.stream));
   c.tables.push_back(t);
   return &c.tables.back();
@@ -513,64 +509,61 @@ void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* 
   uint32_t* total = c.scratch[S_OFFSETS].as<uint32_t>(1);
   Xyzz* buckets = c.scratch[S_BUCKETS].as<Xyzz>(nbins);
 
-  APG_CUDA(cudaMemsetAsync(counts, 0, (nbins + 1) * sizeof(uint32_t), c.stream));
-  APG_CUDA(cudaMemsetAsync(buckets, 0, nbins * sizeof(Xyzz), c.stream));
-  if (small_scalars)
-    k_recode<true><<<blocks_for<int>(n, 256), 256, 0, c.stream>>>(scalars, n, p.c, p.windows, p.precomp, tab_n,
-                                                                   1, entries, counts, c.d_flags);
-  else
-    k_recode<false><<<blocks_for<int>(n, 256), 256, 0, c.stream>>>(scalars, n, p.c, p.windows, p.precomp, tab_n,
-                                                                    scalars_canonical ? 1 : 0, entries, counts,
-                                                                    c.d_flags);
-  APG_LAUNCH_CHECK();
-  k_scan_local<<<(unsigned)scan_blocks, kScanBlock, 0, c.stream>>>(counts, nbins, blk);
-  k_scan_blocks<<<1, kScanBlock, 0, c.stream>>>(blk, (int)scan_blocks);
-  k_scan_add<<<blocks_for<int>(nbins, 256), 256, 0, c.stream>>>(counts, nbins, blk, total);
-  k_scatter<<<blocks_for<int>(E, 256), 256, 0, c.stream>>>(entries, E, counts, sorted);
-  APG_LAUNCH_CHECK();
-
   // Segments: enough threads to fill the chip several times over.
-  size_t target_threads = (size_t)c.sm_count * 1024;
-  int seg_len = (int)std::max<size_t>(4, std::min<size_t>(256, E / std::max<size_t>(target_threads, 1)));
-  size_t nseg = (E + seg_len - 1) / seg_len;
+  const size_t target_threads = (size_t)c.sm_count * 1024;
+  const int seg_len = (int)std::max<size_t>(4, std::min<size_t>(256, E / std::max<size_t>(target_threads, 1)));
+  const size_t nseg = (E + seg_len - 1) / seg_len;
   Xyzz* head = c.scratch[S_HEAD].as<Xyzz>(nseg);
   Xyzz* tail = c.scratch[S_TAIL].as<Xyzz>(nseg);
   uint8_t* flags = c.scratch[S_FLAGS].as<uint8_t>(nseg);
-  k_accumulate<<<blocks_for<int>(nseg, 128), 128, 0, c.stream>>>(sorted, total, seg_len, nseg, src, buckets, head,
-                                                                  tail, flags);
-  APG_LAUNCH_CHECK();
-  k_fixup<<<blocks_for<int>(nseg, 128), 128, 0, c.stream>>>(sorted, total, seg_len, nseg, flags, head, tail,
-                                                             buckets);
-  APG_LAUNCH_CHECK();
 
-  // Reduction levels.
   int fan_log = 0;
   while ((1 << fan_log) < kLevelFan) ++fan_log;
   int levels = 0;
-  {
-    int M = K;
-    while (true) {
-      ++levels;
-      if (M <= kLevelFan) break;
-      M = (M + kLevelFan - 1) / kLevelFan;
-    }
+  for (int M = K;; M = (M + kLevelFan - 1) / kLevelFan) {
+    ++levels;
+    if (M <= kLevelFan) break;
   }
   Xyzz* tsum = c.scratch[S_TSUM].as<Xyzz>((size_t)levels * spaces);
-  Xyzz* lvl_in = buckets;
+  const int G0 = (K + kLevelFan - 1) / kLevelFan;
+  Xyzz* outT = c.scratch[S_LEVEL_T].as<Xyzz>((size_t)spaces * G0);
+  Xyzz* lvlA = c.scratch[S_LEVEL_A].as<Xyzz>((size_t)spaces * G0);
+  Xyzz* lvlB = c.scratch[S_LEVEL_B].as<Xyzz>((size_t)spaces * G0);
+  uint32_t* res = c.scratch[S_RESULT].as<uint32_t>(16);
+
+  cudaEvent_t t_total = c.timer_begin();
+  APG_CUDA(cudaMemsetAsync(counts, 0, (nbins + 1) * sizeof(uint32_t), c.stream));
+  APG_CUDA(cudaMemsetAsync(buckets, 0, nbins * sizeof(Xyzz), c.stream));
+  if (small_scalars)
+    launch(c, k_recode<true>, blocks_for<int>(n, 256), 256, 0, scalars, n, p.c, p.windows, (int)p.precomp, tab_n,
+           1, entries, counts, c.d_flags);
+  else
+    launch(c, k_recode<false>, blocks_for<int>(n, 256), 256, 0, scalars, n, p.c, p.windows, (int)p.precomp,
+           tab_n, scalars_canonical ? 1 : 0, entries, counts, c.d_flags);
+  launch(c, k_scan_local, (unsigned)scan_blocks, kScanBlock, 0, counts, nbins, blk);
+  launch(c, k_scan_blocks, 1, kScanBlock, 0, blk, (int)scan_blocks);
+  launch(c, k_scan_add, blocks_for<int>(nbins, 256), 256, 0, counts, nbins, (const uint32_t*)blk, total);
+  launch(c, k_scatter, blocks_for<int>(E, 256), 256, 0, (const uint64_t*)entries, E, counts, sorted);
+  cudaEvent_t t_acc = c.timer_begin();
+  launch(c, k_accumulate, blocks_for<int>(nseg, 128), 128, 0, (const uint64_t*)sorted, (const uint32_t*)total,
+         seg_len, nseg, src, buckets, head, tail, flags);
+  c.timer_end(APG_TIMER_MSM_ACCUMULATE, t_acc);
+  launch(c, k_fixup, blocks_for<int>(nseg, 128), 128, 0, (const uint64_t*)sorted, (const uint32_t*)total, seg_len,
+         nseg, (const uint8_t*)flags, (const Xyzz*)head, (const Xyzz*)tail, buckets);
+
+  const Xyzz* lvl_in = buckets;
   int M = K;
   for (int l = 0; l < levels; ++l) {
     int G = (M + kLevelFan - 1) / kLevelFan;
-    Xyzz* outT = c.scratch[S_LEVEL_T].as<Xyzz>((size_t)spaces * G);
-    Xyzz* outR = c.scratch[(l & 1) ? S_LEVEL_B : S_LEVEL_A].as<Xyzz>((size_t)spaces * G);
-    k_level<<<blocks_for<int>((size_t)spaces * G, 64), 64, 0, c.stream>>>(lvl_in, M, spaces, kLevelFan, outT, outR);
-    k_sum<<<spaces, 128, 0, c.stream>>>(outT, G, tsum + (size_t)l * spaces);
-    APG_LAUNCH_CHECK();
+    Xyzz* outR = (l & 1) ? lvlB : lvlA;
+    launch(c, k_level, blocks_for<int>((size_t)spaces * G, 64), 64, 0, lvl_in, M, spaces, kLevelFan, outT, outR);
+    launch(c, k_sum, spaces, 128, 0, (const Xyzz*)outT, G, tsum + (size_t)l * spaces);
     lvl_in = outR;
     M = G;
   }
-  uint32_t* res = c.scratch[S_RESULT].as<uint32_t>(16);
-  k_finish<<<1, 32, 0, c.stream>>>(tsum, levels, spaces, fan_log, p.c, out64_device ? (uint32_t*)out64_device : res);
-  APG_LAUNCH_CHECK();
+  launch(c, k_finish, 1, 32, 0, (const Xyzz*)tsum, levels, spaces, fan_log, p.c,
+         out64_device ? (uint32_t*)out64_device : res);
+  c.timer_end(APG_TIMER_MSM_TOTAL, t_total);
   if (host_out) {
     APG_CUDA(cudaMemcpyAsync(host_out, out64_device ? (void*)out64_device : (void*)res, 64, cudaMemcpyDeviceToHost,
                              c.stream));

@@ -1,0 +1,384 @@
+#!/usr/bin/env python
+"""Benchmark: G1 MSM points/s at 2^22 on one GB300 (the commit phase of the
+largest shard: 16 columns x 2^22 Fr committed by 2^22-point MSMs over a
+seeded-tau SRS).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+One step commits the 16 columns. `value` is points/s with the columns already
+resident in HBM (2 GiB of inputs, far above the 129 MB L2, so no flush is
+needed); `e2e` is the same metric through the public C ABI with pinned host
+buffers, the host-to-device copies inside the timed region. The roofline
+object covers the dominant kernel (bucket accumulation) on a uniform-scalar
+2^22 MSM, against this device's measured Montgomery-multiply throughput. Under
+torchrun every rank commits its own 16 columns (weak scaling, no collective on
+the data path).
+
+--impl reference times the reference algorithm's CPU implementation (the C++
+restatement in oracle/, all host threads) on a bounded sample of the same
+workload and prints the same line with "impl": "reference".
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "apogee-vm_gb300"))
+
+METRIC = "G1 MSM points/s at 2^22"
+UNIT = "points/s"
+SEED = 20260903
+TAU_SEED = 0x7A75_5EED
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def reference_window_windows(n):
+    """The reference's window rule (crates/curve/src/msm.rs:112-142)."""
+    lg = n.bit_length() - 1 if n & (n - 1) == 0 else n.bit_length()
+    w = 3 if n < 32 else (lg * 69) // 100 + 2
+    return w, -(-255 // w)
+
+
+def algorithmic_imad_accumulate(n):
+    """Bucket accumulation's algorithmic IMAD32 count at n points: one mixed
+    add (8M + 2S) per point per reference window, 264 IMAD32 per Fq multiply
+    (8x32-limb CIOS)."""
+    _, windows = reference_window_windows(n)
+    return n * windows * 10 * 264
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 7:
+                    continue
+                try:
+                    sm.append(float(f[0]))
+                    mx = float(f[1])
+                except ValueError:
+                    continue
+                for nm, v in zip(names, f[3:7]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_traffic():
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_msm_points_per_s(bases: bytes, scalars: bytes, n: int, threads: int, reps: int = 3):
+    """Best-of-reps oracle MSM time on n points (the reference's best-of-3)."""
+    import ctypes
+
+    import oracle_lib as O
+
+    out = ctypes.create_string_buffer(64)
+    best = None
+    for _ in range(reps):
+        t = O.lib().oracle_time_msm(bases, scalars, ctypes.c_size_t(n), ctypes.c_size_t(threads), out)
+        if t < 0:
+            raise RuntimeError("oracle rejected the sample")
+        best = t if best is None else min(best, t)
+    return n / best, out.raw
+
+
+def run_reference(args):
+    rank = env_int("RANK", 0)
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+
+    import oracle_lib as O
+    import synth
+
+    log2n = 18
+    n = 1 << log2n
+    threads = os.cpu_count() or 1
+    tau = O.Rng(TAU_SEED).next_fr()
+    bases = O.toy_srs(tau, n, threads)
+    col = synth.mixed_column(n, SEED)
+    scalars = col.tobytes()
+    import ctypes
+
+    out = ctypes.create_string_buffer(64)
+    for _ in range(max(args.warmup, 0)):
+        O.lib().oracle_time_msm(bases, scalars, ctypes.c_size_t(n), ctypes.c_size_t(threads), out)
+    times = []
+    for _ in range(args.steps):
+        times.append(O.lib().oracle_time_msm(bases, scalars, ctypes.c_size_t(n), ctypes.c_size_t(threads), out))
+    t = sum(times) / len(times)
+    value = n / t
+    sample = (f"one 2^{log2n}-point MSM per step (mixed VM-trace scalars, seeded-tau SRS), "
+              f"reference window rule and window x chunk split")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32 limbs (Fq/Fr Montgomery, 4x64)", "data": "synthetic",
+        "config": {"workload": "commit: 16 columns x 2^22 Fr, mixed VM-trace distribution, seeded-tau SRS",
+                   "sampled_as": f"2^{log2n}-point MSMs"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_msm_only(args):
+    """A lean case for profiling: warm-up and timed 2^log2n uniform-scalar SRS
+    MSMs and nothing else (no end-to-end leg, no CPU baseline)."""
+    import numpy as np
+    import torch
+
+    import apogee_gpu as A
+    import synth
+
+    local = env_int("LOCAL_RANK", 0)
+    torch.cuda.set_device(local)
+    n = 1 << args.log2n
+    ctx = A.Context(local)
+    ctx.srs_generate((TAU_SEED * 0x9E3779B97F4A7C15) % A.P_R, n)
+    ctx.srs_prepare()
+    cols = []
+    for j in range(args.cols):
+        t = torch.from_numpy(synth.uniform_column(n, SEED + j).view(np.int32).reshape(-1)).to(f"cuda:{local}")
+        ctx.fr_to_mont_device(t.data_ptr(), n)
+        cols.append(t)
+    ptrs = [t.data_ptr() for t in cols]
+    for _ in range(args.warmup):
+        ctx.commit_batch_device(ptrs, args.log2n)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.commit_batch_device(ptrs, args.log2n)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / args.steps
+    print(json.dumps({"msm_only": True, "log2n": args.log2n, "cols": args.cols, "ms_per_step": dt * 1e3,
+                      "points_per_s": args.cols * n / dt}), flush=True)
+    ctx.close()
+    return 0
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    import apogee_gpu as A
+    import synth
+
+    rank, world, local = env_int("RANK", 0), env_int("WORLD_SIZE", 1), env_int("LOCAL_RANK", 0)
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_
+
+        dist_.init_process_group("nccl", device_id=torch.device("cuda", local))
+        dist = dist_
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    log2n, k = args.log2n, args.cols
+    n = 1 << log2n
+    ctx = A.Context(local)
+    tau = (TAU_SEED * 0x9E3779B97F4A7C15) % A.P_R
+    ctx.srs_generate(tau, n)
+    ctx.srs_prepare()
+
+    # Inputs: k mixed columns per rank, canonical on the host, Montgomery on
+    # the device and in a pinned host mirror for the end-to-end leg.
+    dev_cols, host_cols = [], []
+    for j in range(k):
+        col = synth.mixed_column(n, SEED + 1000 * rank + j)
+        t = torch.from_numpy(col.view(np.int32).reshape(-1)).to(f"cuda:{local}")
+        ctx.fr_to_mont_device(t.data_ptr(), n)
+        dev_cols.append(t)
+        h = torch.empty_like(t, device="cpu").pin_memory()
+        h.copy_(t)
+        host_cols.append(h)
+    torch.cuda.synchronize()
+    ptrs = [t.data_ptr() for t in dev_cols]
+    hptrs = [h.data_ptr() for h in host_cols]
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    # Warm-up.
+    for _ in range(args.warmup):
+        ctx.commit_batch_device(ptrs, log2n)
+
+    # Timed: device-resident inputs.
+    barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            cms = ctx.commit_batch_device(ptrs, log2n)
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    launches = ctx.launch_count() - launches0
+    ms_step = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms_step], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * k * n / (ms_step / 1e3)
+
+    # End to end through the public API with host buffers.
+    for _ in range(1):
+        ctx.commit_batch_host(hptrs, log2n)
+    e2e_steps = max(1, min(args.steps, 3))
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        cms_h = ctx.commit_batch_host(hptrs, log2n)
+    torch.cuda.synchronize()
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    barrier()
+    if dist:
+        t = torch.tensor([t_e2e], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    assert cms_h == cms, "device-resident and host-buffer commits disagree"
+    e2e = {"value": world * k * n / t_e2e, "unit": UNIT, "h2d_bytes_per_step": k * n * 32,
+           "d2h_bytes_per_step": k * 64}
+
+    # Roofline: the accumulation kernel on uniform 254-bit scalars.
+    ucol = synth.uniform_column(n, SEED + 999)
+    ut = torch.from_numpy(ucol.view(np.int32).reshape(-1)).to(f"cuda:{local}")
+    ctx.fr_to_mont_device(ut.data_ptr(), n)
+    ctx.commit_device(ut.data_ptr(), log2n)
+    ctx.set_timing(True)
+    reps = 5
+    for _ in range(reps):
+        ctx.commit_device(ut.data_ptr(), log2n)
+    acc_ms, acc_n = ctx.timer(A.Context.TIMER_MSM_ACCUMULATE)
+    tot_ms, tot_n = ctx.timer(A.Context.TIMER_MSM_TOTAL)
+    ctx.set_timing(False)
+    fq_rate = ctx.probe_fq_mul_rate(300.0)
+    peak_imad = fq_rate * 264
+    algo = algorithmic_imad_accumulate(n)
+    achieved = algo / (acc_ms / acc_n / 1e3)
+    traffic = load_traffic().get("msm_accumulate_2p22", {}).get("dram_bytes_per_launch")
+    roofline = {
+        "bound": "int", "kernel": "k_accumulate (bucket accumulation, 2^22 uniform scalars)",
+        "achieved": achieved / 1e12, "peak": peak_imad / 1e12, "unit": "TIMAD32/s", "frac": achieved / peak_imad,
+        "traffic": traffic, "peak_source": "measured on this device: dependency-free Fq Montgomery products x 264",
+        "kernel_ms": acc_ms / acc_n, "msm_ms": tot_ms / tot_n,
+        "msm_uniform_points_per_s": n / (tot_ms / tot_n / 1e3), "algorithmic_imad_per_launch": algo,
+    }
+
+    cpu = None
+    if rank == 0:
+        threads = os.cpu_count() or 1
+        m = 1 << 18
+        bases = ctx.srs_download(m)
+        sample_scalars = synth.mixed_column(m, SEED).tobytes()
+        try:
+            sys.path.insert(0, os.path.join(ROOT, "tests"))
+            v, _ = cpu_msm_points_per_s(bases, sample_scalars, m, threads)
+            cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": "best of 3 2^18-point MSMs (mixed VM-trace scalars) by the C++ restatement of the "
+                             "reference Pippenger, all host threads"}
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": UNIT, "cores": threads, "kind": "port", "sample": f"failed: {e}"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32 limbs (Fq/Fr Montgomery, 8x32)", "data": "synthetic",
+            "config": {"workload": f"commit: {k} columns x 2^{log2n} Fr per GPU, mixed VM-trace distribution "
+                                   "(25% {0,1}, 60% u32, 15% uniform Fr), seeded-tau SRS",
+                       "msm_points": n, "columns_per_gpu": k, "parallelism": f"replicas x{world}",
+                       "l2": "inputs 2 GiB per GPU > 129 MB L2, no flush needed"},
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--log2n", type=int, default=22)
+    ap.add_argument("--cols", type=int, default=16)
+    ap.add_argument("--only-msm", action="store_true", help="lean uniform-scalar MSM case for profiling")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.only_msm:
+        return run_msm_only(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -118,6 +118,34 @@ int apg_commit_batch(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_t 
 /* As apg_commit, with the evaluations already in device memory (a pointer
  * the caller allocated on this context's device). */
 int apg_commit_device(apg_ctx* ctx, const void* d_evals, size_t num_vars, uint8_t out[64]);
+/* As apg_commit_batch over device-resident columns; the k MSMs run back to
+ * back on the context's stream and the call returns once all are done. */
+int apg_commit_batch_device(apg_ctx* ctx, const void* const* d_cols, size_t k, size_t num_vars, uint8_t* out);
+
+/* ---- utilities ---------------------------------------------------------- */
+
+/* Canonical Fr values in device memory -> Montgomery (in-memory) form, in
+ * place; APG_ERR_NONCANONICAL if any value is >= p. */
+int apg_fr_to_mont_device(apg_ctx* ctx, void* d_vals, size_t n);
+/* Kernels this context has launched since it was created. */
+uint64_t apg_ctx_launch_count(apg_ctx* ctx);
+
+/* Per-kernel device timing with CUDA events on the context's stream. */
+enum apg_timer {
+  APG_TIMER_MSM_ACCUMULATE = 0, /* bucket accumulation kernel */
+  APG_TIMER_MSM_TOTAL = 1,      /* one whole MSM, recode to normalisation */
+  APG_TIMER_SUMCHECK_ROUND = 2, /* sumcheck evaluate+fold kernel */
+  APG_TIMER_GKR_FORWARD = 3,    /* GKR forward layer kernel */
+  APG_TIMER_MERCURY_PASS = 4    /* Mercury O(n) field passes */
+};
+/* Enable (1) or disable (0) timers; enabling clears accumulated totals. */
+int apg_ctx_set_timing(apg_ctx* ctx, int on);
+/* Total milliseconds and launch count recorded under `timer` so far. */
+int apg_ctx_timer(apg_ctx* ctx, int timer, double* ms, uint64_t* launches);
+/* Measure this device's Montgomery-multiply throughput: a dependency-free
+ * stream of Fq products over every SM for about `ms` milliseconds. Writes
+ * Fq multiplications per second. */
+int apg_probe_fq_mul_rate(apg_ctx* ctx, double ms, double* fq_mul_per_s);
 
 #ifdef __cplusplus
 }
