@@ -14,7 +14,7 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libapogee_gpu.so")
+LIB_PATH = os.environ.get("APOGEE_GPU_LIB") or os.path.join(HERE, "libapogee_gpu.so")
 
 P_R = 21888242871839275222246405745257275088548364400416034343698204186575808495617
 P_Q = 21888242871839275222246405745257275088696311157297823662689037894645226208583

@@ -35,7 +35,10 @@ def _stale(obj: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, extra=None) -> str:
+def build(verbose: bool = False, extra=None, build_dir: str = BUILD, lib: str = LIB) -> str:
+    """Compile csrc/*.cu into `lib`; `extra` nvcc flags and a separate
+    `build_dir` let a variant build sit beside the default one."""
+    BUILD, LIB = build_dir, lib  # noqa: N806
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))

@@ -20,6 +20,16 @@ struct Affine {
   Fq x, y;
 };
 
+// The curve formulas call one out-of-line Fq product: a point addition inlines
+// ten of them, and ten inlined copies of a 300-instruction multiply overflow
+// the instruction cache of a bucket-accumulation loop.
+#ifdef APG_INLINE_CURVE_MUL
+__device__ __forceinline__ Fq cmul(const Fq& a, const Fq& b) { return fe_mul(a, b); }
+#else
+static __device__ __noinline__ Fq cmul(const Fq a, const Fq b) { return fe_mul(a, b); }
+#endif
+__device__ __forceinline__ Fq csqr(const Fq& a) { return cmul(a, a); }
+
 struct Xyzz {
   Fq x, y, zz, zzz;
 };
@@ -50,14 +60,14 @@ __device__ __forceinline__ Xyzz xyzz_from_affine(const Affine& a) {
 // mdbl-2008-s-1: 2 * (x, y) for an affine finite point.
 __device__ __forceinline__ Xyzz xyzz_dbl_affine(const Affine& a) {
   Fq u = fe_dbl(a.y);
-  Fq v = fe_sqr(u);
-  Fq w = fe_mul(u, v);
-  Fq s = fe_mul(a.x, v);
-  Fq x2 = fe_sqr(a.x);
+  Fq v = csqr(u);
+  Fq w = cmul(u, v);
+  Fq s = cmul(a.x, v);
+  Fq x2 = csqr(a.x);
   Fq m = fe_add(fe_dbl(x2), x2);
   Xyzz r;
-  r.x = fe_sub(fe_sub(fe_sqr(m), s), s);
-  r.y = fe_sub(fe_mul(m, fe_sub(s, r.x)), fe_mul(w, a.y));
+  r.x = fe_sub(fe_sub(csqr(m), s), s);
+  r.y = fe_sub(cmul(m, fe_sub(s, r.x)), cmul(w, a.y));
   r.zz = v;
   r.zzz = w;
   return r;
@@ -67,38 +77,38 @@ __device__ __forceinline__ Xyzz xyzz_dbl_affine(const Affine& a) {
 __device__ __forceinline__ Xyzz xyzz_dbl(const Xyzz& p) {
   if (xyzz_is_inf(p)) return p;
   Fq u = fe_dbl(p.y);
-  Fq v = fe_sqr(u);
-  Fq w = fe_mul(u, v);
-  Fq s = fe_mul(p.x, v);
-  Fq x2 = fe_sqr(p.x);
+  Fq v = csqr(u);
+  Fq w = cmul(u, v);
+  Fq s = cmul(p.x, v);
+  Fq x2 = csqr(p.x);
   Fq m = fe_add(fe_dbl(x2), x2);
   Xyzz r;
-  r.x = fe_sub(fe_sub(fe_sqr(m), s), s);
-  r.y = fe_sub(fe_mul(m, fe_sub(s, r.x)), fe_mul(w, p.y));
-  r.zz = fe_mul(v, p.zz);
-  r.zzz = fe_mul(w, p.zzz);
+  r.x = fe_sub(fe_sub(csqr(m), s), s);
+  r.y = fe_sub(cmul(m, fe_sub(s, r.x)), cmul(w, p.y));
+  r.zz = cmul(v, p.zz);
+  r.zzz = cmul(w, p.zzz);
   return r;
 }
 
 // madd-2008-s: acc + (x2, y2), the affine point assumed finite.
 __device__ __forceinline__ Xyzz xyzz_add_affine(const Xyzz& p, const Affine& a) {
   if (xyzz_is_inf(p)) return xyzz_from_affine(a);
-  Fq u2 = fe_mul(a.x, p.zz);
-  Fq s2 = fe_mul(a.y, p.zzz);
+  Fq u2 = cmul(a.x, p.zz);
+  Fq s2 = cmul(a.y, p.zzz);
   Fq pp_ = fe_sub(u2, p.x);
   Fq r = fe_sub(s2, p.y);
   if (fe_is_zero(pp_)) {
     if (fe_is_zero(r)) return xyzz_dbl_affine(a);
     return xyzz_inf();
   }
-  Fq pp = fe_sqr(pp_);
-  Fq ppp = fe_mul(pp_, pp);
-  Fq q = fe_mul(p.x, pp);
+  Fq pp = csqr(pp_);
+  Fq ppp = cmul(pp_, pp);
+  Fq q = cmul(p.x, pp);
   Xyzz o;
-  o.x = fe_sub(fe_sub(fe_sub(fe_sqr(r), ppp), q), q);
-  o.y = fe_sub(fe_mul(r, fe_sub(q, o.x)), fe_mul(p.y, ppp));
-  o.zz = fe_mul(p.zz, pp);
-  o.zzz = fe_mul(p.zzz, ppp);
+  o.x = fe_sub(fe_sub(fe_sub(csqr(r), ppp), q), q);
+  o.y = fe_sub(cmul(r, fe_sub(q, o.x)), cmul(p.y, ppp));
+  o.zz = cmul(p.zz, pp);
+  o.zzz = cmul(p.zzz, ppp);
   return o;
 }
 
@@ -106,24 +116,24 @@ __device__ __forceinline__ Xyzz xyzz_add_affine(const Xyzz& p, const Affine& a) 
 __device__ __forceinline__ Xyzz xyzz_add(const Xyzz& p, const Xyzz& q) {
   if (xyzz_is_inf(p)) return q;
   if (xyzz_is_inf(q)) return p;
-  Fq u1 = fe_mul(p.x, q.zz);
-  Fq u2 = fe_mul(q.x, p.zz);
-  Fq s1 = fe_mul(p.y, q.zzz);
-  Fq s2 = fe_mul(q.y, p.zzz);
+  Fq u1 = cmul(p.x, q.zz);
+  Fq u2 = cmul(q.x, p.zz);
+  Fq s1 = cmul(p.y, q.zzz);
+  Fq s2 = cmul(q.y, p.zzz);
   Fq pp_ = fe_sub(u2, u1);
   Fq r = fe_sub(s2, s1);
   if (fe_is_zero(pp_)) {
     if (fe_is_zero(r)) return xyzz_dbl(p);
     return xyzz_inf();
   }
-  Fq pp = fe_sqr(pp_);
-  Fq ppp = fe_mul(pp_, pp);
-  Fq qq = fe_mul(u1, pp);
+  Fq pp = csqr(pp_);
+  Fq ppp = cmul(pp_, pp);
+  Fq qq = cmul(u1, pp);
   Xyzz o;
-  o.x = fe_sub(fe_sub(fe_sub(fe_sqr(r), ppp), qq), qq);
-  o.y = fe_sub(fe_mul(r, fe_sub(qq, o.x)), fe_mul(s1, ppp));
-  o.zz = fe_mul(fe_mul(p.zz, q.zz), pp);
-  o.zzz = fe_mul(fe_mul(p.zzz, q.zzz), ppp);
+  o.x = fe_sub(fe_sub(fe_sub(csqr(r), ppp), qq), qq);
+  o.y = fe_sub(cmul(r, fe_sub(qq, o.x)), cmul(s1, ppp));
+  o.zz = cmul(cmul(p.zz, q.zz), pp);
+  o.zzz = cmul(cmul(p.zzz, q.zzz), ppp);
   return o;
 }
 
@@ -141,9 +151,9 @@ __device__ __forceinline__ Affine xyzz_to_affine(const Xyzz& p) {
     a.y = fe_zero<FqConsts>();
     return a;
   }
-  Fq t = fe_inverse(fe_mul(p.zz, p.zzz));
-  a.x = fe_mul(p.x, fe_mul(t, p.zzz));
-  a.y = fe_mul(p.y, fe_mul(t, p.zz));
+  Fq t = fe_inverse(cmul(p.zz, p.zzz));
+  a.x = cmul(p.x, cmul(t, p.zzz));
+  a.y = cmul(p.y, cmul(t, p.zz));
   return a;
 }
 

@@ -265,31 +265,52 @@ __device__ __forceinline__ Affine load_base(const Affine* bases, uint64_t e) {
   return a;
 }
 
-enum SegFlag : uint8_t { SEG_STARTS_BEFORE = 1, SEG_CONTINUES = 2, SEG_SINGLE_RUN = 4 };
+// Runs of equal buckets are folded by fixed-length segments; a run that
+// touches a segment edge is only partial and leaves the segment as an item
+// (key, point, present) in slot 2s (the run the segment started inside) or
+// 2s+1 (the run it ends inside). Absent slots carry the neighbouring key and
+// the identity, so the item list stays sorted and gap-free; the next level
+// folds it the same way until one segment holds everything. A run that
+// starts and ends inside a segment is a whole bucket and is written directly,
+// so every bucket is written exactly once however skewed the digits are.
+constexpr uint32_t kNoKey = 0xffffffffu;
+
+__device__ __forceinline__ void put_item(uint32_t* keys, Xyzz* pts, uint8_t* present, size_t slot, uint32_t key,
+                                         const Xyzz* p) {
+  keys[slot] = key;
+  present[slot] = p ? 1 : 0;
+  if (p) st_xyzz(&pts[slot], *p);
+}
 
 __global__ void __launch_bounds__(128) k_accumulate(const uint64_t* sorted, const uint32_t* total, int seg_len,
-                                                    size_t nseg, const Affine* bases, Xyzz* buckets, Xyzz* head,
-                                                    Xyzz* tail, uint8_t* seg_flags) {
+                                                    size_t nseg, const Affine* bases, Xyzz* buckets,
+                                                    uint32_t* okeys, Xyzz* opts, uint8_t* opres) {
   size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (s >= nseg) return;
   const size_t E = *total;
   const size_t lo = s * (size_t)seg_len;
   if (lo >= E) {
-    seg_flags[s] = 0;
+    put_item(okeys, opts, opres, 2 * s, kNoKey, nullptr);
+    put_item(okeys, opts, opres, 2 * s + 1, kNoKey, nullptr);
     return;
   }
   const size_t hi = min(lo + (size_t)seg_len, E);
-  uint32_t cur = (uint32_t)(sorted[lo] >> 32);
+  const uint32_t first = (uint32_t)(sorted[lo] >> 32);
+  uint32_t cur = first;
   const bool starts_before = lo > 0 && (uint32_t)(sorted[lo - 1] >> 32) == cur;
   const bool continues = hi < E && (uint32_t)(sorted[hi] >> 32) == (uint32_t)(sorted[hi - 1] >> 32);
-  bool first_run = true;
+  bool first_run = true, head_written = false;
   Xyzz acc = xyzz_inf();
   for (size_t i = lo; i < hi; ++i) {
     uint64_t e = sorted[i];
     uint32_t b = (uint32_t)(e >> 32);
     if (b != cur) {
-      if (first_run && starts_before) st_xyzz(&head[s], acc);
-      else st_xyzz(&buckets[cur], acc);
+      if (first_run && starts_before) {
+        put_item(okeys, opts, opres, 2 * s, cur, &acc);
+        head_written = true;
+      } else {
+        st_xyzz(&buckets[cur], acc);
+      }
       first_run = false;
       cur = b;
       acc = xyzz_inf();
@@ -297,38 +318,70 @@ __global__ void __launch_bounds__(128) k_accumulate(const uint64_t* sorted, cons
     Affine p = load_base(bases, e);
     if (!aff_is_inf(p)) acc = xyzz_add_affine(acc, p);
   }
-  if (continues) {
-    if (first_run && starts_before) st_xyzz(&head[s], acc);
-    else st_xyzz(&tail[s], acc);
+  if (first_run && starts_before) {
+    put_item(okeys, opts, opres, 2 * s, cur, &acc);
+    head_written = true;
+    put_item(okeys, opts, opres, 2 * s + 1, cur, nullptr);
   } else {
-    if (first_run && starts_before) st_xyzz(&head[s], acc);
-    else st_xyzz(&buckets[cur], acc);
+    if (continues) put_item(okeys, opts, opres, 2 * s + 1, cur, &acc);
+    else {
+      st_xyzz(&buckets[cur], acc);
+      put_item(okeys, opts, opres, 2 * s + 1, cur, nullptr);
+    }
   }
-  seg_flags[s] = (starts_before ? SEG_STARTS_BEFORE : 0) | (continues ? SEG_CONTINUES : 0) |
-                 (first_run ? SEG_SINGLE_RUN : 0);
+  if (!head_written) put_item(okeys, opts, opres, 2 * s, first, nullptr);
 }
 
-// A bucket whose run crosses segment edges: the segment where it starts sums
-// its tail with the heads of the segments it spills into.
-__global__ void k_fixup(const uint64_t* sorted, const uint32_t* total, int seg_len, size_t nseg,
-                        const uint8_t* seg_flags, const Xyzz* head, const Xyzz* tail, Xyzz* buckets) {
+// One level of the edge-run folding over items (see k_accumulate).
+__global__ void __launch_bounds__(128) k_fold_edges(const uint32_t* keys, const Xyzz* pts, const uint8_t* pres,
+                                                    size_t len, int seg_len, size_t nseg, Xyzz* buckets,
+                                                    uint32_t* okeys, Xyzz* opts, uint8_t* opres) {
   size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (s >= nseg) return;
-  const size_t E = *total;
-  if (s * (size_t)seg_len >= E) return;
-  uint8_t f = seg_flags[s];
-  if (!(f & SEG_CONTINUES)) return;
-  if ((f & SEG_SINGLE_RUN) && (f & SEG_STARTS_BEFORE)) return;  // a middle piece
-  const size_t hi = min((s + 1) * (size_t)seg_len, E);
-  const uint32_t b = (uint32_t)(sorted[hi - 1] >> 32);
-  Xyzz acc = ld_xyzz(&tail[s]);
-  for (size_t t = s + 1; t < nseg; ++t) {
-    acc = xyzz_add(acc, ld_xyzz(&head[t]));
-    uint8_t g = seg_flags[t];
-    if ((g & SEG_SINGLE_RUN) && (g & SEG_CONTINUES)) continue;
-    break;
+  const size_t lo = s * (size_t)seg_len;
+  if (lo >= len) {
+    put_item(okeys, opts, opres, 2 * s, kNoKey, nullptr);
+    put_item(okeys, opts, opres, 2 * s + 1, kNoKey, nullptr);
+    return;
   }
-  st_xyzz(&buckets[b], acc);
+  const size_t hi = min(lo + (size_t)seg_len, len);
+  const uint32_t first = keys[lo];
+  uint32_t cur = first;
+  const bool starts_before = lo > 0 && keys[lo - 1] == cur;
+  const bool continues = hi < len && keys[hi] == keys[hi - 1];
+  bool first_run = true, head_written = false, any = false;
+  Xyzz acc = xyzz_inf();
+  for (size_t i = lo; i < hi; ++i) {
+    uint32_t b = keys[i];
+    if (b != cur) {
+      if (first_run && starts_before) {
+        put_item(okeys, opts, opres, 2 * s, cur, any ? &acc : nullptr);
+        head_written = true;
+      } else if (any && cur != kNoKey) {
+        st_xyzz(&buckets[cur], acc);
+      }
+      first_run = false;
+      cur = b;
+      acc = xyzz_inf();
+      any = false;
+    }
+    if (pres[i]) {
+      acc = any ? xyzz_add(acc, ld_xyzz(&pts[i])) : ld_xyzz(&pts[i]);
+      any = true;
+    }
+  }
+  if (first_run && starts_before) {
+    put_item(okeys, opts, opres, 2 * s, cur, any ? &acc : nullptr);
+    head_written = true;
+    put_item(okeys, opts, opres, 2 * s + 1, cur, nullptr);
+  } else {
+    if (continues) put_item(okeys, opts, opres, 2 * s + 1, cur, any ? &acc : nullptr);
+    else {
+      if (any && cur != kNoKey) st_xyzz(&buckets[cur], acc);
+      put_item(okeys, opts, opres, 2 * s + 1, cur, nullptr);
+    }
+  }
+  if (!head_written) put_item(okeys, opts, opres, 2 * s, first, nullptr);
 }
 
 // ---- bucket reduction -------------------------------------------------------
@@ -513,9 +566,11 @@ void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* 
   const size_t target_threads = (size_t)c.sm_count * 1024;
   const int seg_len = (int)std::max<size_t>(4, std::min<size_t>(256, E / std::max<size_t>(target_threads, 1)));
   const size_t nseg = (E + seg_len - 1) / seg_len;
-  Xyzz* head = c.scratch[S_HEAD].as<Xyzz>(nseg);
-  Xyzz* tail = c.scratch[S_TAIL].as<Xyzz>(nseg);
-  uint8_t* flags = c.scratch[S_FLAGS].as<uint8_t>(nseg);
+  // Edge-run item lists, ping-pong between two sets of (keys, points, present).
+  constexpr int kFoldLen = 8;
+  uint32_t* ikeys[2] = {c.scratch[S_HEAD].as<uint32_t>(2 * nseg), c.scratch[S_TAIL].as<uint32_t>(2 * nseg)};
+  Xyzz* ipts[2] = {c.scratch[S_TMP0].as<Xyzz>(2 * nseg), c.scratch[S_TMP1].as<Xyzz>(2 * nseg)};
+  uint8_t* ipres[2] = {c.scratch[S_FLAGS].as<uint8_t>(2 * nseg), c.scratch[S_TMP2].as<uint8_t>(2 * nseg)};
 
   int fan_log = 0;
   while ((1 << fan_log) < kLevelFan) ++fan_log;
@@ -546,10 +601,20 @@ void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* 
   launch(c, k_scatter, blocks_for<int>(E, 256), 256, 0, (const uint64_t*)entries, E, counts, sorted);
   cudaEvent_t t_acc = c.timer_begin();
   launch(c, k_accumulate, blocks_for<int>(nseg, 128), 128, 0, (const uint64_t*)sorted, (const uint32_t*)total,
-         seg_len, nseg, src, buckets, head, tail, flags);
+         seg_len, nseg, src, buckets, ikeys[0], ipts[0], ipres[0]);
   c.timer_end(APG_TIMER_MSM_ACCUMULATE, t_acc);
-  launch(c, k_fixup, blocks_for<int>(nseg, 128), 128, 0, (const uint64_t*)sorted, (const uint32_t*)total, seg_len,
-         nseg, (const uint8_t*)flags, (const Xyzz*)head, (const Xyzz*)tail, buckets);
+  {
+    size_t len = 2 * nseg;
+    int cur = 0;
+    for (size_t fseg = nseg; fseg > 1;) {
+      fseg = (len + kFoldLen - 1) / kFoldLen;
+      launch(c, k_fold_edges, blocks_for<int>(fseg, 128), 128, 0, (const uint32_t*)ikeys[cur],
+             (const Xyzz*)ipts[cur], (const uint8_t*)ipres[cur], len, kFoldLen, fseg, buckets, ikeys[cur ^ 1],
+             ipts[cur ^ 1], ipres[cur ^ 1]);
+      cur ^= 1;
+      len = 2 * fseg;
+    }
+  }
 
   const Xyzz* lvl_in = buckets;
   int M = K;

@@ -150,6 +150,39 @@ def test_commit_u32_and_batch(ctx):
         assert cm == O.g1_mul(O.G1_GEN, f_tau)
 
 
+@pytest.mark.parametrize("kind", ["ones", "bits", "mixed", "identical"])
+def test_commit_skewed_digits(ctx, kind):
+    """Skewed scalars pile most digits into a few buckets (a column of ones
+    puts every entry in bucket 1): the edge-run folding must still write each
+    bucket exactly once. Checked by the known-tau identity at 2^14."""
+    import apogee_gpu as A
+    import synth
+
+    tau = 0xC0FFEE
+    nv = 14
+    n = 1 << nv
+    ctx.srs_generate(tau, n)
+    rng = random.Random(hash(kind) & 0xFFFF)
+    if kind == "ones":
+        coeffs = [1] * n
+    elif kind == "bits":
+        coeffs = [rng.getrandbits(1) for _ in range(n)]
+    elif kind == "identical":
+        coeffs = [rng.randrange(O.P_R)] * n
+    else:
+        coeffs = synth.to_ints(synth.mixed_column(n, 5))
+    cm = ctx.commit(A.to_mont_bytes(coeffs), nv)
+    acc = 0
+    for c in reversed(coeffs):
+        acc = (acc * tau + c) % O.P_R
+    assert cm == O.g1_mul(O.G1_GEN, acc)
+
+
+def test_msm_identical_large_against_oracle(ctx):
+    bases, scalars = O.msm_case("identical", 4096, 31)
+    assert ctx.msm(bases, mont(scalars)) == O.msm(bases, scalars, 4096, threads=8)
+
+
 def test_commit_large_known_tau(ctx):
     """2^16 points through the wide-window table: the known-tau identity."""
     import apogee_gpu as A
