@@ -84,6 +84,34 @@ def fe(x: int) -> bytes:
 
 
 # ---------------------------------------------------------------------------
+# Transcript snapshots (crates/transcript/src/lib.rs)
+# ---------------------------------------------------------------------------
+
+def transcript_init() -> bytes:
+    snap = ctypes.create_string_buffer(TRANSCRIPT_BYTES)
+    lib().apg_transcript_init(snap)
+    return snap.raw
+
+
+def transcript_append_scalars(snap: bytes, tag: int, xs) -> bytes:
+    buf = ctypes.create_string_buffer(bytes(snap), TRANSCRIPT_BYTES)
+    data = to_mont_bytes(xs)
+    st = lib().apg_transcript_append_scalars(buf, ctypes.c_uint64(tag), data, ctypes.c_size_t(len(xs)))
+    if st:
+        raise ApogeeError(st, "apg_transcript_append_scalars")
+    return buf.raw
+
+
+def transcript_challenge(snap: bytes, tag: int):
+    buf = ctypes.create_string_buffer(bytes(snap), TRANSCRIPT_BYTES)
+    out = ctypes.create_string_buffer(32)
+    st = lib().apg_transcript_challenge(buf, ctypes.c_uint64(tag), out)
+    if st:
+        raise ApogeeError(st, "apg_transcript_challenge")
+    return buf.raw, from_mont_bytes(out.raw)[0]
+
+
+# ---------------------------------------------------------------------------
 # Context
 # ---------------------------------------------------------------------------
 
@@ -214,6 +242,39 @@ class Context:
         f = lib().apg_ctx_launch_count
         f.restype = ctypes.c_uint64
         return f(self._h)
+
+    # ---- zerocheck -----------------------------------------------------------
+    def prove_zerocheck(self, terms, polys, num_vars: int, transcript: bytes, on_device: bool = False):
+        """sumcheck::prove_zerocheck. terms: (coef, a, b-or-None) with coef a
+        canonical int; polys: per column Fr in-memory bytes (or device pointers
+        with on_device). Returns (rounds, finals, transcript) with rounds as
+        lists of 4 canonical ints and finals canonical ints."""
+        nt = len(terms)
+        coefs = to_mont_bytes([t[0] for t in terms])
+        ta = (ctypes.c_uint32 * max(nt, 1))(*[t[1] for t in terms])
+        tb = (ctypes.c_uint32 * max(nt, 1))(*[0xFFFFFFFF if t[2] is None else t[2] for t in terms])
+        k = len(polys)
+        snap = ctypes.create_string_buffer(bytes(transcript), TRANSCRIPT_BYTES)
+        rounds = ctypes.create_string_buffer(128 * max(num_vars, 1))
+        finals = ctypes.create_string_buffer(32 * k)
+        if on_device:
+            ptrs = (ctypes.c_void_p * k)(*polys)
+            st = lib().apg_prove_zerocheck_device(self._h, ctypes.c_size_t(k), coefs, ta, tb, ctypes.c_size_t(nt),
+                                                  ptrs, ctypes.c_size_t(num_vars), snap, rounds, finals)
+        else:
+            ptrs = (ctypes.c_char_p * k)(*polys)
+            st = lib().apg_prove_zerocheck(self._h, ctypes.c_size_t(k), coefs, ta, tb, ctypes.c_size_t(nt), ptrs,
+                                           ctypes.c_size_t(num_vars), snap, rounds, finals)
+        self._check(st)
+        rs = from_mont_bytes(rounds.raw[:128 * num_vars])
+        return [rs[4 * i:4 * i + 4] for i in range(num_vars)], from_mont_bytes(finals.raw), snap.raw
+
+    def witness_digest(self, cols, num_vars: int) -> int:
+        k = len(cols)
+        ptrs = (ctypes.c_char_p * k)(*cols)
+        out = ctypes.create_string_buffer(32)
+        self._check(lib().apg_witness_digest(self._h, ptrs, ctypes.c_size_t(k), ctypes.c_size_t(num_vars), out))
+        return from_mont_bytes(out.raw)[0]
 
     TIMER_MSM_ACCUMULATE, TIMER_MSM_TOTAL, TIMER_SUMCHECK_ROUND, TIMER_GKR_FORWARD, TIMER_MERCURY_PASS = range(5)
 

@@ -2,6 +2,7 @@
 // reference's refusal order, context locking, and the mapping of every
 // failure to an apg_status. No exception crosses this file's functions.
 #include "common.cuh"
+#include "sumcheck.cuh"
 
 using namespace apg;
 
@@ -259,6 +260,54 @@ int apg_fr_to_mont_device(apg_ctx* ctx, void* d_vals, size_t n) {
     c.check_flags();
     return (int)APG_OK;
   });
+}
+
+int apg_prove_zerocheck(apg_ctx* ctx, size_t arity, const uint8_t* coefs, const uint32_t* a, const uint32_t* b,
+                        size_t nterms, const uint8_t* const* polys, size_t num_vars, uint8_t* transcript,
+                        uint8_t* rounds_out, uint8_t* finals_out) {
+  return guarded(ctx, [&](Ctx& c) {
+    return prove_zerocheck_impl(c, arity, coefs, a, b, nterms, polys, false, num_vars, transcript, rounds_out,
+                                finals_out);
+  });
+}
+
+int apg_prove_zerocheck_device(apg_ctx* ctx, size_t arity, const uint8_t* coefs, const uint32_t* a,
+                               const uint32_t* b, size_t nterms, const void* const* d_polys, size_t num_vars,
+                               uint8_t* transcript, uint8_t* rounds_out, uint8_t* finals_out) {
+  return guarded(ctx, [&](Ctx& c) {
+    return prove_zerocheck_impl(c, arity, coefs, a, b, nterms, (const uint8_t* const*)d_polys, true, num_vars,
+                                transcript, rounds_out, finals_out);
+  });
+}
+
+int apg_witness_digest(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_t num_vars, uint8_t out[32]) {
+  return guarded(ctx, [&](Ctx& c) { return witness_digest_impl(c, cols, k, num_vars, out); });
+}
+
+void apg_transcript_init(uint8_t snapshot[226]) {
+  if (snapshot) host::Transcript().save(snapshot);
+}
+
+int apg_transcript_append_scalars(uint8_t snapshot[226], uint64_t tag, const uint8_t* xs, size_t n) {
+  host::Transcript tr;
+  if (!snapshot || (n && !xs) || !tr.load(snapshot)) return APG_ERR_INVALID_ARGUMENT;
+  std::vector<host::F> v(n);
+  for (size_t i = 0; i < n; ++i) {
+    memcpy(v[i].w, xs + 32 * i, 32);
+    if (!host::below_p(v[i].w)) return APG_ERR_NONCANONICAL;
+  }
+  tr.absorb(tag, v);
+  tr.save(snapshot);
+  return APG_OK;
+}
+
+int apg_transcript_challenge(uint8_t snapshot[226], uint64_t tag, uint8_t out[32]) {
+  host::Transcript tr;
+  if (!snapshot || !out || !tr.load(snapshot)) return APG_ERR_INVALID_ARGUMENT;
+  host::F x = tr.challenge(tag);
+  memcpy(out, x.w, 32);
+  tr.save(snapshot);
+  return APG_OK;
 }
 
 int apg_ctx_set_timing(apg_ctx* ctx, int on) {

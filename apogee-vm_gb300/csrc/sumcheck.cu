@@ -1,0 +1,291 @@
+// The sumcheck prover on the device: one fused kernel per round folds every
+// table with the previous round's challenge and evaluates the round's cubic
+// at X = 0..3, reduced over the hypercube; the host draws the next challenge.
+//
+// Restates crates/sumcheck/src/lib.rs (prove_zerocheck :359-408,
+// round_evaluations :324-349) and crates/gkr/src/lib.rs (prove_sumcheck
+// :792-899): per pair (2i, 2i+1) of every table the line lo + X*(hi - lo),
+// the summand at the four nodes weighted by eq, SUMCHECK_ROUND then
+// SUMCHECK_CHALLENGE, and the bind f'(i) = f(2i) + r*(f(2i+1) - f(2i))
+// (crates/poly/src/lib.rs:156-185). Round r's kernel reads the level-(r-1)
+// tables once, writes the level-r tables once and never re-reads them.
+#include "sumcheck.cuh"
+
+namespace apg {
+
+namespace {
+
+constexpr int kRoundThreads = 128;
+
+struct RoundArgs {
+  int nd;                    // data tables (eq is separate)
+  int nv;                    // virtual tables
+  uint8_t vkinds[8];
+  const Fr* const* src;      // round-0 tables (nd data, then eq), device pointers
+  const Fr* in_base;         // previous level (when !in_is_src): table k at in_base + k * in_len
+  size_t in_len;
+  int in_is_src;
+  int bind;                  // fold the previous level with c first
+  Fr c;
+  Fr* out_base;              // this level (when bind): table k at out_base + k * (in_len / 2)
+  size_t npairs;
+  int slots_step0;           // first step slot
+  int n_val_slots;           // nd + nv
+};
+
+__device__ __forceinline__ const Fr* table_in(const RoundArgs& A, int k) {
+  return A.in_is_src ? A.src[k] : A.in_base + (size_t)k * A.in_len;
+}
+
+__device__ __forceinline__ void load_line(const RoundArgs& A, int k, size_t i, Fr& lo, Fr& hi) {
+  const Fr* t = table_in(A, k);
+  if (!A.bind) {
+    lo = ld_fe(&t[2 * i]);
+    hi = ld_fe(&t[2 * i + 1]);
+    return;
+  }
+  Fr a0 = ld_fe(&t[4 * i]), a1 = ld_fe(&t[4 * i + 1]), a2 = ld_fe(&t[4 * i + 2]), a3 = ld_fe(&t[4 * i + 3]);
+  lo = fe_add(a0, fe_mul(A.c, fe_sub(a1, a0)));
+  hi = fe_add(a2, fe_mul(A.c, fe_sub(a3, a2)));
+  Fr* o = A.out_base + (size_t)k * (A.in_len / 2);
+  st_fe(&o[2 * i], lo);
+  st_fe(&o[2 * i + 1], hi);
+}
+
+__global__ void __launch_bounds__(kRoundThreads) k_round(RoundArgs A, DevProgram P, VirtualRound V, Fr* partials) {
+  extern __shared__ uint32_t sm[];
+  __shared__ Fr red[kRoundThreads];
+  Fr acc[4];
+#pragma unroll
+  for (int x = 0; x < 4; ++x) acc[x] = fe_zero<FrConsts>();
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < A.npairs; i += stride) {
+    Fr lo, hi;
+    for (int k = 0; k < A.nd; ++k) {
+      load_line(A, k, i, lo, hi);
+      sm_st(sm, k, lo);
+      sm_st(sm, A.slots_step0 + k, fe_sub(hi, lo));
+    }
+    Fr e_lo, e_hi;
+    load_line(A, A.nd, i, e_lo, e_hi);
+    Fr e_step = fe_sub(e_hi, e_lo);
+    for (int v = 0; v < A.nv; ++v) {
+      virtual_line_dev(V, A.vkinds[v], i, lo, hi);
+      sm_st(sm, A.nd + v, lo);
+      sm_st(sm, A.slots_step0 + A.nd + v, hi);
+    }
+    for (int x = 0; x < 4; ++x) {
+      Fr s = eval_summand(P, sm);
+      acc[x] = fe_add(acc[x], fe_mul(e_lo, s));
+      if (x < 3) {
+        e_lo = fe_add(e_lo, e_step);
+        for (int k = 0; k < A.n_val_slots; ++k) sm_st(sm, k, fe_add(sm_ld(sm, k), sm_ld(sm, A.slots_step0 + k)));
+      }
+    }
+  }
+  // Block reduction, one node at a time through shared memory.
+  for (int x = 0; x < 4; ++x) {
+    red[threadIdx.x] = acc[x];
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+      if (threadIdx.x < (unsigned)off) red[threadIdx.x] = fe_add(red[threadIdx.x], red[threadIdx.x + off]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) st_fe(&partials[(size_t)blockIdx.x * 4 + x], red[0]);
+    __syncthreads();
+  }
+}
+
+// Sum `nblocks` groups of 4 partials into out[0..4).
+__global__ void k_round_total(const Fr* partials, int nblocks, Fr* out) {
+  __shared__ Fr red[256];
+  for (int x = 0; x < 4; ++x) {
+    Fr a = fe_zero<FrConsts>();
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) a = fe_add(a, ld_fe(&partials[(size_t)b * 4 + x]));
+    red[threadIdx.x] = a;
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+      if (threadIdx.x < (unsigned)off) red[threadIdx.x] = fe_add(red[threadIdx.x], red[threadIdx.x + off]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) st_fe(&out[x], red[0]);
+    __syncthreads();
+  }
+}
+
+// Tables of length 2 -> their bound value (the last round's fold).
+__global__ void k_final_bind(const Fr* const* src, const Fr* in_base, size_t in_len, int in_is_src, int nt, Fr c,
+                             Fr* out) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt) return;
+  const Fr* t = in_is_src ? src[k] : in_base + (size_t)k * in_len;
+  Fr a0 = ld_fe(&t[0]), a1 = ld_fe(&t[1]);
+  st_fe(&out[k], fe_add(a0, fe_mul(c, fe_sub(a1, a0))));
+}
+
+// eq(r, y) for every y < 2^n: prod_j (y_j ? r_j : 1 - r_j).
+__global__ void k_eq_table(const Fr* r, int n, size_t len, Fr* out) {
+  size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (y >= len) return;
+  Fr acc = fe_one<FrConsts>();
+  for (int j = 0; j < n; ++j) {
+    Fr rj = ld_fe(&r[j]);
+    acc = fe_mul(acc, ((y >> j) & 1) ? rj : fe_sub(fe_one<FrConsts>(), rj));
+  }
+  st_fe(&out[y], acc);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+
+using host::F;
+
+static Fr to_dev(const F& a) {
+  Fr r;
+  memcpy(r.v, a.w, 32);
+  return r;
+}
+
+void build_eq_table(Ctx& c, const std::vector<F>& r, Fr* out) {
+  const size_t len = (size_t)1 << r.size();
+  Fr* d_r = c.scratch[S_TMP4].as<Fr>(std::max<size_t>(r.size(), 1));
+  if (!r.empty()) APG_CUDA(cudaMemcpyAsync(d_r, r.data(), 32 * r.size(), cudaMemcpyHostToDevice, c.stream));
+  launch(c, k_eq_table, (unsigned)((len + 255) / 256), 256, 0, (const Fr*)d_r, (int)r.size(), len, out);
+}
+
+static VirtualRound virtual_round(const std::vector<F>& point, int nvars) {
+  using namespace host;
+  VirtualRound V;
+  memset(&V, 0, sizeof(V));
+  const int b = (int)point.size();
+  V.bound = b;
+  V.nvars = nvars;
+  F row = fzero(), r19 = fzero(), r16 = fzero(), q = fone(), pw = fone();
+  for (int j = 0; j < b; ++j) {
+    F t = fmul(point[j], pw);
+    row = fadd(row, t);
+    if (j < 19) r19 = fadd(r19, t);
+    if (j < 16) r16 = fadd(r16, t);
+    if (j >= 14) q = fmul(q, fsub(fone(), point[j]));
+    if (j < 16) V.r16[j] = to_dev(point[j]);
+    pw = fadd(pw, pw);
+  }
+  V.row_prefix = to_dev(row);
+  V.range19_prefix = to_dev(r19);
+  V.range16_prefix = to_dev(r16);
+  V.ram_q = to_dev(q);
+  V.pow2_b = to_dev(pw);
+  return V;
+}
+
+void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint8_t>& vkinds, int n_cached,
+                  const std::vector<const Fr*>& src, const std::vector<F>& eq_point, host::Transcript& tr,
+                  std::vector<std::array<F, 4>>& rounds, std::vector<F>& point, std::vector<F>& finals) {
+  const int n = (int)eq_point.size();
+  const int nt = nd + 1;  // with eq
+  if (vkinds.size() > 8) throw Error(APG_ERR_BAD_CIRCUIT, "more than 8 virtual tables");
+  rounds.clear();
+  point.clear();
+  finals.assign(nd, host::fzero());
+
+  // Round-0 sources: the data tables, then eq built from the eq point.
+  const size_t len0 = (size_t)1 << n;
+  Fr* eq = c.scratch[S_TMP3].as<Fr>(len0);
+  build_eq_table(c, eq_point, eq);
+  std::vector<const Fr*> srcs(src);
+  srcs.push_back(eq);
+  const Fr** d_src = c.scratch[S_TMP5].as<const Fr*>(nt);
+  APG_CUDA(cudaMemcpyAsync(d_src, srcs.data(), sizeof(Fr*) * nt, cudaMemcpyHostToDevice, c.stream));
+
+  // Level buffers: level r (r >= 1) holds nt tables of 2^(n-r) entries.
+  Fr* lvl[2] = {nullptr, nullptr};
+  if (n >= 2) {
+    lvl[1] = c.scratch[S_LEVEL_A].as<Fr>((size_t)nt * (len0 / 2));
+    lvl[0] = c.scratch[S_LEVEL_B].as<Fr>((size_t)nt * (len0 / 4 > 0 ? len0 / 4 : 1));
+  }
+  const int n_val = nd + (int)vkinds.size();
+  const int slots = 2 * n_val + n_cached;
+  const size_t smem = (size_t)std::max(slots, 1) * 32 * kRoundThreads;
+  if (smem > 200 * 1024) throw Error(APG_ERR_BAD_CIRCUIT, "gate list too wide for one thread block");
+  APG_CUDA(cudaFuncSetAttribute(k_round, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  const int max_blocks = c.sm_count * 8;
+  Fr* partials = c.scratch[S_TMP6].as<Fr>((size_t)max_blocks * 4);
+  Fr* d_out = c.scratch[S_RESULT].as<Fr>(4);
+  DevProgram P = prog;
+  P.cached_slot0 = n_val;
+
+  F chal = host::fzero();
+  for (int r = 0; r < n; ++r) {
+    RoundArgs A;
+    memset(&A, 0, sizeof(A));
+    A.nd = nd;
+    A.nv = (int)vkinds.size();
+    for (size_t v = 0; v < vkinds.size(); ++v) A.vkinds[v] = vkinds[v];
+    A.src = d_src;
+    A.bind = r > 0;
+    A.c = to_dev(chal);
+    A.in_is_src = r <= 1;
+    A.in_len = (size_t)1 << (n - r + (r > 0 ? 1 : 0));
+    A.in_base = r >= 2 ? lvl[(r - 1) & 1] : nullptr;
+    A.out_base = r >= 1 ? lvl[r & 1] : nullptr;
+    A.npairs = (size_t)1 << (n - r - 1);
+    A.slots_step0 = n_val + n_cached;
+    A.n_val_slots = n_val;
+    VirtualRound V = virtual_round(point, n);
+    const int blocks = (int)std::min<size_t>((A.npairs + kRoundThreads - 1) / kRoundThreads, (size_t)max_blocks);
+    cudaEvent_t t0 = c.timer_begin();
+    launch(c, k_round, blocks, kRoundThreads, smem, A, P, V, partials);
+    c.timer_end(APG_TIMER_SUMCHECK_ROUND, t0);
+    launch(c, k_round_total, 1, 256, 0, (const Fr*)partials, blocks, d_out);
+    F v[4];
+    APG_CUDA(cudaMemcpyAsync(v, d_out, 128, cudaMemcpyDeviceToHost, c.stream));
+    APG_CUDA(cudaStreamSynchronize(c.stream));
+    auto g = host::cubic_through(v);
+    tr.absorb(host::T_SUMCHECK_ROUND, g.data(), 4);
+    chal = tr.challenge(host::T_SUMCHECK_CHALLENGE);
+    rounds.push_back(g);
+    point.push_back(chal);
+  }
+  // The last fold: every table bound to the full point.
+  Fr* d_fin = c.scratch[S_TMP7].as<Fr>(nt);
+  if (n == 0) {
+    for (int k = 0; k < nd; ++k) APG_CUDA(cudaMemcpyAsync(&finals[k], src[k], 32, cudaMemcpyDeviceToHost, c.stream));
+  } else {
+    const Fr* base = n >= 2 ? lvl[(n - 1) & 1] : nullptr;
+    launch(c, k_final_bind, 1, 64, 0, (const Fr* const*)d_src, base, (size_t)2, n <= 1 ? 1 : 0, nd, to_dev(chal),
+           d_fin);
+    APG_CUDA(cudaMemcpyAsync(finals.data(), d_fin, 32 * (size_t)nd, cudaMemcpyDeviceToHost, c.stream));
+  }
+  APG_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+// A device copy of a resolved gate list.
+void upload_program(Ctx& c, const HostProgram& hp, DevProgram& P, int slot_cap) {
+  (void)slot_cap;
+  const size_t gb = hp.gates.size() * sizeof(DevGate);
+  const size_t ob = hp.ops.size() * sizeof(uint16_t);
+  const size_t cb = hp.coeffs.size() * 32;
+  const size_t wb = hp.weights.size() * 32;
+  const size_t total = gb + ob + cb + wb + 256;
+  uint8_t* d = c.scratch[S_TMP2].as<uint8_t>(total);
+  std::vector<uint8_t> h(total, 0);
+  size_t off = 0;
+  auto put = [&](const void* p, size_t n) {
+    size_t at = (off + 31) & ~(size_t)31;
+    if (n) memcpy(h.data() + at, p, n);
+    off = at + n;
+    return d + at;
+  };
+  P.gates = (const DevGate*)put(hp.gates.data(), gb);
+  P.ops = (const uint16_t*)put(hp.ops.data(), ob);
+  P.coeffs = (const Fr*)put(hp.coeffs.data(), cb);
+  P.weights = (const Fr*)put(hp.weights.data(), wb);
+  P.n_cached = hp.n_cached;
+  P.n_weighted = hp.n_weighted;
+  APG_CUDA(cudaMemcpyAsync(d, h.data(), off, cudaMemcpyHostToDevice, c.stream));
+}
+
+}  // namespace apg

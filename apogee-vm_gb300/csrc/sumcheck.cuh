@@ -1,0 +1,40 @@
+// Shared declarations of the sumcheck engine (sumcheck.cu) and its callers
+// (the zerocheck and GKR entry points).
+#pragma once
+#include <array>
+
+#include "common.cuh"
+#include "host_fr.hpp"
+#include "summand.cuh"
+
+namespace apg {
+
+// A resolved gate list as the host builds it. Slot numbering: data tables
+// [0, nd), virtual tables [nd, nd + nv), cached entries after them.
+struct HostProgram {
+  std::vector<DevGate> gates;
+  std::vector<uint16_t> ops;
+  std::vector<host::F> coeffs;
+  std::vector<host::F> weights;
+  int n_cached = 0;
+  int n_weighted = 0;
+};
+
+void upload_program(Ctx& c, const HostProgram& hp, DevProgram& P, int slot_cap);
+void build_eq_table(Ctx& c, const std::vector<host::F>& r, Fr* out);
+
+// Prove sum_y eq(eq_point, y) * S(y) over `src` tables (nd of them, each
+// 2^|eq_point| entries, device memory), drawing challenges from `tr`. Returns
+// the rounds' ascending coefficients, the bound point and each data table's
+// final value.
+void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint8_t>& vkinds, int n_cached,
+                  const std::vector<const Fr*>& src, const std::vector<host::F>& eq_point, host::Transcript& tr,
+                  std::vector<std::array<host::F, 4>>& rounds, std::vector<host::F>& point,
+                  std::vector<host::F>& finals);
+
+int prove_zerocheck_impl(Ctx& c, size_t arity, const uint8_t* coefs, const uint32_t* ta, const uint32_t* tb,
+                         size_t nterms, const uint8_t* const* polys, bool polys_on_device, size_t num_vars,
+                         uint8_t* transcript, uint8_t* rounds_out, uint8_t* finals_out);
+int witness_digest_impl(Ctx& c, const uint8_t* const* cols, size_t k, size_t num_vars, uint8_t out[32]);
+
+}  // namespace apg

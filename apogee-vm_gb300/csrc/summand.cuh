@@ -1,0 +1,216 @@
+// The gate kernel on the device: a resolved gate list evaluated from
+// per-thread value slots in shared memory.
+//
+// Restates crates/gkr-verify/src/lib.rs: eval_gate (:142-202) over the seven
+// GateDef shapes, ResolvedList's evaluation order (cached entries first, then
+// producing, then enforcing gates, :315-480) and the virtual tables' closed
+// forms (virtual_at_row / virtual_at_point, :205-286). A zerocheck Gate
+// (crates/sumcheck/src/lib.rs:109-169) is the one-gate list
+// `Quadratic { 0, linear terms, product terms }` with weight 1.
+//
+// Slots hold one Fr each, word-major across the block's threads so that a
+// warp's 32-bit accesses fall in distinct banks: word w of slot s of thread t
+// sits at smem[(s * 8 + w) * blockDim.x + t].
+#pragma once
+#include "field.cuh"
+
+namespace apg {
+
+enum GateKind : uint8_t { G_LINEAR = 0, G_PRODUCT = 1, G_MASK = 2, G_AFFINE = 3, G_TREE_PRODUCT = 4,
+                          G_TREE_CROSS = 5, G_QUADRATIC = 6 };
+
+enum VirtualKindDev : uint8_t { V_ROW = 0, V_RAM_LIVE = 1, V_RANGE19 = 2, V_RANGE16 = 3, V_XOR8A = 4, V_XOR8B = 5,
+                                V_XOR8OUT = 6 };
+
+struct DevGate {
+  uint8_t kind;
+  uint8_t pad;
+  uint16_t nops;
+  uint16_t p1, p2;   // shape: Linear t; Affine t, u; Quadratic t, u
+  uint32_t op_off;   // first operand slot index in ops[]
+  uint32_t cf_off;   // first coefficient in coeffs[]
+};
+
+// A resolved list on the device. Gates [0, n_cached) fill the cached slots in
+// order; gates [n_cached, n_cached + n_weighted) are summed with weights.
+struct DevProgram {
+  const DevGate* gates;
+  const uint16_t* ops;  // slot indices
+  const Fr* coeffs;     // Montgomery, challenges already substituted
+  const Fr* weights;    // one per weighted gate (lambda^j), Montgomery
+  int n_cached;
+  int n_weighted;
+  int cached_slot0;     // slot of cached entry 0
+};
+
+__device__ __forceinline__ Fr sm_ld(const uint32_t* sm, int slot) {
+  Fr r;
+  const int nt = blockDim.x, t = threadIdx.x;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) r.v[w] = sm[(slot * 8 + w) * nt + t];
+  return r;
+}
+
+__device__ __forceinline__ void sm_st(uint32_t* sm, int slot, const Fr& a) {
+  const int nt = blockDim.x, t = threadIdx.x;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) sm[(slot * 8 + w) * nt + t] = a.v[w];
+}
+
+__device__ __forceinline__ Fr ld_g(const Fr* p) { return ld_fe(p); }
+
+// Affine form sum_{i<t} c[i] * x_i + c[t], operands ops[0..t).
+__device__ __forceinline__ Fr affine_form(const uint32_t* sm, const uint16_t* ops, const Fr* c, int t) {
+  Fr acc = ld_g(&c[t]);
+  for (int i = 0; i < t; ++i) acc = fe_add(acc, fe_mul(ld_g(&c[i]), sm_ld(sm, ops[i])));
+  return acc;
+}
+
+static __device__ __noinline__ Fr eval_gate_dev(const DevProgram& P, int g, const uint32_t* sm) {
+  const DevGate G = P.gates[g];
+  const uint16_t* ops = P.ops + G.op_off;
+  const Fr* c = P.coeffs + G.cf_off;
+  switch (G.kind) {
+    case G_LINEAR:
+      return affine_form(sm, ops, c, G.p1);
+    case G_PRODUCT:
+      return fe_mul(fe_mul(ld_g(&c[0]), sm_ld(sm, ops[0])), sm_ld(sm, ops[1]));
+    case G_MASK: {
+      Fr x = sm_ld(sm, ops[0]), m = sm_ld(sm, ops[1]);
+      return fe_sub(fe_add(fe_mul(x, m), fe_one<FrConsts>()), m);
+    }
+    case G_AFFINE: {
+      const int t = G.p1, u = G.p2;
+      Fr l = affine_form(sm, ops, c, t);
+      Fr r = affine_form(sm, ops + t, c + t + 1, u);
+      return fe_mul(l, r);
+    }
+    case G_TREE_PRODUCT:
+      return fe_mul(sm_ld(sm, ops[0]), sm_ld(sm, ops[1]));
+    case G_TREE_CROSS:
+      return fe_add(fe_mul(sm_ld(sm, ops[0]), sm_ld(sm, ops[3])), fe_mul(sm_ld(sm, ops[1]), sm_ld(sm, ops[2])));
+    case G_QUADRATIC: {
+      const int t = G.p1, u = G.p2;
+      Fr acc = ld_g(&c[0]);
+      for (int i = 0; i < t; ++i) acc = fe_add(acc, fe_mul(ld_g(&c[1 + i]), sm_ld(sm, ops[i])));
+      for (int j = 0; j < u; ++j) {
+        Fr yz = fe_mul(sm_ld(sm, ops[t + 2 * j]), sm_ld(sm, ops[t + 2 * j + 1]));
+        acc = fe_add(acc, fe_mul(ld_g(&c[1 + t + j]), yz));
+      }
+      return acc;
+    }
+  }
+  return fe_zero<FrConsts>();
+}
+
+// Cached entries into their slots, then the weighted sum of the gates.
+__device__ __forceinline__ Fr eval_summand(const DevProgram& P, uint32_t* sm) {
+  for (int g = 0; g < P.n_cached; ++g) sm_st(sm, P.cached_slot0 + g, eval_gate_dev(P, g, sm));
+  Fr acc = fe_zero<FrConsts>();
+  for (int j = 0; j < P.n_weighted; ++j) {
+    Fr v = eval_gate_dev(P, P.n_cached + j, sm);
+    acc = fe_add(acc, fe_mul(v, ld_g(&P.weights[j])));
+  }
+  return acc;
+}
+
+// ---- virtual tables ----------------------------------------------------------
+
+__device__ __forceinline__ Fr fr_u64(uint64_t x) { return fe_from_u64<FrConsts>(x); }
+
+// Row y's value of a virtual table (virtual_at_row).
+__device__ __forceinline__ Fr virtual_at_row_dev(int kind, uint64_t y) {
+  switch (kind) {
+    case V_ROW: return fr_u64(y);
+    case V_RAM_LIVE: return y >= (1ull << 14) ? fe_one<FrConsts>() : fe_zero<FrConsts>();
+    case V_RANGE19: return fr_u64(y & ((1ull << 19) - 1));
+    case V_RANGE16: return fr_u64(y & ((1ull << 16) - 1));
+    case V_XOR8A: return fr_u64(y & 0xff);
+    case V_XOR8B: return fr_u64((y >> 8) & 0xff);
+    case V_XOR8OUT: return fr_u64((y & 0xff) ^ ((y >> 8) & 0xff));
+  }
+  return fe_zero<FrConsts>();
+}
+
+// Per-round constants of the closed forms, prepared on the host from the
+// challenges bound so far (r_0 .. r_{b-1}).
+struct VirtualRound {
+  int bound;          // b
+  int nvars;          // n: variables of the sumcheck
+  Fr row_prefix;      // sum_{j<b} 2^j r_j
+  Fr range19_prefix;  // sum_{j<min(b,19)} 2^j r_j
+  Fr range16_prefix;  // sum_{j<min(b,16)} 2^j r_j
+  Fr ram_q;           // prod_{14<=j<b} (1 - r_j)
+  Fr r16[16];         // r_j for j < min(b, 16)
+  Fr pow2_b;          // 2^b
+};
+
+// y_j of the point (r_0..r_{b-1}, X, bits of i) for j < 16, at X in {0, 1}.
+__device__ __forceinline__ Fr point_coord(const VirtualRound& V, uint64_t i, int j, int X) {
+  if (j >= V.nvars) return fe_zero<FrConsts>();
+  if (j < V.bound) return V.r16[j];
+  if (j == V.bound) return X ? fe_one<FrConsts>() : fe_zero<FrConsts>();
+  return ((i >> (j - V.bound - 1)) & 1) ? fe_one<FrConsts>() : fe_zero<FrConsts>();
+}
+
+__device__ __forceinline__ Fr xor8_at(const VirtualRound& V, int kind, uint64_t i, int X) {
+  Fr acc = fe_zero<FrConsts>();
+  for (int j = 7; j >= 0; --j) {
+    acc = fe_dbl(acc);
+    Fr y = point_coord(V, i, j, X), z = point_coord(V, i, j + 8, X);
+    if (kind == V_XOR8A) acc = fe_add(acc, y);
+    else if (kind == V_XOR8B) acc = fe_add(acc, z);
+    else {
+      Fr yz = fe_mul(y, z);
+      acc = fe_sub(fe_add(acc, fe_add(y, z)), fe_dbl(yz));
+    }
+  }
+  return acc;
+}
+
+// The line lo + X * step of a virtual table over pair i after b bound rounds.
+__device__ __forceinline__ void virtual_line_dev(const VirtualRound& V, int kind, uint64_t i, Fr& lo, Fr& step) {
+  const int b = V.bound;
+  switch (kind) {
+    case V_ROW:
+      lo = fe_add(V.row_prefix, fr_u64(i << (b + 1)));
+      step = V.pow2_b;
+      return;
+    case V_RANGE19:
+    case V_RANGE16: {
+      const int bits = kind == V_RANGE19 ? 19 : 16;
+      const Fr pre = kind == V_RANGE19 ? V.range19_prefix : V.range16_prefix;
+      if (b < bits) {
+        uint64_t low = (bits - b - 1) >= 63 ? i : (i & ((1ull << (bits - b - 1)) - 1));
+        lo = fe_add(pre, fr_u64(low << (b + 1)));
+        step = V.pow2_b;
+      } else {
+        lo = pre;
+        step = fe_zero<FrConsts>();
+      }
+      return;
+    }
+    case V_RAM_LIVE: {
+      const int sh = b >= 13 ? 0 : 13 - b;
+      const bool high_bit = (i >> sh) != 0;
+      if (high_bit) {
+        lo = fe_one<FrConsts>();
+        step = fe_zero<FrConsts>();
+      } else if (b >= 14) {
+        lo = fe_sub(fe_one<FrConsts>(), V.ram_q);
+        step = V.ram_q;
+      } else {
+        lo = fe_zero<FrConsts>();
+        step = fe_zero<FrConsts>();
+      }
+      return;
+    }
+    default: {
+      lo = xor8_at(V, kind, i, 0);
+      step = fe_sub(xor8_at(V, kind, i, 1), lo);
+      return;
+    }
+  }
+}
+
+}  // namespace apg

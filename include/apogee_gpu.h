@@ -122,6 +122,38 @@ int apg_commit_device(apg_ctx* ctx, const void* d_evals, size_t num_vars, uint8_
  * back on the context's stream and the call returns once all are done. */
 int apg_commit_batch_device(apg_ctx* ctx, const void* const* d_cols, size_t k, size_t num_vars, uint8_t* out);
 
+/* ---- zerocheck (crates/sumcheck/src/lib.rs) ------------------------------ */
+
+/* sumcheck::prove_zerocheck (lib.rs:359): prove that the gate
+ *   G = sum_t coefs[t] * x_{a[t]} * x_{b[t]}   (b[t] = 0xffffffff: no 2nd factor)
+ * over `arity` columns of 2^num_vars evaluations vanishes on the hypercube.
+ * coefs and columns are Fr in memory; polys[k] points at column k (host).
+ * The transcript (226-byte snapshot, in/out) must already hold the witness
+ * digest. Writes num_vars rounds of 4 ascending coefficients (rounds_out,
+ * num_vars x 128 bytes) and the columns' values at the bound point
+ * (finals_out, arity x 32), both Fr in memory. The columns are not modified:
+ * the reference's binding of them in place is the returned final values. */
+int apg_prove_zerocheck(apg_ctx* ctx, size_t arity, const uint8_t* coefs, const uint32_t* a, const uint32_t* b,
+                        size_t nterms, const uint8_t* const* polys, size_t num_vars, uint8_t* transcript,
+                        uint8_t* rounds_out, uint8_t* finals_out);
+/* As apg_prove_zerocheck with the columns in device memory. */
+int apg_prove_zerocheck_device(apg_ctx* ctx, size_t arity, const uint8_t* coefs, const uint32_t* a,
+                               const uint32_t* b, size_t nterms, const void* const* d_polys, size_t num_vars,
+                               uint8_t* transcript, uint8_t* rounds_out, uint8_t* finals_out);
+/* sumcheck::witness_digest (lib.rs:228-256): the Poseidon2 sponge over the
+ * column count, the variable count and every cell, squeezed once. Columns
+ * are host Fr in memory; out is Fr in memory. Inherently sequential. */
+int apg_witness_digest(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_t num_vars, uint8_t out[32]);
+
+/* ---- transcript (crates/transcript/src/lib.rs:214-346) ------------------- */
+
+/* A fresh transcript snapshot (Transcript::new). */
+void apg_transcript_init(uint8_t snapshot[226]);
+/* Transcript::append_scalars(tag, xs): xs are n Fr in memory. */
+int apg_transcript_append_scalars(uint8_t snapshot[226], uint64_t tag, const uint8_t* xs, size_t n);
+/* Transcript::challenge_scalar(tag) -> out (Fr in memory). */
+int apg_transcript_challenge(uint8_t snapshot[226], uint64_t tag, uint8_t out[32]);
+
 /* ---- utilities ---------------------------------------------------------- */
 
 /* Canonical Fr values in device memory -> Montgomery (in-memory) form, in
