@@ -83,6 +83,35 @@ def fe(x: int) -> bytes:
     return int(x).to_bytes(32, "little")
 
 
+class GkrValues:
+    """Device-resident layer values from gkr_forward (gkr::LayerValues)."""
+
+    def __init__(self, ctx, handle):
+        self.ctx = ctx
+        self.handle = handle
+
+    def read(self, layer: int, col: int):
+        L = lib()
+        L.apg_gkr_values_len.restype = ctypes.c_size_t
+        n = L.apg_gkr_values_len(self.handle, ctypes.c_size_t(layer))
+        out = ctypes.create_string_buffer(32 * n)
+        st = L.apg_gkr_values_read(self.handle, ctypes.c_size_t(layer), ctypes.c_size_t(col), out)
+        if st:
+            raise ApogeeError(st, "apg_gkr_values_read")
+        return from_mont_bytes(out.raw)
+
+    def free(self):
+        if self.handle:
+            lib().apg_gkr_values_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
 # ---------------------------------------------------------------------------
 # Transcript snapshots (crates/transcript/src/lib.rs)
 # ---------------------------------------------------------------------------
@@ -268,6 +297,36 @@ class Context:
         self._check(st)
         rs = from_mont_bytes(rounds.raw[:128 * num_vars])
         return [rs[4 * i:4 * i + 4] for i in range(num_vars)], from_mont_bytes(finals.raw), snap.raw
+
+    # ---- GKR ------------------------------------------------------------------
+    def gkr_forward(self, blob: bytes, base, challenges: dict):
+        """gkr::forward. base: committed columns as Fr in-memory bytes (layout
+        order); challenges: {slot: canonical int}. Returns a GkrValues handle."""
+        k = len(base)
+        ptrs = (ctypes.c_char_p * k)(*base)
+        slots = sorted(challenges)
+        sarr = (ctypes.c_uint32 * max(len(slots), 1))(*slots)
+        vals = to_mont_bytes([challenges[s] for s in slots])
+        h = ctypes.c_void_p()
+        self._check(lib().apg_gkr_forward(self._h, blob, ctypes.c_size_t(len(blob)), ptrs, sarr, vals,
+                                          ctypes.c_size_t(len(slots)), ctypes.byref(h)))
+        return GkrValues(self, h)
+
+    def gkr_prove(self, blob: bytes, values: "GkrValues", challenges: dict, transcript: bytes):
+        """gkr::prove. Returns (proof as canonical ints in the documented
+        layout, transcript)."""
+        L = lib()
+        L.apg_gkr_proof_len.restype = ctypes.c_size_t
+        cap = L.apg_gkr_proof_len(blob, ctypes.c_size_t(len(blob)))
+        out = ctypes.create_string_buffer(max(cap, 32))
+        n = ctypes.c_size_t()
+        slots = sorted(challenges)
+        sarr = (ctypes.c_uint32 * max(len(slots), 1))(*slots)
+        vals = to_mont_bytes([challenges[s] for s in slots])
+        snap = ctypes.create_string_buffer(bytes(transcript), TRANSCRIPT_BYTES)
+        self._check(L.apg_gkr_prove(self._h, blob, ctypes.c_size_t(len(blob)), values.handle, sarr, vals,
+                                    ctypes.c_size_t(len(slots)), snap, out, ctypes.c_size_t(cap), ctypes.byref(n)))
+        return from_mont_bytes(out.raw[:n.value]), snap.raw
 
     def witness_digest(self, cols, num_vars: int) -> int:
         k = len(cols)

@@ -284,6 +284,60 @@ int apg_witness_digest(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_
   return guarded(ctx, [&](Ctx& c) { return witness_digest_impl(c, cols, k, num_vars, out); });
 }
 
+struct apg_gkr_values {
+  GkrValues* v;
+  apg_ctx* ctx;
+};
+
+int apg_gkr_forward(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, const uint8_t* const* base,
+                    const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, apg_gkr_values** out) {
+  if (!out) return APG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  return guarded(ctx, [&](Ctx& c) {
+    GkrValues* v = gkr_forward_impl(c, circuit, circuit_len, base, false, slots, slot_values, n_slots);
+    *out = new apg_gkr_values{v, ctx};
+    return (int)APG_OK;
+  });
+}
+
+int apg_gkr_values_read(apg_gkr_values* values, size_t layer, size_t col, uint8_t* out) {
+  if (!values) return APG_ERR_INVALID_ARGUMENT;
+  return guarded(values->ctx, [&](Ctx&) { return gkr_values_read_impl(values->v, layer, col, out); });
+}
+
+size_t apg_gkr_values_len(apg_gkr_values* values, size_t layer) {
+  return values ? gkr_values_len(values->v, layer) : 0;
+}
+
+void apg_gkr_values_free(apg_gkr_values* values) {
+  if (!values) return;
+  if (values->ctx) {
+    std::lock_guard<std::mutex> lock(values->ctx->c.mu);
+    cudaSetDevice(values->ctx->c.device);
+    cudaStreamSynchronize(values->ctx->c.stream);
+    gkr_values_free(values->v);
+  }
+  delete values;
+}
+
+size_t apg_gkr_proof_len(const uint8_t* circuit, size_t circuit_len) {
+  try {
+    return gkr_proof_len_impl(circuit, circuit_len);
+  } catch (...) {
+    return 0;
+  }
+}
+
+int apg_gkr_prove(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, apg_gkr_values* values,
+                  const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, uint8_t* transcript,
+                  uint8_t* proof_out, size_t proof_cap, size_t* proof_len) {
+  if (!values || values->ctx != ctx) return APG_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&](Ctx& c) {
+    return gkr_prove_impl(c, circuit, circuit_len, values->v, slots, slot_values, n_slots, transcript, proof_out,
+                          proof_cap, proof_len);
+  });
+}
+
 void apg_transcript_init(uint8_t snapshot[226]) {
   if (snapshot) host::Transcript().save(snapshot);
 }

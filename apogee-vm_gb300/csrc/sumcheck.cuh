@@ -37,4 +37,18 @@ int prove_zerocheck_impl(Ctx& c, size_t arity, const uint8_t* coefs, const uint3
                          uint8_t* transcript, uint8_t* rounds_out, uint8_t* finals_out);
 int witness_digest_impl(Ctx& c, const uint8_t* const* cols, size_t k, size_t num_vars, uint8_t out[32]);
 
+struct Circuit;
+struct GkrValues;
+Circuit parse_circuit_blob(const uint8_t* blob, size_t len);
+size_t gkr_proof_elems(const Circuit& C);
+GkrValues* gkr_forward_impl(Ctx& c, const uint8_t* blob, size_t blob_len, const uint8_t* const* base,
+                            bool base_on_device, const uint32_t* slots, const uint8_t* slot_values, size_t n_slots);
+int gkr_prove_impl(Ctx& c, const uint8_t* blob, size_t blob_len, GkrValues* V, const uint32_t* slots,
+                   const uint8_t* slot_values, size_t n_slots, uint8_t* transcript, uint8_t* proof_out,
+                   size_t proof_cap, size_t* proof_len);
+void gkr_values_free(GkrValues* v);
+int gkr_values_read_impl(GkrValues* v, size_t layer, size_t col, uint8_t* out);
+size_t gkr_values_len(GkrValues* v, size_t layer);
+size_t gkr_proof_len_impl(const uint8_t* blob, size_t len);
+
 }  // namespace apg

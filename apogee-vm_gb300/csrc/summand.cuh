@@ -22,6 +22,10 @@ enum GateKind : uint8_t { G_LINEAR = 0, G_PRODUCT = 1, G_MASK = 2, G_AFFINE = 3,
 enum VirtualKindDev : uint8_t { V_ROW = 0, V_RAM_LIVE = 1, V_RANGE19 = 2, V_RANGE16 = 3, V_XOR8A = 4, V_XOR8B = 5,
                                 V_XOR8OUT = 6 };
 
+struct VirtualKinds {
+  uint8_t k[8];
+};
+
 struct DevGate {
   uint8_t kind;
   uint8_t pad;

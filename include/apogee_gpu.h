@@ -145,6 +145,52 @@ int apg_prove_zerocheck_device(apg_ctx* ctx, size_t arity, const uint8_t* coefs,
  * are host Fr in memory; out is Fr in memory. Inherently sequential. */
 int apg_witness_digest(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_t num_vars, uint8_t out[32]);
 
+/* ---- GKR (crates/gkr/src/lib.rs) ----------------------------------------- */
+
+/* A circuit crosses the boundary as an "APGC" blob: the resolved form of a
+ * constraints::CircuitArtifact (crates/constraints/src/lib.rs:549-672) that
+ * the prover reads, all integers u32 little-endian, literals 32-byte
+ * canonical Fr:
+ *   'APGC'(0x43475041) version(1) trace_vars n_committed
+ *   n_virtuals kind[n_virtuals]        (0 RowIndex, 1 RamLive, 2 Range19,
+ *                                       3 Range16, 4 Xor8A, 5 Xor8B, 6 Xor8Out)
+ *   n_outputs offset[n_outputs]        (top-layer columns, output-map order)
+ *   depth, then per gate list k:
+ *     halving num_vars(k+1) width(k+1) n_cached n_producing n_enforcing
+ *     gates (cached, producing, enforcing), each:
+ *       kind (0 Linear 1 Product 2 MaskIntoIdentity 3 AffineProduct
+ *             4 TreeProduct 5 TreeCross 6 Quadratic) p1 p2 (Linear t; Affine
+ *             t, u; Quadratic t, u; else 0)
+ *       n_operands, (source, index)*  source 0 = column of layer k (layout
+ *             order M, W, S at k = 0), 1 = virtual table, 2 = cached entry
+ *       n_coeffs, (is_challenge, slot | Fr)*  in GateDef::coefficients order
+ * Operand and coefficient orders are GateDef::operands / coefficients
+ * (crates/constraints/src/lib.rs:375-421). Malformed blobs return
+ * APG_ERR_BAD_CIRCUIT before any device work. */
+typedef struct apg_gkr_values apg_gkr_values;
+
+/* gkr::forward (lib.rs:279): materialise every layer on the device. base
+ * holds n_committed host column pointers (Fr in memory, 2^trace_vars each);
+ * the external challenges are slots[i] -> slot_values[i] (Fr in memory). The
+ * values stay resident until apg_gkr_values_free. */
+int apg_gkr_forward(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, const uint8_t* const* base,
+                    const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, apg_gkr_values** out);
+/* Read column `col` of layer `layer` (0 = base) into out (Fr in memory). */
+int apg_gkr_values_read(apg_gkr_values* values, size_t layer, size_t col, uint8_t* out);
+/* Entries per column of layer `layer`. */
+size_t apg_gkr_values_len(apg_gkr_values* values, size_t layer);
+void apg_gkr_values_free(apg_gkr_values* values);
+/* Bytes of the proof apg_gkr_prove writes for this circuit (0 if malformed). */
+size_t apg_gkr_proof_len(const uint8_t* circuit, size_t circuit_len);
+/* gkr::prove (lib.rs:933): the backward pass over forward's values, on a
+ * transcript the caller has bound to the base (226-byte snapshot, in/out).
+ * The proof (GkrProof, crates/gkr-verify/src/lib.rs:90-92) is written as, for
+ * each gate list k = 0 .. depth-1, its rounds (4 Fr each) then its claims,
+ * all Fr in memory. */
+int apg_gkr_prove(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, apg_gkr_values* values,
+                  const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, uint8_t* transcript,
+                  uint8_t* proof_out, size_t proof_cap, size_t* proof_len);
+
 /* ---- transcript (crates/transcript/src/lib.rs:214-346) ------------------- */
 
 /* A fresh transcript snapshot (Transcript::new). */
