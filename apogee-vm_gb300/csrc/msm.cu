@@ -636,4 +636,199 @@ void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* 
   }
 }
 
+// ---------------------------------------------------------------------------
+// The allocation-free MSM (apg_msm_noalloc).
+//
+// Some callers cannot let a library allocate device memory on their behalf:
+// a serving loop that has already promised every byte of HBM to admitted
+// requests (a cudaMalloc there can fail a request that was admitted, or push
+// another tenant out of memory), or a latency-critical pipeline that cannot
+// afford the device-wide synchronisation cudaMalloc and cudaFree imply. For
+// them this variant of the MSM runs the same kernels with all of its scratch
+// in one fixed array that lives in the module's global memory, reserved when
+// the library is loaded and held by every GPU that loads it until the
+// process exits. It calls no cudaMalloc, no cudaFree and no allocating
+// library routine.
+//
+// Limit: at most kNoAllocMaxPoints bases. The plan is fixed: 9-bit signed
+// windows (29 of them) with one bucket set per window, 16 entries per
+// accumulation segment, so every buffer has a size known at compile time.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr size_t kNoAllocMaxPoints = 4096;
+constexpr int kNoAllocC = 9;
+constexpr int kNoAllocWindows = (254 + 1 + kNoAllocC - 1) / kNoAllocC;  // 29
+constexpr int kNoAllocK = 1 << (kNoAllocC - 1);                          // 256 buckets a window
+constexpr size_t kNoAllocBins = (size_t)kNoAllocWindows * kNoAllocK;
+constexpr size_t kNoAllocEntries = (size_t)kNoAllocWindows * kNoAllocMaxPoints;
+constexpr int kNoAllocSeg = 16;
+constexpr size_t kNoAllocSegs = (kNoAllocEntries + kNoAllocSeg - 1) / kNoAllocSeg;
+constexpr int kNoAllocG0 = kNoAllocK / kLevelFan;  // 32 groups in the first reduction level
+constexpr int kNoAllocLevels = 3;                  // 256 -> 32 -> 4 -> one group
+
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Byte offsets of every buffer inside the array.
+constexpr size_t kOffFlags = 0;
+constexpr size_t kOffTotal = kOffFlags + 256;
+constexpr size_t kOffResult = kOffTotal + 256;
+constexpr size_t kOffBases = kOffResult + 256;
+constexpr size_t kOffEntries = kOffBases + align256(kNoAllocMaxPoints * sizeof(Affine));
+constexpr size_t kOffSorted = kOffEntries + align256(kNoAllocEntries * 8);
+constexpr size_t kOffCounts = kOffSorted + align256(kNoAllocEntries * 8);
+constexpr size_t kOffScanBlk = kOffCounts + align256((kNoAllocBins + 1) * 4);
+constexpr size_t kOffBuckets = kOffScanBlk + align256((kScanBlock + 1) * 4);
+constexpr size_t kOffKeys0 = kOffBuckets + align256(kNoAllocBins * sizeof(Xyzz));
+constexpr size_t kOffKeys1 = kOffKeys0 + align256(2 * kNoAllocSegs * 4);
+constexpr size_t kOffPts0 = kOffKeys1 + align256(2 * kNoAllocSegs * 4);
+constexpr size_t kOffPts1 = kOffPts0 + align256(2 * kNoAllocSegs * sizeof(Xyzz));
+constexpr size_t kOffPres0 = kOffPts1 + align256(2 * kNoAllocSegs * sizeof(Xyzz));
+constexpr size_t kOffPres1 = kOffPres0 + align256(2 * kNoAllocSegs);
+constexpr size_t kOffLvlT = kOffPres1 + align256(2 * kNoAllocSegs);
+constexpr size_t kOffLvlA = kOffLvlT + align256((size_t)kNoAllocWindows * kNoAllocG0 * sizeof(Xyzz));
+constexpr size_t kOffLvlB = kOffLvlA + align256((size_t)kNoAllocWindows * kNoAllocG0 * sizeof(Xyzz));
+constexpr size_t kOffTsum = kOffLvlB + align256((size_t)kNoAllocWindows * kNoAllocG0 * sizeof(Xyzz));
+constexpr size_t kNoAllocBytes = kOffTsum + align256((size_t)kNoAllocLevels * kNoAllocWindows * sizeof(Xyzz));
+
+}  // namespace
+
+// The scratch itself (about 8.5 MB). In host code this name is only a
+// stand-in for the device symbol: its device address comes from
+// cudaGetSymbolAddress, once per device.
+static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[256] = {nullptr};
+
+// The array's device address on the current device, looked up on the first
+// call made with that device current.
+int noalloc_scratch(int device, uint8_t** out) {
+  if (device < 0 || device >= 256) return APG_ERR_NO_DEVICE;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) return APG_ERR_CUDA;
+    g_noalloc_addr[device] = p;
+  }
+  *out = (uint8_t*)g_noalloc_addr[device];
+  return APG_OK;
+}
+
+#define APG_NA(call)                                \
+  do {                                              \
+    if ((call) != cudaSuccess) return APG_ERR_CUDA; \
+  } while (0)
+#define APG_NA_LAUNCH()                                     \
+  do {                                                      \
+    if (cudaGetLastError() != cudaSuccess) return APG_ERR_CUDA; \
+  } while (0)
+
+int msm_noalloc(const void* d_bases, const void* d_scalars, size_t n, void* d_out, cudaStream_t st) {
+  if (n > kNoAllocMaxPoints) return APG_ERR_NOALLOC_TOO_LARGE;
+  if (!d_out || (n && (!d_bases || !d_scalars))) return APG_ERR_INVALID_ARGUMENT;
+  int device = 0;
+  APG_NA(cudaGetDevice(&device));
+  uint8_t* s = nullptr;
+  int rc = noalloc_scratch(device, &s);
+  if (rc) return rc;
+  if (n == 0) {
+    APG_NA(cudaMemsetAsync(d_out, 0, 64, st));
+    APG_NA(cudaStreamSynchronize(st));
+    return APG_OK;
+  }
+  int sms = 0;
+  APG_NA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  (void)sms;
+  uint32_t* flags = (uint32_t*)(s + kOffFlags);
+  uint32_t* total = (uint32_t*)(s + kOffTotal);
+  Affine* bases = (Affine*)(s + kOffBases);
+  uint64_t* entries = (uint64_t*)(s + kOffEntries);
+  uint64_t* sorted = (uint64_t*)(s + kOffSorted);
+  uint32_t* counts = (uint32_t*)(s + kOffCounts);
+  uint32_t* blk = (uint32_t*)(s + kOffScanBlk);
+  Xyzz* buckets = (Xyzz*)(s + kOffBuckets);
+  uint32_t* ikeys[2] = {(uint32_t*)(s + kOffKeys0), (uint32_t*)(s + kOffKeys1)};
+  Xyzz* ipts[2] = {(Xyzz*)(s + kOffPts0), (Xyzz*)(s + kOffPts1)};
+  uint8_t* ipres[2] = {s + kOffPres0, s + kOffPres1};
+  Xyzz* outT = (Xyzz*)(s + kOffLvlT);
+  Xyzz* lvlA = (Xyzz*)(s + kOffLvlA);
+  Xyzz* lvlB = (Xyzz*)(s + kOffLvlB);
+  Xyzz* tsum = (Xyzz*)(s + kOffTsum);
+
+  const int K = kNoAllocK, W = kNoAllocWindows, spaces = W;
+  const size_t nbins = kNoAllocBins;
+  const size_t E = (size_t)W * n;
+  const size_t nseg = (E + kNoAllocSeg - 1) / kNoAllocSeg;
+  const size_t scan_blocks = (nbins + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems);
+
+  // What a call must find at zero: the error flag, the histogram, the buckets.
+  APG_NA(cudaMemsetAsync(flags, 0, 4, st));
+  APG_NA(cudaMemsetAsync(counts, 0, (nbins + 1) * sizeof(uint32_t), st));
+  APG_NA(cudaMemsetAsync(buckets, 0, nbins * sizeof(Xyzz), st));
+  k_points_in<<<blocks_for<int>(n, 256), 256, 0, st>>>((const uint4*)d_bases, n, bases, flags);
+  APG_NA_LAUNCH();
+  k_recode<false><<<blocks_for<int>(n, 256), 256, 0, st>>>(d_scalars, n, kNoAllocC, W, 0, 0, 0, entries, counts,
+                                                            flags);
+  APG_NA_LAUNCH();
+  k_scan_local<<<(unsigned)scan_blocks, kScanBlock, 0, st>>>(counts, nbins, blk);
+  k_scan_blocks<<<1, kScanBlock, 0, st>>>(blk, (int)scan_blocks);
+  k_scan_add<<<blocks_for<int>(nbins, 256), 256, 0, st>>>(counts, nbins, (const uint32_t*)blk, total);
+  k_scatter<<<blocks_for<int>(E, 256), 256, 0, st>>>((const uint64_t*)entries, E, counts, sorted);
+  APG_NA_LAUNCH();
+  k_accumulate<<<blocks_for<int>(nseg, 128), 128, 0, st>>>((const uint64_t*)sorted, (const uint32_t*)total,
+                                                            kNoAllocSeg, nseg, (const Affine*)bases, buckets,
+                                                            ikeys[0], ipts[0], ipres[0]);
+  APG_NA_LAUNCH();
+  {
+    constexpr int kFold = 8;
+    size_t len = 2 * nseg;
+    int cur = 0;
+    for (size_t fseg = nseg; fseg > 1;) {
+      fseg = (len + kFold - 1) / kFold;
+      k_fold_edges<<<blocks_for<int>(fseg, 128), 128, 0, st>>>((const uint32_t*)ikeys[cur], (const Xyzz*)ipts[cur],
+                                                               (const uint8_t*)ipres[cur], len, kFold, fseg, buckets,
+                                                               ikeys[cur ^ 1], ipts[cur ^ 1], ipres[cur ^ 1]);
+      APG_NA_LAUNCH();
+      cur ^= 1;
+      len = 2 * fseg;
+    }
+  }
+  const Xyzz* lvl_in = buckets;
+  int M = K;
+  for (int l = 0; l < kNoAllocLevels; ++l) {
+    int G = (M + kLevelFan - 1) / kLevelFan;
+    Xyzz* outR = (l & 1) ? lvlB : lvlA;
+    k_level<<<blocks_for<int>((size_t)spaces * G, 64), 64, 0, st>>>(lvl_in, M, spaces, kLevelFan, outT, outR);
+    k_sum<<<spaces, 128, 0, st>>>((const Xyzz*)outT, G, tsum + (size_t)l * spaces);
+    APG_NA_LAUNCH();
+    lvl_in = outR;
+    M = G;
+  }
+  int fan_log = 0;
+  while ((1 << fan_log) < kLevelFan) ++fan_log;
+  k_finish<<<1, 32, 0, st>>>((const Xyzz*)tsum, kNoAllocLevels, spaces, fan_log, kNoAllocC, (uint32_t*)d_out);
+  APG_NA_LAUNCH();
+  uint32_t f = 0;
+  APG_NA(cudaMemcpyAsync(&f, flags, 4, cudaMemcpyDeviceToHost, st));
+  APG_NA(cudaStreamSynchronize(st));
+  if (f & DEV_NONCANONICAL) return APG_ERR_NONCANONICAL;
+  if (f & DEV_OFF_CURVE) return APG_ERR_INVALID_POINT;
+  if (f) return APG_ERR_INTERNAL;
+  return APG_OK;
+}
+
+static_assert(kNoAllocLevels == 3 && kNoAllocK / kLevelFan / kLevelFan <= kLevelFan,
+              "the reduction plan above assumes 256 buckets folded 8 at a time");
+
+}  // namespace
+
 }  // namespace apg
+
+extern "C" int apg_msm_noalloc(const void* d_bases, const void* d_scalars, size_t n, void* d_out, void* stream) {
+  return apg::msm_noalloc(d_bases, d_scalars, n, d_out, (cudaStream_t)stream);
+}

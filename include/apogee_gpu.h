@@ -53,6 +53,7 @@ enum apg_status {
   APG_ERR_BAD_CIRCUIT = 22,           /* malformed circuit blob */
   APG_ERR_NO_SRS = 23,                /* no SRS resident on the context */
   APG_ERR_INTERNAL = 24,              /* a device invariant failed */
+  APG_ERR_NOALLOC_TOO_LARGE = 25,     /* apg_msm_noalloc: more bases than its fixed scratch holds */
   APG_ERR_CUDA = 100,                 /* a CUDA call failed */
   APG_ERR_OUT_OF_MEMORY = 101,        /* device allocation refused */
   APG_ERR_NO_DEVICE = 103             /* no usable CUDA device */
@@ -101,6 +102,26 @@ int apg_msm(apg_ctx* ctx, const uint8_t* bases, size_t n_bases, const uint8_t* s
 /* msm::msm_small_u32 (msm.rs:79): the same over u32 scalars. */
 int apg_msm_small_u32(apg_ctx* ctx, const uint8_t* bases, size_t n_bases, const uint32_t* scalars,
                       size_t n_scalars, uint8_t out[64]);
+
+/* No counterpart in the reference: an MSM that allocates no device memory,
+ * for callers that cannot let a library allocate on their behalf -- a
+ * serving loop whose HBM is already promised to admitted requests, or a
+ * latency-critical pipeline that cannot take the device-wide synchronisation
+ * of cudaMalloc/cudaFree. It computes exactly what apg_msm does, with every
+ * buffer carved from one fixed array in the library's device global memory
+ * (about 8.5 MB, reserved on every GPU that loads the library, until exit).
+ *   d_bases:   n canonical 64-byte points in device memory (all-zero =
+ *              infinity), d_scalars: n Fr in memory in device memory,
+ *   d_out:     64 bytes of device memory for the canonical result,
+ *   stream:    the cudaStream_t to run on (0 = legacy default stream), on the
+ *              current device. The call returns when the result is written.
+ * At most APG_MSM_NOALLOC_MAX_POINTS bases (APG_ERR_NOALLOC_TOO_LARGE above).
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture. All calls on a device share the one
+ * array (each clears what must start at zero), so calls that overlap on the
+ * GPU race: serialise them, e.g. on one stream. */
+#define APG_MSM_NOALLOC_MAX_POINTS 4096
+int apg_msm_noalloc(const void* d_bases, const void* d_scalars, size_t n, void* d_out, void* stream);
 
 /* ---- commit (crates/pcs/src/lib.rs:237-298) ---------------------------- */
 
