@@ -272,6 +272,37 @@ class Context:
         f.restype = ctypes.c_uint64
         return f(self._h)
 
+    # ---- Mercury --------------------------------------------------------------
+    def open(self, evals: bytes, num_vars: int, cm: bytes, u, transcript: bytes):
+        """pcs::open. evals: Fr in-memory bytes; u: canonical ints. Returns
+        (v canonical int, 704-byte proof, transcript)."""
+        snap = ctypes.create_string_buffer(bytes(transcript), TRANSCRIPT_BYTES)
+        v = ctypes.create_string_buffer(32)
+        proof = ctypes.create_string_buffer(PROOF_BYTES)
+        self._check(lib().apg_mercury_open(self._h, evals, ctypes.c_size_t(num_vars), cm, to_mont_bytes(u), snap, v,
+                                           proof))
+        return from_mont_bytes(v.raw)[0], proof.raw, snap.raw
+
+    def batch_open(self, cols, num_vars: int, cms, u, transcript: bytes, on_device: bool = False):
+        """pcs::batch_open. cols: Fr in-memory bytes per column (or device
+        pointers with on_device); cms: 64-byte commitments. Returns (values,
+        704-byte proof, transcript)."""
+        k = len(cols)
+        snap = ctypes.create_string_buffer(bytes(transcript), TRANSCRIPT_BYTES)
+        vs = ctypes.create_string_buffer(32 * max(k, 1))
+        proof = ctypes.create_string_buffer(PROOF_BYTES)
+        cmb = b"".join(cms)
+        if on_device:
+            ptrs = (ctypes.c_void_p * max(k, 1))(*cols)
+            st = lib().apg_mercury_batch_open_device(self._h, ptrs, ctypes.c_size_t(k), ctypes.c_size_t(num_vars), cmb,
+                                                     to_mont_bytes(u), snap, vs, proof)
+        else:
+            ptrs = (ctypes.c_char_p * max(k, 1))(*cols)
+            st = lib().apg_mercury_batch_open(self._h, ptrs, ctypes.c_size_t(k), ctypes.c_size_t(num_vars), cmb,
+                                              to_mont_bytes(u), snap, vs, proof)
+        self._check(st)
+        return from_mont_bytes(vs.raw[:32 * k]), proof.raw, snap.raw
+
     # ---- zerocheck -----------------------------------------------------------
     def prove_zerocheck(self, terms, polys, num_vars: int, transcript: bytes, on_device: bool = False):
         """sumcheck::prove_zerocheck. terms: (coef, a, b-or-None) with coef a

@@ -284,6 +284,93 @@ int apg_witness_digest(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_
   return guarded(ctx, [&](Ctx& c) { return witness_digest_impl(c, cols, k, num_vars, out); });
 }
 
+static bool read_points_u(const uint8_t* u, size_t nv, std::vector<host::F>& out) {
+  out.resize(nv);
+  for (size_t i = 0; i < nv; ++i) {
+    memcpy(out[i].w, u + 32 * i, 32);
+    if (!host::below_p(out[i].w)) return false;
+  }
+  return true;
+}
+
+int apg_mercury_open(apg_ctx* ctx, const uint8_t* evals, size_t num_vars, const uint8_t cm[64], const uint8_t* u,
+                     uint8_t* transcript, uint8_t v_out[32], uint8_t proof_out[704]) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (!evals || !cm || (!u && num_vars) || !transcript || !v_out || !proof_out) return (int)APG_ERR_INVALID_ARGUMENT;
+    if (num_vars < 2 || num_vars > 54 || num_vars % 2) return (int)APG_ERR_UNSUPPORTED_NUM_VARS;
+    if (num_vars > 40) return (int)APG_ERR_OUT_OF_MEMORY;
+    std::vector<host::F> uu;
+    if (!read_points_u(u, num_vars, uu)) return (int)APG_ERR_NONCANONICAL;
+    host::Transcript tr;
+    if (!tr.load(transcript)) return (int)APG_ERR_INVALID_ARGUMENT;
+    const size_t n = (size_t)1 << num_vars;
+    if (c.srs && c.srs_n < n) return (int)APG_ERR_SRS_TOO_SMALL;
+    Fr* d = c.scratch[S_SCALARS].as<Fr>(n);
+    APG_CUDA(cudaMemcpyAsync(d, evals, 32 * n, cudaMemcpyHostToDevice, c.stream));
+    host::F v;
+    int st = mercury_open_impl(c, d, num_vars, cm, uu, tr, v, proof_out);
+    if (st) return st;
+    memcpy(v_out, v.w, 32);
+    tr.save(transcript);
+    return (int)APG_OK;
+  });
+}
+
+static int batch_open_common(Ctx& c, const void* const* cols, bool on_device, size_t k, size_t num_vars,
+                             const uint8_t* cms, const uint8_t* u, uint8_t* transcript, uint8_t* vs_out,
+                             uint8_t* proof_out) {
+  if (k == 0) return APG_ERR_EMPTY_BATCH;
+  if (!cols || !cms || (!u && num_vars) || !transcript || !vs_out || !proof_out) return APG_ERR_INVALID_ARGUMENT;
+  if (num_vars < 2 || num_vars > 54 || num_vars % 2) return APG_ERR_UNSUPPORTED_NUM_VARS;
+  if (num_vars > 40) return APG_ERR_OUT_OF_MEMORY;
+  std::vector<host::F> uu;
+  if (!read_points_u(u, num_vars, uu)) return APG_ERR_NONCANONICAL;
+  host::Transcript tr;
+  if (!tr.load(transcript)) return APG_ERR_INVALID_ARGUMENT;
+  const size_t n = (size_t)1 << num_vars;
+  if (c.srs && c.srs_n < n) return APG_ERR_SRS_TOO_SMALL;
+  std::vector<const Fr*> ptrs(k);
+  Fr* staged = nullptr;
+  if (on_device) {
+    for (size_t j = 0; j < k; ++j) ptrs[j] = (const Fr*)cols[j];
+  } else {
+    APG_CUDA(cudaMallocAsync((void**)&staged, 32 * n * k, c.stream));
+    for (size_t j = 0; j < k; ++j) {
+      APG_CUDA(cudaMemcpyAsync(staged + j * n, cols[j], 32 * n, cudaMemcpyHostToDevice, c.stream));
+      ptrs[j] = staged + j * n;
+    }
+  }
+  std::vector<host::F> vs;
+  int st;
+  try {
+    st = mercury_batch_open_impl(c, ptrs.data(), k, num_vars, cms, uu, tr, vs, proof_out);
+  } catch (...) {
+    if (staged) cudaFreeAsync(staged, c.stream);
+    throw;
+  }
+  if (staged) APG_CUDA(cudaFreeAsync(staged, c.stream));
+  if (st) return st;
+  memcpy(vs_out, vs.data(), 32 * k);
+  tr.save(transcript);
+  return APG_OK;
+}
+
+int apg_mercury_batch_open(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_t num_vars, const uint8_t* cms,
+                           const uint8_t* u, uint8_t* transcript, uint8_t* vs_out, uint8_t proof_out[704]) {
+  return guarded(ctx, [&](Ctx& c) {
+    return batch_open_common(c, (const void* const*)cols, false, k, num_vars, cms, u, transcript, vs_out,
+                             proof_out);
+  });
+}
+
+int apg_mercury_batch_open_device(apg_ctx* ctx, const void* const* d_cols, size_t k, size_t num_vars,
+                                  const uint8_t* cms, const uint8_t* u, uint8_t* transcript, uint8_t* vs_out,
+                                  uint8_t proof_out[704]) {
+  return guarded(ctx, [&](Ctx& c) {
+    return batch_open_common(c, d_cols, true, k, num_vars, cms, u, transcript, vs_out, proof_out);
+  });
+}
+
 struct apg_gkr_values {
   GkrValues* v;
   apg_ctx* ctx;

@@ -1,0 +1,551 @@
+// Mercury opening (crates/pcs/src/lib.rs:313-492) and the batched opening
+// (:688-789) with the O(n) passes and every MSM on the device.
+//
+// Device: the restriction h (one warp per row of the b x b evaluation
+// matrix), the column-parallel fold into q and g, the numerator and its
+// division by (X - z) -- both linear recurrences, run as multi-level suffix
+// Horner scans -- the size-2b transforms behind S, the batch combination and
+// all eight MSMs over the resident SRS. Host: the transcript and the O(1)
+// and O(b) scalar glue of the BDFG20 step (crates/pcs-verify/src/bdfg.rs),
+// exactly the reference's formulas.
+#include "sumcheck.cuh"
+
+namespace apg {
+
+using host::F;
+
+namespace {
+
+Fr dv(const F& a) {
+  Fr r;
+  memcpy(r.v, a.w, 32);
+  return r;
+}
+
+// h_j = sum_i eq1[i] * f[j*b + i]: one warp per row.
+__global__ void k_row_dot(const Fr* f, const Fr* eq1, size_t b, size_t rows, Fr* h) {
+  const size_t warp = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  if (warp >= rows) return;
+  Fr acc = fe_zero<FrConsts>();
+  for (size_t i = lane; i < b; i += 32) acc = fe_add(acc, fe_mul(ld_fe(&eq1[i]), ld_fe(&f[warp * b + i])));
+  for (int off = 16; off > 0; off >>= 1) {
+    Fr o;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) o.v[w] = __shfl_down_sync(0xffffffffu, acc.v[w], off);
+    acc = fe_add(acc, o);
+  }
+  if (lane == 0) st_fe(&h[warp], acc);
+}
+
+// out[0] = sum_i a[i] * b[i] (one block).
+__global__ void k_dot(const Fr* a, const Fr* b, size_t n, Fr* out) {
+  __shared__ Fr red[256];
+  Fr acc = fe_zero<FrConsts>();
+  for (size_t i = threadIdx.x; i < n; i += blockDim.x) acc = fe_add(acc, fe_mul(ld_fe(&a[i]), ld_fe(&b[i])));
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < (unsigned)off) red[threadIdx.x] = fe_add(red[threadIdx.x], red[threadIdx.x + off]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) st_fe(out, red[0]);
+}
+
+// Suffix Horner over `count` positions of `cols` interleaved columns
+// (element j of column c at j*stride + c): acc_j = sum_{k>=j} x_k r^(k-j).
+// Pass 1: every segment of L positions folds locally from its top and keeps
+// its bottom value as the segment's aggregate.
+__global__ void k_suffix_local(const Fr* in, Fr* out, size_t stride, size_t count, size_t cols, int L, Fr r,
+                               Fr* agg) {
+  const size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t nseg = (count + L - 1) / L;
+  if (id >= nseg * cols) return;
+  const size_t seg = id / cols, col = id % cols;
+  const size_t lo = seg * L, hi = min(lo + (size_t)L, count);
+  Fr acc = fe_zero<FrConsts>();
+  for (size_t j = hi; j-- > lo;) {
+    acc = fe_add(ld_fe(&in[j * stride + col]), fe_mul(r, acc));
+    st_fe(&out[j * stride + col], acc);
+  }
+  st_fe(&agg[seg * cols + col], acc);
+}
+
+// Pass 2: with upper[s] = acc at the bottom of segment s (the next level's
+// result), acc_j = local_j + r^(lo_{s+1} - j) * upper[s+1].
+__global__ void k_suffix_fix(Fr* out, size_t stride, size_t count, size_t cols, int L, const Fr* upper,
+                             const Fr* pows) {
+  const size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (id >= count * cols) return;
+  const size_t j = id / cols, col = id % cols;
+  const size_t seg = j / L;
+  const size_t nseg = (count + L - 1) / L;
+  if (seg + 1 >= nseg) return;
+  const size_t next = (seg + 1) * L;
+  Fr carry = ld_fe(&upper[(seg + 1) * cols + col]);
+  Fr* p = &out[j * stride + col];
+  st_fe(p, fe_add(ld_fe(p), fe_mul(ld_fe(&pows[next - j]), carry)));
+}
+
+// out[i] = base^i.
+__global__ void k_powers(Fr base, size_t count, Fr* out) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  Fr acc = fe_one<FrConsts>(), b = base;
+  for (size_t e = i; e; e >>= 1) {
+    if (e & 1) acc = fe_mul(acc, b);
+    b = fe_sqr(b);
+  }
+  st_fe(&out[i], acc);
+}
+
+__global__ void k_bitrev(Fr* a, size_t m, int bits) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  size_t j = __brevll((unsigned long long)i) >> (64 - bits);
+  if (i < j) {
+    Fr x = ld_fe(&a[i]), y = ld_fe(&a[j]);
+    st_fe(&a[i], y);
+    st_fe(&a[j], x);
+  }
+}
+
+// One radix-2 decimation-in-time stage at half-width `half` (the reference's
+// butterflies, crates/pcs/src/fft.rs:100-134): tw holds w^k for k < m/2.
+__global__ void k_fft_stage(Fr* a, size_t m, size_t half, const Fr* tw) {
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= m / 2) return;
+  size_t start = (t / half) * 2 * half, k = t % half;
+  Fr w = ld_fe(&tw[k * (m / (2 * half))]);
+  Fr lo = ld_fe(&a[start + k]), hi = fe_mul(ld_fe(&a[start + k + half]), w);
+  st_fe(&a[start + k], fe_add(lo, hi));
+  st_fe(&a[start + k + half], fe_sub(lo, hi));
+}
+
+// The four padded operands of S: g, rev(eq1), h, rev(eq2), each b long in 2b.
+__global__ void k_sym_pad(const Fr* g, const Fr* eq1, const Fr* h, const Fr* eq2, size_t b, Fr* G, Fr* P1, Fr* H,
+                          Fr* P2) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= 2 * b) return;
+  const Fr z = fe_zero<FrConsts>();
+  st_fe(&G[i], i < b ? ld_fe(&g[i]) : z);
+  st_fe(&P1[i], i < b ? ld_fe(&eq1[b - 1 - i]) : z);
+  st_fe(&H[i], i < b ? ld_fe(&h[i]) : z);
+  st_fe(&P2[i], i < b ? ld_fe(&eq2[b - 1 - i]) : z);
+}
+
+__global__ void k_sym_mix(const Fr* G, const Fr* P1, const Fr* H, const Fr* P2, size_t m, Fr gamma, Fr* R) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  Fr a = fe_mul(ld_fe(&G[i]), ld_fe(&P1[i]));
+  Fr c = fe_mul(gamma, fe_mul(ld_fe(&H[i]), ld_fe(&P2[i])));
+  st_fe(&R[i], fe_add(a, c));
+}
+
+__global__ void k_scale(Fr* a, size_t m, Fr s) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < m) st_fe(&a[i], fe_mul(ld_fe(&a[i]), s));
+}
+
+// S[k - b] = R[k] + R[2b - 2 - k] for k in [b, 2b - 1); checks R[2b-1] = 0 and
+// R[b-1] = h(alpha) + gamma v (symmetric_witness's two assertions).
+__global__ void k_sym_out(const Fr* R, size_t b, Fr expect_mid, Fr* S, uint32_t* flags) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i == 0) {
+    if (!fe_is_zero(ld_fe(&R[2 * b - 1])) || !fe_eq(ld_fe(&R[b - 1]), expect_mid))
+      atomicOr(flags, (uint32_t)DEV_NONZERO_REM);
+  }
+  if (i >= b - 1) return;
+  size_t k = b + i;
+  st_fe(&S[i], fe_add(ld_fe(&R[k]), ld_fe(&R[2 * b - 2 - k])));
+}
+
+__global__ void k_reverse(const Fr* src, size_t b, Fr* dst) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < b) st_fe(&dst[i], ld_fe(&src[b - 1 - i]));
+}
+
+// numerator = f - (z^b - alpha) q - g(z), with q the n - b coefficients.
+__global__ void k_numerator(const Fr* f, const Fr* q, size_t n, size_t nq, Fr c, Fr gz, Fr* out) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Fr v = ld_fe(&f[i]);
+  if (i < nq) v = fe_sub(v, fe_mul(c, ld_fe(&q[i])));
+  if (i == 0) v = fe_sub(v, gz);
+  st_fe(&out[i], v);
+}
+
+// f* = sum_c w_c col_c.
+__global__ void k_combine(const Fr* const* cols, const Fr* w, int k, size_t n, Fr* out) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Fr acc = fe_zero<FrConsts>();
+  for (int c = 0; c < k; ++c) acc = fe_add(acc, fe_mul(ld_fe(&w[c]), ld_fe(&cols[c][i])));
+  st_fe(&out[i], acc);
+}
+
+__global__ void k_expect_zero(const Fr* x, uint32_t* flags) {
+  if (!fe_is_zero(ld_fe(x))) atomicOr(flags, (uint32_t)DEV_NONZERO_REM);
+}
+
+inline unsigned nb(size_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// ---- host helpers -------------------------------------------------------------
+
+F read_fr(Ctx& c, const Fr* d) {
+  F x;
+  APG_CUDA(cudaMemcpyAsync(x.w, d, 32, cudaMemcpyDeviceToHost, c.stream));
+  APG_CUDA(cudaStreamSynchronize(c.stream));
+  return x;
+}
+
+std::vector<F> read_frs(Ctx& c, const Fr* d, size_t n) {
+  std::vector<F> v(n);
+  if (n) APG_CUDA(cudaMemcpyAsync(v.data(), d, 32 * n, cudaMemcpyDeviceToHost, c.stream));
+  APG_CUDA(cudaStreamSynchronize(c.stream));
+  return v;
+}
+
+// MSM of the first `len` SRS powers against device scalars, canonical bytes.
+void srs_commit(Ctx& c, const Fr* d, size_t len, uint8_t out[64]) {
+  if (len == 0) {
+    memset(out, 0, 64);
+    return;
+  }
+  const SrsTable* t = nullptr;
+  if (len <= ((size_t)1 << 14)) t = srs_table(c, 8, len);
+  if (!t) t = srs_table(c, 16, len);
+  if (!t) throw Error(APG_ERR_SRS_TOO_SMALL, "the SRS holds fewer powers than the polynomial has coefficients");
+  msm_device(c, nullptr, t, d, false, false, len, nullptr, out);
+}
+
+// acc_j = sum_{k >= j} x_k r^(k - j) for every position, in place or not.
+void suffix_horner(Ctx& c, const Fr* in, Fr* out, size_t stride, size_t count, size_t cols, const F& r,
+                   int depth = 0) {
+  if (count == 0) return;
+  const int L = 32;
+  const size_t nseg = (count + L - 1) / L;
+  // Scratch per level: aggregates (nseg x cols) and the power table r^0..r^L,
+  // stream-ordered so every recursion level owns its own.
+  Fr* agg;
+  APG_CUDA(cudaMallocAsync((void**)&agg, 32 * nseg * cols + 32 * (L + 1), c.stream));
+  Fr* pows = agg + nseg * cols;
+  launch(c, k_powers, 1, L + 1, 0, dv(r), (size_t)(L + 1), pows);
+  launch(c, k_suffix_local, nb(nseg * cols, 128), 128, 0, in, out, stride, count, cols, L, dv(r), agg);
+  if (nseg > 1) {
+    F rL = host::fpow_u64(r, L);
+    suffix_horner(c, agg, agg, cols, nseg, cols, rL, depth + 1);
+    launch(c, k_suffix_fix, nb(count * cols, 256), 256, 0, out, stride, count, cols, L, (const Fr*)agg,
+           (const Fr*)pows);
+  }
+  APG_CUDA(cudaFreeAsync(agg, c.stream));
+}
+
+F two_adic_root() {
+  // 5^((p - 1) / 2^28), derived rather than transcribed.
+  uint64_t e[4] = {host::kP[0] - 1, host::kP[1], host::kP[2], host::kP[3]};
+  for (int s = 0; s < 28; ++s) {
+    for (int i = 0; i < 3; ++i) e[i] = (e[i] >> 1) | (e[i + 1] << 63);
+    e[3] >>= 1;
+  }
+  return host::fpow(host::from_u64(5), e);
+}
+
+void fft_inplace(Ctx& c, Fr* a, size_t m, const Fr* tw) {
+  int bits = 0;
+  while (((size_t)1 << bits) < m) ++bits;
+  launch(c, k_bitrev, nb(m, 256), 256, 0, a, m, bits);
+  for (size_t half = 1; half < m; half *= 2) launch(c, k_fft_stage, nb(m / 2, 256), 256, 0, a, m, half, tw);
+}
+
+// ---- univariate helpers on the host (O(b), crates/pcs-verify/src/uni.rs) -------
+
+typedef std::vector<F> Poly;
+
+F ueval(const Poly& p, const F& x) {
+  F acc = host::fzero();
+  for (size_t i = p.size(); i-- > 0;) acc = host::fadd(host::fmul(acc, x), p[i]);
+  return acc;
+}
+
+Poly umul(const Poly& a, const Poly& b) {
+  if (a.empty() || b.empty()) return {};
+  Poly out(a.size() + b.size() - 1, host::fzero());
+  for (size_t i = 0; i < a.size(); ++i)
+    for (size_t j = 0; j < b.size(); ++j) out[i + j] = host::fadd(out[i + j], host::fmul(a[i], b[j]));
+  return out;
+}
+
+void uadd_scaled(Poly& acc, const Poly& src, const F& k) {
+  if (src.size() > acc.size()) acc.resize(src.size(), host::fzero());
+  for (size_t i = 0; i < src.size(); ++i) acc[i] = host::fadd(acc[i], host::fmul(k, src[i]));
+}
+
+Poly uvanishing(const std::vector<F>& roots) {
+  Poly out{host::fone()};
+  for (auto& r : roots) out = umul(out, {host::fneg(r), host::fone()});
+  return out;
+}
+
+Poly uinterpolate(const std::vector<std::pair<F, F>>& pts) {
+  Poly out(pts.size(), host::fzero());
+  for (size_t i = 0; i < pts.size(); ++i) {
+    Poly num{host::fone()};
+    F den = host::fone();
+    for (size_t j = 0; j < pts.size(); ++j) {
+      if (i == j) continue;
+      num = umul(num, {host::fneg(pts[j].first), host::fone()});
+      den = host::fmul(den, host::fsub(pts[i].first, pts[j].first));
+    }
+    uadd_scaled(out, num, host::fmul(pts[i].second, host::finv(den)));
+  }
+  return out;
+}
+
+std::pair<Poly, F> udiv_linear(const Poly& p, const F& r) {
+  if (p.empty()) return {{}, host::fzero()};
+  Poly q(p.size() - 1);
+  F acc = p.back();
+  for (size_t i = p.size() - 1; i-- > 0;) {
+    q[i] = acc;
+    acc = host::fadd(p[i], host::fmul(acc, r));
+  }
+  return {q, acc};
+}
+
+F tensor_eval(const std::vector<F>& u, F x) {
+  F acc = host::fone();
+  for (auto& uk : u) {
+    acc = host::fmul(acc, host::fadd(host::fmul(uk, x), host::fsub(host::fone(), uk)));
+    x = host::fsqr(x);
+  }
+  return acc;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+
+int mercury_open_impl(Ctx& c, const Fr* d_f, size_t nv, const uint8_t cm[64], const std::vector<F>& u,
+                      host::Transcript& tr, F& v_out, uint8_t proof_out[704]) {
+  using namespace host;
+  if (nv < 2 || nv > 54 || nv % 2) return APG_ERR_UNSUPPORTED_NUM_VARS;
+  if (u.size() != nv) return APG_ERR_POINT_LENGTH_MISMATCH;
+  if (!c.srs) return APG_ERR_NO_SRS;
+  const size_t n = (size_t)1 << nv;
+  if (c.srs_n < n) return APG_ERR_SRS_TOO_SMALL;
+  if (nv > 40) return APG_ERR_OUT_OF_MEMORY;
+  const size_t t = nv / 2, b = (size_t)1 << t;
+  std::vector<F> u1(u.begin(), u.begin() + t), u2(u.begin() + t, u.end());
+
+  Fr* work;
+  // eq1 | eq2 | h | g | S | D | acc(n) | num(n) | 4 x (2b) transforms | twiddles
+  const size_t words = 6 * b + 2 * n + 8 * b + b + 16;
+  APG_CUDA(cudaMallocAsync((void**)&work, 32 * words, c.stream));
+  struct Guard {
+    Ctx& c;
+    Fr* p;
+    ~Guard() { cudaFreeAsync(p, c.stream); }
+  } guard{c, work};
+  Fr *eq1 = work, *eq2 = eq1 + b, *h = eq2 + b, *g = h + b, *S = g + b, *D = S + b, *acc = D + b, *num = acc + n;
+  Fr *TG = num + n, *TP1 = TG + 2 * b, *TH = TP1 + 2 * b, *TP2 = TH + 2 * b, *tw = TP2 + 2 * b, *tmp = tw + b;
+
+  // Step 1: h, v.
+  build_eq_table(c, u1, eq1);
+  build_eq_table(c, u2, eq2);
+  launch(c, k_row_dot, nb(b * 32, 256), 256, 0, d_f, (const Fr*)eq1, b, b, h);
+  launch(c, k_dot, 1, 256, 0, (const Fr*)eq2, (const Fr*)h, b, tmp);
+  F v = read_fr(c, tmp);
+  uint8_t pts[8][64];
+  srs_commit(c, h, b, pts[0]);
+  tr.absorb(T_MERCURY_INSTANCE, std::vector<F>{from_u64(n)});
+  tr.absorb_g1(T_COMMITMENT, cm, 1);
+  std::vector<F> claim = u;
+  claim.push_back(v);
+  tr.absorb(T_EVALUATION_CLAIM, claim);
+  tr.absorb_g1(T_PCS_OPENING, pts[0], 1);
+  F alpha = tr.challenge(T_MERCURY_ALPHA);
+
+  // Step 2: the fold. acc rows: acc_j = sum_{k>=j} alpha^(k-j) row_k; q is
+  // rows 1..b-1 of acc, g is row 0.
+  cudaEvent_t tp = c.timer_begin();
+  suffix_horner(c, d_f, acc, b, b, b, alpha);
+  c.timer_end(APG_TIMER_MERCURY_PASS, tp);
+  APG_CUDA(cudaMemcpyAsync(g, acc, 32 * b, cudaMemcpyDeviceToDevice, c.stream));
+  const Fr* q = acc + b;
+  const size_t nq = n - b;
+  srs_commit(c, q, nq, pts[1]);
+  srs_commit(c, g, b, pts[2]);
+  tr.absorb_g1(T_PCS_OPENING, &pts[1][0], 2);
+  F gamma = tr.challenge(T_MERCURY_GAMMA);
+
+  // Step 3: S and D.
+  std::vector<F> hh = read_frs(c, h, b);
+  F h_alpha = ueval(hh, alpha);
+  {
+    const size_t m = 2 * b;
+    int k = 0;
+    while (((size_t)1 << k) < m) ++k;
+    F w = two_adic_root();
+    for (int i = k; i < 28; ++i) w = fsqr(w);
+    launch(c, k_sym_pad, nb(m, 256), 256, 0, (const Fr*)g, (const Fr*)eq1, (const Fr*)h, (const Fr*)eq2, b, TG, TP1,
+           TH, TP2);
+    launch(c, k_powers, nb(m / 2, 256), 256, 0, dv(w), m / 2, tw);
+    fft_inplace(c, TG, m, tw);
+    fft_inplace(c, TP1, m, tw);
+    fft_inplace(c, TH, m, tw);
+    fft_inplace(c, TP2, m, tw);
+    launch(c, k_sym_mix, nb(m, 256), 256, 0, (const Fr*)TG, (const Fr*)TP1, (const Fr*)TH, (const Fr*)TP2, m,
+           dv(gamma), TG);
+    launch(c, k_powers, nb(m / 2, 256), 256, 0, dv(finv(w)), m / 2, tw);
+    fft_inplace(c, TG, m, tw);
+    launch(c, k_scale, nb(m, 256), 256, 0, TG, m, dv(finv(from_u64(m))));
+    launch(c, k_sym_out, nb(b, 256), 256, 0, (const Fr*)TG, b, dv(fadd(h_alpha, fmul(gamma, v))), S, c.d_flags);
+    launch(c, k_reverse, nb(b, 256), 256, 0, (const Fr*)g, b, D);
+  }
+  srs_commit(c, S, b - 1, pts[3]);
+  srs_commit(c, D, b, pts[4]);
+  tr.absorb_g1(T_PCS_OPENING, &pts[3][0], 2);
+  F z;
+  do {
+    z = tr.challenge(T_MERCURY_Z);
+  } while (z.zero());
+  if (fsqr(z) == fone() || z == alpha || fmul(z, alpha) == fone()) {
+    c.last_error = "degenerate challenge set {z, 1/z, alpha}";
+    return APG_ERR_DEGENERATE_CHALLENGE;
+  }
+  F zi = finv(z);
+
+  // Step 4: the six values, the numerator and its quotient by (X - z).
+  std::vector<F> gg = read_frs(c, g, b), ss = read_frs(c, S, b - 1);
+  F ev[6] = {ueval(gg, z), ueval(gg, zi), ueval(hh, z), ueval(hh, zi), ueval(ss, z), ueval(ss, zi)};
+  tr.absorb(T_PCS_OPENING, ev, 6);
+  F zb = fpow_u64(z, b);
+  launch(c, k_numerator, nb(n, 256), 256, 0, d_f, q, n, nq, dv(fsub(zb, alpha)), dv(ev[0]), num);
+  tp = c.timer_begin();
+  suffix_horner(c, num, num, 1, n, 1, z);
+  c.timer_end(APG_TIMER_MERCURY_PASS, tp);
+  launch(c, k_expect_zero, 1, 1, 0, (const Fr*)num, c.d_flags);  // the remainder f(z) - ... = 0
+  srs_commit(c, num + 1, n - 1, pts[5]);
+  tr.absorb_g1(T_PCS_OPENING, pts[5], 1);
+
+  // Step 4(e): BDFG20 over T = {z, 1/z, alpha} (crates/pcs-verify/src/bdfg.rs).
+  F two_inv = finv(from_u64(2));
+  F inner = fadd(fadd(fmul(ev[0], tensor_eval(u1, zi)), fmul(ev[1], tensor_eval(u1, z))),
+                 fmul(gamma, fsub(fsub(fadd(fmul(ev[2], tensor_eval(u2, zi)), fmul(ev[3], tensor_eval(u2, z))), v), v)));
+  inner = fsub(fsub(inner, fmul(z, ev[4])), fmul(zi, ev[5]));
+  F ha = fmul(inner, two_inv);
+  if (ha != h_alpha) throw Error(APG_ERR_INTERNAL, "h(alpha) does not re-derive from the six values");
+  F d_z = fmul(fpow_u64(z, b - 1), ev[1]);
+  std::vector<F> tset = {z, zi, alpha};
+  Poly wa = uvanishing({alpha});
+  Poly zc[4] = {wa, Poly{fone()}, wa, uvanishing({zi, alpha})};
+  Poly rr[4] = {uinterpolate({{z, ev[0]}, {zi, ev[1]}}), uinterpolate({{z, ev[2]}, {zi, ev[3]}, {alpha, h_alpha}}),
+                uinterpolate({{z, ev[4]}, {zi, ev[5]}}), Poly{d_z}};
+  Poly dd(gg.rbegin(), gg.rend());
+  const Poly* polys[4] = {&gg, &hh, &ss, &dd};
+  F delta = tr.challenge(T_BDFG_BATCH);
+  Poly f;
+  F pw = fone();
+  for (int i = 0; i < 4; ++i) {
+    Poly sh = *polys[i];
+    uadd_scaled(sh, rr[i], fneg(fone()));
+    uadd_scaled(f, umul(zc[i], sh), pw);
+    pw = fmul(pw, delta);
+  }
+  Poly W = f;
+  for (auto& root : tset) {
+    auto d = udiv_linear(W, root);
+    if (!d.second.zero()) throw Error(APG_ERR_INTERNAL, "F is not divisible by Z_T");
+    W = d.first;
+  }
+  Fr* dW = TH;  // reuse a transform buffer (2b >= |W|)
+  APG_CUDA(cudaMemcpyAsync(dW, W.data(), 32 * W.size(), cudaMemcpyHostToDevice, c.stream));
+  srs_commit(c, dW, W.size(), pts[6]);
+  tr.absorb_g1(T_PCS_OPENING, pts[6], 1);
+  F zp = tr.challenge(T_BDFG_POINT);
+  Poly Lp;
+  F cst = fzero();
+  uadd_scaled(Lp, W, fneg(ueval(uvanishing(tset), zp)));
+  for (int i = 0; i < 4; ++i) {
+    F cc = fmul(fpow_u64(delta, i), ueval(zc[i], zp));
+    uadd_scaled(Lp, *polys[i], cc);
+    cst = fadd(cst, fmul(cc, ueval(rr[i], zp)));
+  }
+  if (Lp.empty()) Lp.push_back(fzero());
+  Lp[0] = fsub(Lp[0], cst);
+  auto wp = udiv_linear(Lp, zp);
+  if (!wp.second.zero()) throw Error(APG_ERR_INTERNAL, "the linearization does not vanish at z'");
+  Fr* dWp = TP2;
+  APG_CUDA(cudaMemcpyAsync(dWp, wp.first.data(), 32 * wp.first.size(), cudaMemcpyHostToDevice, c.stream));
+  srs_commit(c, dWp, wp.first.size(), pts[7]);
+  tr.absorb_g1(T_PCS_OPENING, pts[7], 1);
+  (void)tr.challenge(T_PAIRING_MERGE);
+  c.check_flags();
+
+  v_out = v;
+  for (int i = 0; i < 8; ++i) memcpy(proof_out + 64 * i, pts[i], 64);
+  for (int i = 0; i < 6; ++i) to_bytes(ev[i], proof_out + 512 + 32 * i);
+  return APG_OK;
+}
+
+int mercury_batch_open_impl(Ctx& c, const Fr* const* d_cols, size_t k, size_t nv, const uint8_t* cms,
+                            const std::vector<F>& u, host::Transcript& tr, std::vector<F>& vs,
+                            uint8_t proof_out[704]) {
+  using namespace host;
+  if (k == 0) return APG_ERR_EMPTY_BATCH;
+  if (nv < 2 || nv > 54 || nv % 2) return APG_ERR_UNSUPPORTED_NUM_VARS;
+  if (u.size() != nv) return APG_ERR_POINT_LENGTH_MISMATCH;
+  if (!c.srs) return APG_ERR_NO_SRS;
+  const size_t n = (size_t)1 << nv;
+  if (c.srs_n < n) return APG_ERR_SRS_TOO_SMALL;
+  const size_t t = nv / 2, b = (size_t)1 << t;
+  std::vector<F> u1(u.begin(), u.begin() + t), u2(u.begin() + t, u.end());
+  Fr* work;
+  const size_t words = 3 * b + k + n + 2;
+  APG_CUDA(cudaMallocAsync((void**)&work, 32 * words, c.stream));
+  struct Guard {
+    Ctx& c;
+    Fr* p;
+    ~Guard() { cudaFreeAsync(p, c.stream); }
+  } guard{c, work};
+  Fr *eq1 = work, *eq2 = eq1 + b, *h = eq2 + b, *w = h + b, *fstar = w + k, *tmp = fstar + n;
+  // Each column's value at u, through the same restriction h: f(u) = <eq2, h>.
+  build_eq_table(c, u1, eq1);
+  build_eq_table(c, u2, eq2);
+  vs.assign(k, fzero());
+  for (size_t col = 0; col < k; ++col) {
+    launch(c, k_row_dot, nb(b * 32, 256), 256, 0, d_cols[col], (const Fr*)eq1, b, b, h);
+    launch(c, k_dot, 1, 256, 0, (const Fr*)eq2, (const Fr*)h, b, tmp);
+    vs[col] = read_fr(c, tmp);
+  }
+  tr.absorb_g1(T_COMMITMENT, cms, k);
+  std::vector<F> claim = u;
+  claim.insert(claim.end(), vs.begin(), vs.end());
+  tr.absorb(T_EVALUATION_CLAIM, claim);
+  F rho = tr.challenge(T_MERCURY_BATCH);
+  std::vector<F> wts(k);
+  F acc = fone();
+  for (size_t i = 0; i < k; ++i) {
+    wts[i] = acc;
+    acc = fmul(acc, rho);
+  }
+  // cm* = sum rho^i cm_i through the general MSM.
+  Affine* d_cms = c.scratch[S_BASES].as<Affine>(k);
+  upload_points(c, cms, k, d_cms);
+  APG_CUDA(cudaMemcpyAsync(w, wts.data(), 32 * k, cudaMemcpyHostToDevice, c.stream));
+  uint8_t cm_star[64];
+  msm_device(c, d_cms, nullptr, w, false, false, k, nullptr, cm_star);
+  const Fr** d_ptrs = c.scratch[S_TMP5].as<const Fr*>(k);
+  APG_CUDA(cudaMemcpyAsync(d_ptrs, d_cols, sizeof(Fr*) * k, cudaMemcpyHostToDevice, c.stream));
+  launch(c, k_combine, nb(n, 256), 256, 0, (const Fr* const*)d_ptrs, (const Fr*)w, (int)k, n, fstar);
+  F v;
+  int st = mercury_open_impl(c, fstar, nv, cm_star, u, tr, v, proof_out);
+  if (st) return st;
+  F vstar = fzero();
+  for (size_t i = 0; i < k; ++i) vstar = fadd(vstar, fmul(wts[i], vs[i]));
+  if (v != vstar) throw Error(APG_ERR_INTERNAL, "the combined value is not the combination of the values");
+  return APG_OK;
+}
+
+}  // namespace apg

@@ -51,4 +51,10 @@ int gkr_values_read_impl(GkrValues* v, size_t layer, size_t col, uint8_t* out);
 size_t gkr_values_len(GkrValues* v, size_t layer);
 size_t gkr_proof_len_impl(const uint8_t* blob, size_t len);
 
+int mercury_open_impl(Ctx& c, const Fr* d_f, size_t nv, const uint8_t cm[64], const std::vector<host::F>& u,
+                      host::Transcript& tr, host::F& v_out, uint8_t proof_out[704]);
+int mercury_batch_open_impl(Ctx& c, const Fr* const* d_cols, size_t k, size_t nv, const uint8_t* cms,
+                            const std::vector<host::F>& u, host::Transcript& tr, std::vector<host::F>& vs,
+                            uint8_t proof_out[704]);
+
 }  // namespace apg
