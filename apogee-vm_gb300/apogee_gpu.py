@@ -279,8 +279,8 @@ class Context:
         snap = ctypes.create_string_buffer(bytes(transcript), TRANSCRIPT_BYTES)
         v = ctypes.create_string_buffer(32)
         proof = ctypes.create_string_buffer(PROOF_BYTES)
-        self._check(lib().apg_mercury_open(self._h, evals, ctypes.c_size_t(num_vars), cm, to_mont_bytes(u), snap, v,
-                                           proof))
+        self._check(lib().apg_mercury_open(self._h, evals, ctypes.c_size_t(num_vars), cm, to_mont_bytes(u),
+                                           ctypes.c_size_t(len(u)), snap, v, proof))
         return from_mont_bytes(v.raw)[0], proof.raw, snap.raw
 
     def batch_open(self, cols, num_vars: int, cms, u, transcript: bytes, on_device: bool = False):
@@ -295,11 +295,11 @@ class Context:
         if on_device:
             ptrs = (ctypes.c_void_p * max(k, 1))(*cols)
             st = lib().apg_mercury_batch_open_device(self._h, ptrs, ctypes.c_size_t(k), ctypes.c_size_t(num_vars), cmb,
-                                                     to_mont_bytes(u), snap, vs, proof)
+                                                     to_mont_bytes(u), ctypes.c_size_t(len(u)), snap, vs, proof)
         else:
             ptrs = (ctypes.c_char_p * max(k, 1))(*cols)
             st = lib().apg_mercury_batch_open(self._h, ptrs, ctypes.c_size_t(k), ctypes.c_size_t(num_vars), cmb,
-                                              to_mont_bytes(u), snap, vs, proof)
+                                              to_mont_bytes(u), ctypes.c_size_t(len(u)), snap, vs, proof)
         self._check(st)
         return from_mont_bytes(vs.raw[:32 * k]), proof.raw, snap.raw
 

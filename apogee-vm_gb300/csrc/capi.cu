@@ -294,10 +294,11 @@ static bool read_points_u(const uint8_t* u, size_t nv, std::vector<host::F>& out
 }
 
 int apg_mercury_open(apg_ctx* ctx, const uint8_t* evals, size_t num_vars, const uint8_t cm[64], const uint8_t* u,
-                     uint8_t* transcript, uint8_t v_out[32], uint8_t proof_out[704]) {
+                     size_t u_len, uint8_t* transcript, uint8_t v_out[32], uint8_t proof_out[704]) {
   return guarded(ctx, [&](Ctx& c) {
-    if (!evals || !cm || (!u && num_vars) || !transcript || !v_out || !proof_out) return (int)APG_ERR_INVALID_ARGUMENT;
+    if (!evals || !cm || (!u && u_len) || !transcript || !v_out || !proof_out) return (int)APG_ERR_INVALID_ARGUMENT;
     if (num_vars < 2 || num_vars > 54 || num_vars % 2) return (int)APG_ERR_UNSUPPORTED_NUM_VARS;
+    if (u_len != num_vars) return (int)APG_ERR_POINT_LENGTH_MISMATCH;
     if (num_vars > 40) return (int)APG_ERR_OUT_OF_MEMORY;
     std::vector<host::F> uu;
     if (!read_points_u(u, num_vars, uu)) return (int)APG_ERR_NONCANONICAL;
@@ -317,11 +318,12 @@ int apg_mercury_open(apg_ctx* ctx, const uint8_t* evals, size_t num_vars, const 
 }
 
 static int batch_open_common(Ctx& c, const void* const* cols, bool on_device, size_t k, size_t num_vars,
-                             const uint8_t* cms, const uint8_t* u, uint8_t* transcript, uint8_t* vs_out,
-                             uint8_t* proof_out) {
+                             const uint8_t* cms, const uint8_t* u, size_t u_len, uint8_t* transcript,
+                             uint8_t* vs_out, uint8_t* proof_out) {
   if (k == 0) return APG_ERR_EMPTY_BATCH;
-  if (!cols || !cms || (!u && num_vars) || !transcript || !vs_out || !proof_out) return APG_ERR_INVALID_ARGUMENT;
+  if (!cols || !cms || (!u && u_len) || !transcript || !vs_out || !proof_out) return APG_ERR_INVALID_ARGUMENT;
   if (num_vars < 2 || num_vars > 54 || num_vars % 2) return APG_ERR_UNSUPPORTED_NUM_VARS;
+  if (u_len != num_vars) return APG_ERR_POINT_LENGTH_MISMATCH;
   if (num_vars > 40) return APG_ERR_OUT_OF_MEMORY;
   std::vector<host::F> uu;
   if (!read_points_u(u, num_vars, uu)) return APG_ERR_NONCANONICAL;
@@ -356,18 +358,19 @@ static int batch_open_common(Ctx& c, const void* const* cols, bool on_device, si
 }
 
 int apg_mercury_batch_open(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_t num_vars, const uint8_t* cms,
-                           const uint8_t* u, uint8_t* transcript, uint8_t* vs_out, uint8_t proof_out[704]) {
+                           const uint8_t* u, size_t u_len, uint8_t* transcript, uint8_t* vs_out,
+                           uint8_t proof_out[704]) {
   return guarded(ctx, [&](Ctx& c) {
-    return batch_open_common(c, (const void* const*)cols, false, k, num_vars, cms, u, transcript, vs_out,
+    return batch_open_common(c, (const void* const*)cols, false, k, num_vars, cms, u, u_len, transcript, vs_out,
                              proof_out);
   });
 }
 
 int apg_mercury_batch_open_device(apg_ctx* ctx, const void* const* d_cols, size_t k, size_t num_vars,
-                                  const uint8_t* cms, const uint8_t* u, uint8_t* transcript, uint8_t* vs_out,
-                                  uint8_t proof_out[704]) {
+                                  const uint8_t* cms, const uint8_t* u, size_t u_len, uint8_t* transcript,
+                                  uint8_t* vs_out, uint8_t proof_out[704]) {
   return guarded(ctx, [&](Ctx& c) {
-    return batch_open_common(c, d_cols, true, k, num_vars, cms, u, transcript, vs_out, proof_out);
+    return batch_open_common(c, d_cols, true, k, num_vars, cms, u, u_len, transcript, vs_out, proof_out);
   });
 }
 

@@ -146,25 +146,27 @@ int apg_commit_batch_device(apg_ctx* ctx, const void* const* d_cols, size_t k, s
 /* ---- Mercury opening (crates/pcs/src/lib.rs) ----------------------------- */
 
 /* pcs::open (lib.rs:313): open the commitment `cm` (64 bytes, absorbed as
- * passed) of the 2^num_vars evaluations `evals` (Fr in memory) at u
- * (num_vars Fr in memory) over the resident SRS, on the transcript (226-byte
+ * passed) of the 2^num_vars evaluations `evals` (Fr in memory) at the point
+ * u (u_len Fr in memory) over the resident SRS, on the transcript (226-byte
  * snapshot, in/out; left where the verifier leaves it, PAIRING_MERGE drawn).
  * Writes v = f(u) (Fr in memory) and the 704-byte MercuryProof::to_bytes.
- * Errors: APG_ERR_UNSUPPORTED_NUM_VARS, APG_ERR_POINT_LENGTH_MISMATCH,
- * APG_ERR_SRS_TOO_SMALL, APG_ERR_DEGENERATE_CHALLENGE. */
+ * Errors, in the reference's order: APG_ERR_UNSUPPORTED_NUM_VARS,
+ * APG_ERR_POINT_LENGTH_MISMATCH (u_len != num_vars), APG_ERR_SRS_TOO_SMALL,
+ * APG_ERR_DEGENERATE_CHALLENGE. */
 int apg_mercury_open(apg_ctx* ctx, const uint8_t* evals, size_t num_vars, const uint8_t cm[64], const uint8_t* u,
-                     uint8_t* transcript, uint8_t v_out[32], uint8_t proof_out[704]);
+                     size_t u_len, uint8_t* transcript, uint8_t v_out[32], uint8_t proof_out[704]);
 /* pcs::batch_open (lib.rs:688, batch_open_stacked at r = []): k columns of one
  * size at one point; cols[j] points at column j (host, Fr in memory), cms is
  * k x 64 bytes. Writes each column's value (vs_out, k x 32, Fr in memory)
- * and the one proof of cm* = sum rho^i cm_i. Errors add APG_ERR_EMPTY_BATCH,
- * APG_ERR_BATCH_LENGTH_MISMATCH is the caller's (k is shared). */
+ * and the one proof of cm* = sum rho^i cm_i. Errors add APG_ERR_EMPTY_BATCH
+ * (k = 0); the column and commitment lists share k. */
 int apg_mercury_batch_open(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_t num_vars, const uint8_t* cms,
-                           const uint8_t* u, uint8_t* transcript, uint8_t* vs_out, uint8_t proof_out[704]);
+                           const uint8_t* u, size_t u_len, uint8_t* transcript, uint8_t* vs_out,
+                           uint8_t proof_out[704]);
 /* As apg_mercury_batch_open with the columns in device memory. */
 int apg_mercury_batch_open_device(apg_ctx* ctx, const void* const* d_cols, size_t k, size_t num_vars,
-                                  const uint8_t* cms, const uint8_t* u, uint8_t* transcript, uint8_t* vs_out,
-                                  uint8_t proof_out[704]);
+                                  const uint8_t* cms, const uint8_t* u, size_t u_len, uint8_t* transcript,
+                                  uint8_t* vs_out, uint8_t proof_out[704]);
 
 /* ---- zerocheck (crates/sumcheck/src/lib.rs) ------------------------------ */
 
