@@ -83,6 +83,10 @@ def fe(x: int) -> bytes:
     return int(x).to_bytes(32, "little")
 
 
+def struct_u32(blob: bytes, off: int) -> int:
+    return int.from_bytes(blob[off:off + 4], "little")
+
+
 class GkrValues:
     """Device-resident layer values from gkr_forward (gkr::LayerValues)."""
 
@@ -330,22 +334,30 @@ class Context:
         return [rs[4 * i:4 * i + 4] for i in range(num_vars)], from_mont_bytes(finals.raw), snap.raw
 
     # ---- GKR ------------------------------------------------------------------
-    def gkr_forward(self, blob: bytes, base, challenges: dict):
+    def gkr_forward(self, blob: bytes, base, challenges: dict, on_device: bool = False):
         """gkr::forward. base: committed columns as Fr in-memory bytes (layout
-        order); challenges: {slot: canonical int}. Returns a GkrValues handle."""
+        order), or device pointers with on_device; challenges: {slot:
+        canonical int}. Returns a GkrValues handle."""
         k = len(base)
-        ptrs = (ctypes.c_char_p * k)(*base)
         slots = sorted(challenges)
         sarr = (ctypes.c_uint32 * max(len(slots), 1))(*slots)
         vals = to_mont_bytes([challenges[s] for s in slots])
         h = ctypes.c_void_p()
-        self._check(lib().apg_gkr_forward(self._h, blob, ctypes.c_size_t(len(blob)), ptrs, sarr, vals,
-                                          ctypes.c_size_t(len(slots)), ctypes.byref(h)))
+        if on_device:
+            ptrs = (ctypes.c_void_p * k)(*base)
+            st = lib().apg_gkr_forward_device(self._h, blob, ctypes.c_size_t(len(blob)), ptrs, sarr, vals,
+                                              ctypes.c_size_t(len(slots)), ctypes.byref(h))
+        else:
+            ptrs = (ctypes.c_char_p * k)(*base)
+            st = lib().apg_gkr_forward(self._h, blob, ctypes.c_size_t(len(blob)), ptrs, sarr, vals,
+                                       ctypes.c_size_t(len(slots)), ctypes.byref(h))
+        self._check(st)
         return GkrValues(self, h)
 
-    def gkr_prove(self, blob: bytes, values: "GkrValues", challenges: dict, transcript: bytes):
+    def gkr_prove(self, blob: bytes, values: "GkrValues", challenges: dict, transcript: bytes,
+                  with_point: bool = False):
         """gkr::prove. Returns (proof as canonical ints in the documented
-        layout, transcript)."""
+        layout, transcript) and, with with_point, the base layer's point."""
         L = lib()
         L.apg_gkr_proof_len.restype = ctypes.c_size_t
         cap = L.apg_gkr_proof_len(blob, ctypes.c_size_t(len(blob)))
@@ -355,9 +367,18 @@ class Context:
         sarr = (ctypes.c_uint32 * max(len(slots), 1))(*slots)
         vals = to_mont_bytes([challenges[s] for s in slots])
         snap = ctypes.create_string_buffer(bytes(transcript), TRANSCRIPT_BYTES)
+        point = ctypes.create_string_buffer(32 * 64)
         self._check(L.apg_gkr_prove(self._h, blob, ctypes.c_size_t(len(blob)), values.handle, sarr, vals,
-                                    ctypes.c_size_t(len(slots)), snap, out, ctypes.c_size_t(cap), ctypes.byref(n)))
-        return from_mont_bytes(out.raw[:n.value]), snap.raw
+                                    ctypes.c_size_t(len(slots)), snap, out, ctypes.c_size_t(cap), ctypes.byref(n),
+                                    point))
+        proof = from_mont_bytes(out.raw[:n.value])
+        if with_point:
+            nv = struct_u32(blob, 8)
+            return proof, snap.raw, point.raw[:32 * nv]
+        return proof, snap.raw
+
+    def srs_share(self, src: "Context"):
+        self._check(lib().apg_srs_share(self._h, src._h))
 
     def witness_digest(self, cols, num_vars: int) -> int:
         k = len(cols)

@@ -121,8 +121,9 @@ void apg_ctx_destroy(apg_ctx* ctx) {
     cudaSetDevice(c.device);
     if (c.stream) cudaStreamSynchronize(c.stream);
     for (auto& b : c.scratch) b.release();
-    for (auto& t : c.tables) cudaFree(t.tab);
-    if (c.srs) cudaFree(c.srs);
+    for (auto& t : c.tables)
+      if (t.owned) cudaFree(t.tab);
+    if (c.srs && c.srs_owned) cudaFree(c.srs);
     if (c.d_flags) cudaFree(c.d_flags);
     if (c.stream) cudaStreamDestroy(c.stream);
   }
@@ -142,11 +143,40 @@ int apg_ctx_synchronize(apg_ctx* ctx) {
 
 static void drop_srs(Ctx& c) {
   APG_CUDA(cudaStreamSynchronize(c.stream));
-  for (auto& t : c.tables) cudaFree(t.tab);
+  for (auto& t : c.tables)
+    if (t.owned) cudaFree(t.tab);
   c.tables.clear();
-  if (c.srs) cudaFree(c.srs);
+  if (c.srs && c.srs_owned) cudaFree(c.srs);
   c.srs = nullptr;
   c.srs_n = 0;
+  c.srs_owned = true;
+}
+
+int apg_srs_share(apg_ctx* dst, apg_ctx* src) {
+  if (!dst || !src || dst == src) return APG_ERR_INVALID_ARGUMENT;
+  if (dst->c.device != src->c.device) return APG_ERR_INVALID_ARGUMENT;
+  std::vector<SrsTable> tabs;
+  Affine* srs;
+  size_t n;
+  {
+    std::lock_guard<std::mutex> lock(src->c.mu);
+    if (!src->c.srs) return APG_ERR_NO_SRS;
+    srs = src->c.srs;
+    n = src->c.srs_n;
+    tabs.assign(src->c.tables.begin(), src->c.tables.end());
+    cudaStreamSynchronize(src->c.stream);
+  }
+  return guarded(dst, [&](Ctx& c) {
+    drop_srs(c);
+    c.srs = srs;
+    c.srs_n = n;
+    c.srs_owned = false;
+    for (auto t : tabs) {
+      t.owned = false;
+      c.tables.push_back(t);
+    }
+    return (int)APG_OK;
+  });
 }
 
 int apg_srs_upload(apg_ctx* ctx, const uint8_t* g1_points, size_t n) {
@@ -420,11 +450,23 @@ size_t apg_gkr_proof_len(const uint8_t* circuit, size_t circuit_len) {
 
 int apg_gkr_prove(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, apg_gkr_values* values,
                   const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, uint8_t* transcript,
-                  uint8_t* proof_out, size_t proof_cap, size_t* proof_len) {
+                  uint8_t* proof_out, size_t proof_cap, size_t* proof_len, uint8_t* point_out) {
   if (!values || values->ctx != ctx) return APG_ERR_INVALID_ARGUMENT;
   return guarded(ctx, [&](Ctx& c) {
     return gkr_prove_impl(c, circuit, circuit_len, values->v, slots, slot_values, n_slots, transcript, proof_out,
-                          proof_cap, proof_len);
+                          proof_cap, proof_len, point_out);
+  });
+}
+
+int apg_gkr_forward_device(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, const void* const* d_base,
+                           const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, apg_gkr_values** out) {
+  if (!out) return APG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  return guarded(ctx, [&](Ctx& c) {
+    GkrValues* v = gkr_forward_impl(c, circuit, circuit_len, (const uint8_t* const*)d_base, true, slots, slot_values,
+                                    n_slots);
+    *out = new apg_gkr_values{v, ctx};
+    return (int)APG_OK;
   });
 }
 

@@ -74,6 +74,7 @@ struct SrsTable {
   int c = 0, windows = 0;
   size_t n = 0;
   Affine* tab = nullptr;
+  bool owned = true;  // false: borrowed from another context (apg_srs_share)
 };
 
 enum ScratchSlot {
@@ -122,6 +123,7 @@ struct Ctx {
   std::string last_error;
   Affine* srs = nullptr;
   size_t srs_n = 0;
+  bool srs_owned = true;  // false: borrowed from another context (apg_srs_share)
   std::vector<SrsTable> tables;
   DevBuf scratch[S_COUNT];
   uint32_t* d_flags = nullptr;  // device error flags (DeviceFlag bits)

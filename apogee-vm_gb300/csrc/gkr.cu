@@ -317,7 +317,7 @@ size_t gkr_proof_elems(const Circuit& C) {
 
 int gkr_prove_impl(Ctx& c, const uint8_t* blob, size_t blob_len, GkrValues* V, const uint32_t* slots,
                    const uint8_t* slot_values, size_t n_slots, uint8_t* transcript, uint8_t* proof_out,
-                   size_t proof_cap, size_t* proof_len) {
+                   size_t proof_cap, size_t* proof_len, uint8_t* point_out) {
   if (!V || !transcript || !proof_len) return APG_ERR_INVALID_ARGUMENT;
   Circuit C = parse_circuit_blob(blob, blob_len);
   const Circuit& VC = V->circuit;
@@ -404,6 +404,8 @@ int gkr_prove_impl(Ctx& c, const uint8_t* blob, size_t blob_len, GkrValues* V, c
     memcpy(proof_out + off, v.data(), 32 * v.size());
     off += 32 * v.size();
   }
+  // The base layer's point: what the committed columns are opened at.
+  if (point_out) memcpy(point_out, point.data(), 32 * point.size());
   tr.save(transcript);
   c.check_flags();
   return APG_OK;

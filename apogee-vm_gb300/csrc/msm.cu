@@ -509,7 +509,7 @@ const SrsTable* srs_table(Ctx& c, int cbits, size_t need) {
   for (auto it = c.tables.begin(); it != c.tables.end(); ++it)
     if (it->c == cbits) {
       APG_CUDA(cudaStreamSynchronize(c.stream));
-      cudaFree(it->tab);
+      if (it->owned) cudaFree(it->tab);
       c.tables.erase(it);
       break;
     }

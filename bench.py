@@ -22,6 +22,7 @@ import argparse
 import json
 import math
 import os
+import random
 import statistics
 import subprocess
 import sys
@@ -216,6 +217,108 @@ def run_msm_only(args):
     return 0
 
 
+def run_shard_workloads(ctx, local, contexts=6, serve_budget_gb=150):
+    """Configs 1-5 beside the headline: the small plain case, one execution
+    shard, the largest shard's commit + batched opening, the 207-shard mix
+    proved one shard at a time vs concurrently, and Poisson serving."""
+    import torch
+
+    import apogee_gpu as A
+    import circuits as Cm
+    import shard
+
+    dev = f"cuda:{local}"
+    out = {}
+
+    def timed(fn, reps=3):
+        best = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        return best
+
+    # Config 1: commit one 2^16 column, then zerocheck of a*b over two columns
+    # (witness digest absorbed first), challenges from the seeded duplex.
+    cols = shard.device_columns(torch, 1 << 16, 2, SEED + 1, dev, ctx)
+    host_cols = [bytes(c.cpu().numpy().tobytes()) for c in cols]
+
+    def cfg1():
+        ctx.commit_device(cols[0].data_ptr(), 16)
+        d = ctx.witness_digest(host_cols, 16)
+        tr = A.transcript_append_scalars(A.transcript_init(), 8, [d])
+        ctx.prove_zerocheck([(1, 0, 1)], [c.data_ptr() for c in cols], 16, tr, on_device=True)
+
+    cfg1()
+    out["cfg1_small_ms"] = timed(cfg1) * 1e3
+
+    # Config 2: 8 columns x 2^20: commit, then the 12-list GKR proof.
+    cols2 = shard.device_columns(torch, 1 << 20, 8, SEED + 2, dev, ctx)
+    blob2 = Cm.shard_circuit(20, 8).to_blob()
+
+    def cfg2():
+        ptrs = [c.data_ptr() for c in cols2]
+        cms = ctx.commit_batch_device(ptrs, 20)
+        limbs = []
+        for cm in cms:
+            limbs += shard.g1_limbs(cm)
+        tr = A.transcript_append_scalars(A.transcript_init(), 3, limbs)
+        tr, gamma = A.transcript_challenge(tr, 33)
+        v = ctx.gkr_forward(blob2, ptrs, {0: gamma}, on_device=True)
+        ctx.gkr_prove(blob2, v, {0: gamma}, tr)
+        v.free()
+
+    cfg2()
+    out["cfg2_shard_2p20_ms"] = timed(cfg2) * 1e3
+    del cols2
+
+    # Config 3: 16 columns x 2^22: commit, then the batched opening.
+    cols3 = shard.device_columns(torch, 1 << 22, 16, SEED + 3, dev, ctx)
+    rng = random.Random(SEED)
+    u3 = [rng.randrange(A.P_R) for _ in range(22)]
+
+    def cfg3():
+        ptrs = [c.data_ptr() for c in cols3]
+        cms = ctx.commit_batch_device(ptrs, 22)
+        ctx.batch_open(ptrs, 22, cms, u3, A.transcript_init(), on_device=True)
+
+    cfg3()
+    out["cfg3_commit_open_2p22x16_ms"] = timed(cfg3, reps=2) * 1e3
+    del cols3
+    torch.cuda.empty_cache()
+
+    # Configs 4 and 5: the 207-shard mix, columns resident in HBM.
+    specs = shard.shard_mix(207)
+    columns = {s["index"]: shard.device_columns(torch, 1 << s["log_rows"], s["cols"], SEED + 100 + s["index"], dev,
+                                                ctx) for s in specs}
+    torch.cuda.synchronize()
+    shard.prove_sequential(ctx, specs[:12], columns)  # warm the circuits and scratch
+    seq_t, _ = shard.prove_sequential(ctx, specs, columns)
+    extra = [A.Context(local) for _ in range(contexts - 1)]
+    for c in extra:
+        c.srs_share(ctx)
+    ctxs = [ctx] + extra
+    shard.prove_batched(ctxs, specs[:24], columns)
+    bat_t, _ = shard.prove_batched(ctxs, specs, columns)
+    cap = len(specs) / bat_t
+    wall, lat, _ = shard.serve(ctxs, specs, columns, rate=0.8 * cap, budget_bytes=int(serve_budget_gb * 1e9))
+    for c in extra:
+        c.close()
+    out["cfg4"] = {"shards": len(specs), "points": sum(s["cols"] << s["log_rows"] for s in specs),
+                   "sequential_shards_per_s": len(specs) / seq_t, "batched_shards_per_s": cap,
+                   "batched_over_sequential": seq_t / bat_t, "contexts": contexts,
+                   "mix": "207 shards, 23 families, 2^8..2^22 rows (even), 4-16 columns"}
+    out["cfg5"] = {"rate_per_s": 0.8 * cap, "shards_per_s": len(lat) / wall,
+                   "p50_ms": shard.percentile(lat, 0.50) * 1e3, "p99_ms": shard.percentile(lat, 0.99) * 1e3,
+                   "hbm_budget_gb": serve_budget_gb, "requests": len(lat)}
+    del columns
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -329,6 +432,13 @@ def run_gpu(args):
         "msm_uniform_points_per_s": n / (tot_ms / tot_n / 1e3), "algorithmic_imad_per_launch": algo,
     }
 
+    shards = None
+    if args.shards:
+        try:
+            shards = run_shard_workloads(ctx, local)
+        except Exception as e:  # reported, never allowed to hide the headline
+            shards = {"error": repr(e)}
+
     cpu = None
     if rank == 0:
         threads = os.cpu_count() or 1
@@ -354,7 +464,7 @@ def run_gpu(args):
                        "msm_points": n, "columns_per_gpu": k, "parallelism": f"replicas x{world}",
                        "l2": "inputs 2 GiB per GPU > 129 MB L2, no flush needed"},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
-            "gpu_launches": launches,
+            "gpu_launches": launches, "shard_workloads": shards,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -372,6 +482,8 @@ def main():
     ap.add_argument("--log2n", type=int, default=22)
     ap.add_argument("--cols", type=int, default=16)
     ap.add_argument("--only-msm", action="store_true", help="lean uniform-scalar MSM case for profiling")
+    ap.add_argument("--no-shards", dest="shards", action="store_false",
+                    help="skip the per-config shard timings and the 207-shard mix / serving run")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -87,6 +87,11 @@ int apg_srs_generate(apg_ctx* ctx, const uint8_t tau[32], size_t n);
 int apg_srs_download(apg_ctx* ctx, uint8_t* g1_points, size_t n);
 /* Number of resident powers. */
 size_t apg_srs_len(apg_ctx* ctx);
+/* Let `dst` read the SRS (and the window tables built so far) that `src`
+ * holds on the same device, without a copy: contexts that prove shards
+ * concurrently share one resident SRS. `src` must outlive `dst`'s use of it
+ * and must not replace its SRS meanwhile. */
+int apg_srs_share(apg_ctx* dst, apg_ctx* src);
 /* Precompute the window table that commits over the resident SRS read
  * (window width `cbits`, 0 = the library's choice). Optional: the first
  * commit builds it. Costs windows x n x 64 bytes of device memory. */
@@ -232,10 +237,15 @@ size_t apg_gkr_proof_len(const uint8_t* circuit, size_t circuit_len);
  * transcript the caller has bound to the base (226-byte snapshot, in/out).
  * The proof (GkrProof, crates/gkr-verify/src/lib.rs:90-92) is written as, for
  * each gate list k = 0 .. depth-1, its rounds (4 Fr each) then its claims,
- * all Fr in memory. */
+ * all Fr in memory. point_out (nullable, trace_vars x 32 bytes) receives the
+ * base layer's point, the one crates/prover's replay_point re-derives
+ * (crates/prover/src/lib.rs:1111-1140) and the openings use. */
 int apg_gkr_prove(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, apg_gkr_values* values,
                   const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, uint8_t* transcript,
-                  uint8_t* proof_out, size_t proof_cap, size_t* proof_len);
+                  uint8_t* proof_out, size_t proof_cap, size_t* proof_len, uint8_t* point_out);
+/* As apg_gkr_forward with the base columns already in device memory. */
+int apg_gkr_forward_device(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, const void* const* d_base,
+                           const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, apg_gkr_values** out);
 
 /* ---- transcript (crates/transcript/src/lib.rs:214-346) ------------------- */
 
