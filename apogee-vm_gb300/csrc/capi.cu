@@ -10,6 +10,10 @@ struct apg_ctx {
   Ctx c;
 };
 
+extern "C" {
+static void release_lane(Ctx& c);
+}
+
 namespace {
 
 template <class F>
@@ -120,6 +124,7 @@ void apg_ctx_destroy(apg_ctx* ctx) {
     Ctx& c = ctx->c;
     cudaSetDevice(c.device);
     if (c.stream) cudaStreamSynchronize(c.stream);
+    release_lane(c);
     for (auto& b : c.scratch) b.release();
     for (auto& t : c.tables)
       if (t.owned) cudaFree(t.tab);
@@ -266,21 +271,87 @@ int apg_commit_device(apg_ctx* ctx, const void* d_evals, size_t num_vars, uint8_
   return guarded(ctx, [&](Ctx& c) { return commit_common(c, d_evals, true, false, num_vars, out); });
 }
 
+// The context's second lane, borrowing its SRS and every window table built
+// so far (refreshed per batch so the lane never builds a table of its own).
+static Ctx& lane_of(Ctx& c) {
+  if (!c.lane) {
+    std::unique_ptr<Ctx> L(new Ctx());
+    L->device = c.device;
+    L->sm_count = c.sm_count;
+    APG_CUDA(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
+    APG_CUDA(cudaMalloc(&L->d_flags, 4));
+    APG_CUDA(cudaMemset(L->d_flags, 0, 4));
+    c.lane = std::move(L);
+  }
+  Ctx& L = *c.lane;
+  for (auto& t : L.tables)
+    if (t.owned) cudaFree(t.tab);
+  L.tables.clear();
+  for (auto t : c.tables) {
+    t.owned = false;
+    L.tables.push_back(t);
+  }
+  L.srs = c.srs;
+  L.srs_n = c.srs_n;
+  L.srs_owned = false;
+  return L;
+}
+
+static void release_lane(Ctx& c) {
+  if (!c.lane) return;
+  Ctx& L = *c.lane;
+  cudaStreamSynchronize(L.stream);
+  for (auto& b : L.scratch) b.release();
+  for (auto& t : L.tables)
+    if (t.owned) cudaFree(t.tab);
+  if (L.d_flags) cudaFree(L.d_flags);
+  if (L.stream) cudaStreamDestroy(L.stream);
+  c.lane.reset();
+}
+
+// k commits of one size over the resident SRS, alternating between the
+// context's two lanes. Columns come from device pointers or, when `host` is
+// set, from host memory copied on the lane that commits them.
+static int commit_batch_lanes(Ctx& c, const void* const* cols, bool host, size_t k, size_t num_vars, uint8_t* out) {
+  if (!cols || !out) return APG_ERR_INVALID_ARGUMENT;
+  if (!mercury_num_vars_ok(num_vars)) return APG_ERR_UNSUPPORTED_NUM_VARS;
+  if (!c.srs) return APG_ERR_NO_SRS;
+  const size_t n = (size_t)1 << num_vars;
+  if (c.srs_n < n) return APG_ERR_SRS_TOO_SMALL;
+  if (k == 0) return APG_OK;
+  if (!commit_table(c, n)) throw Error(APG_ERR_INTERNAL, "no SRS window table");
+  Ctx& L = lane_of(c);
+  Ctx* lanes[2] = {&c, &L};
+  uint8_t* d_out = c.scratch[S_TMP5].as<uint8_t>(64 * k);
+  // The second lane starts after everything already queued on the first.
+  cudaEvent_t ev;
+  APG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  APG_CUDA(cudaEventRecord(ev, c.stream));
+  APG_CUDA(cudaStreamWaitEvent(L.stream, ev, 0));
+  for (size_t j = 0; j < k; ++j) {
+    Ctx& X = *lanes[j & 1];
+    const SrsTable* t = commit_table(X, n);
+    const void* src = cols[j];
+    if (host) {
+      void* buf = X.scratch[S_SCALARS].get(32 * n);
+      APG_CUDA(cudaMemcpyAsync(buf, cols[j], 32 * n, cudaMemcpyHostToDevice, X.stream));
+      src = buf;
+    }
+    msm_device(X, nullptr, t, src, false, false, n, d_out + 64 * j, nullptr);
+  }
+  APG_CUDA(cudaEventRecord(ev, L.stream));
+  APG_CUDA(cudaStreamWaitEvent(c.stream, ev, 0));
+  APG_CUDA(cudaEventDestroy(ev));
+  APG_CUDA(cudaMemcpyAsync(out, d_out, 64 * k, cudaMemcpyDeviceToHost, c.stream));
+  L.check_flags();
+  c.check_flags();
+  c.launches += L.launches;
+  L.launches = 0;
+  return APG_OK;
+}
+
 int apg_commit_batch_device(apg_ctx* ctx, const void* const* d_cols, size_t k, size_t num_vars, uint8_t* out) {
-  return guarded(ctx, [&](Ctx& c) {
-    if (!d_cols || !out) return (int)APG_ERR_INVALID_ARGUMENT;
-    if (!mercury_num_vars_ok(num_vars)) return (int)APG_ERR_UNSUPPORTED_NUM_VARS;
-    if (!c.srs) return (int)APG_ERR_NO_SRS;
-    size_t n = (size_t)1 << num_vars;
-    if (c.srs_n < n) return (int)APG_ERR_SRS_TOO_SMALL;
-    const SrsTable* t = commit_table(c, n);
-    if (!t) throw Error(APG_ERR_INTERNAL, "no SRS window table");
-    uint8_t* d_out = c.scratch[S_TMP5].as<uint8_t>(64 * k);
-    for (size_t j = 0; j < k; ++j) msm_device(c, nullptr, t, d_cols[j], false, false, n, d_out + 64 * j, nullptr);
-    APG_CUDA(cudaMemcpyAsync(out, d_out, 64 * k, cudaMemcpyDeviceToHost, c.stream));
-    c.check_flags();
-    return (int)APG_OK;
-  });
+  return guarded(ctx, [&](Ctx& c) { return commit_batch_lanes(c, d_cols, false, k, num_vars, out); });
 }
 
 int apg_fr_to_mont_device(apg_ctx* ctx, void* d_vals, size_t n) {
@@ -533,14 +604,7 @@ uint64_t apg_ctx_launch_count(apg_ctx* ctx) {
 }
 
 int apg_commit_batch(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_t num_vars, uint8_t* out) {
-  return guarded(ctx, [&](Ctx& c) {
-    if (!cols || !out) return (int)APG_ERR_INVALID_ARGUMENT;
-    for (size_t j = 0; j < k; ++j) {
-      int st = commit_common(c, cols[j], false, false, num_vars, out + 64 * j);
-      if (st) return st;
-    }
-    return (int)APG_OK;
-  });
+  return guarded(ctx, [&](Ctx& c) { return commit_batch_lanes(c, (const void* const*)cols, true, k, num_vars, out); });
 }
 
 }  // extern "C"

@@ -129,6 +129,11 @@ struct Ctx {
   uint32_t* d_flags = nullptr;  // device error flags (DeviceFlag bits)
   uint64_t launches = 0;        // kernels launched on this context
   Timers timers;
+  // A second stream with its own scratch that borrows this context's SRS:
+  // batches of commits alternate between the two so that one MSM's
+  // latency-bound tail (and the next column's copy) overlaps another's
+  // bucket accumulation.
+  std::unique_ptr<Ctx> lane;
 
   // Bracket work on the stream with a timer's events (no-op unless enabled).
   cudaEvent_t timer_begin() {

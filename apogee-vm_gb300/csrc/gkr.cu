@@ -290,12 +290,14 @@ GkrValues* gkr_forward_impl(Ctx& c, const uint8_t* blob, size_t blob_len, const 
     const Fr** d_cols = c.scratch[S_TMP5].as<const Fr*>(w);
     APG_CUDA(cudaMemcpyAsync(d_cols, cols.data(), sizeof(Fr*) * w, cudaMemcpyHostToDevice, c.stream));
     const size_t slots_n = (size_t)P.cached_slot0 + L.cached.size();
-    const size_t smem = std::max<size_t>(slots_n, 1) * 32 * kFwdThreads;
+    int threads = kFwdThreads;
+    while (threads > 32 && std::max<size_t>(slots_n, 1) * 32 * threads > 200 * 1024) threads /= 2;
+    const size_t smem = std::max<size_t>(slots_n, 1) * 32 * threads;
     if (smem > 200 * 1024) throw Error(APG_ERR_BAD_CIRCUIT, "gate list too wide for one thread block");
     APG_CUDA(cudaFuncSetAttribute(k_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     cudaEvent_t t0 = c.timer_begin();
     if (L.width)
-      launch(c, k_forward, (unsigned)((rows + kFwdThreads - 1) / kFwdThreads), kFwdThreads, smem, P, w, nv, vk,
+      launch(c, k_forward, (unsigned)((rows + threads - 1) / threads), threads, smem, P, w, nv, vk,
              (const Fr* const*)d_cols, rows, L.halving ? 1 : 0, (int)L.width, V->layers[k + 1]);
     c.timer_end(APG_TIMER_GKR_FORWARD, t0);
     // The program and column list buffers are reused by the next layer.

@@ -208,7 +208,11 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
   }
   const int n_val = nd + (int)vkinds.size();
   const int slots = 2 * n_val + n_cached;
-  const size_t smem = (size_t)std::max(slots, 1) * 32 * kRoundThreads;
+  // Wide gate lists get narrower blocks (a power of two, for the reduction
+  // tree) so that every thread's slots still fit in shared memory.
+  int threads = kRoundThreads;
+  while (threads > 32 && (size_t)std::max(slots, 1) * 32 * threads > 200 * 1024) threads /= 2;
+  const size_t smem = (size_t)std::max(slots, 1) * 32 * threads;
   if (smem > 200 * 1024) throw Error(APG_ERR_BAD_CIRCUIT, "gate list too wide for one thread block");
   APG_CUDA(cudaFuncSetAttribute(k_round, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   const int max_blocks = c.sm_count * 8;
@@ -235,9 +239,9 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
     A.slots_step0 = n_val + n_cached;
     A.n_val_slots = n_val;
     VirtualRound V = virtual_round(point, n);
-    const int blocks = (int)std::min<size_t>((A.npairs + kRoundThreads - 1) / kRoundThreads, (size_t)max_blocks);
+    const int blocks = (int)std::min<size_t>((A.npairs + threads - 1) / threads, (size_t)max_blocks);
     cudaEvent_t t0 = c.timer_begin();
-    launch(c, k_round, blocks, kRoundThreads, smem, A, P, V, partials);
+    launch(c, k_round, blocks, threads, smem, A, P, V, partials);
     c.timer_end(APG_TIMER_SUMCHECK_ROUND, t0);
     launch(c, k_round_total, 1, 256, 0, (const Fr*)partials, blocks, d_out);
     F v[4];

@@ -97,20 +97,43 @@ def device_columns(torch, n: int, k: int, seed: int, device: str, ctx):
     return cols
 
 
+TAG_SHARD_TS_WINDOW = 40
+TAG_LOOKUP_CHALLENGE = 33
+
+
+def statement_digest(spec) -> int:
+    """A stand-in for the statement digest a shard transcript is seeded with
+    (the global phase's output, not part of the hot path): seeded per shard."""
+    return random.Random(0x5EED0000 + spec["index"]).randrange(C.P_R)
+
+
+def shard_transcript(spec, cms):
+    """verifier_core::shard_transcript (crates/verifier-core/src/statement.rs:
+    548-572): SHARD_SEED [digest, family, index], SHARD_TS_WINDOW [lo, hi],
+    the witness commitments as one G1 list under COMMITMENT, then g and beta
+    under LOOKUP_CHALLENGE. Returns the transcript snapshot, g and beta."""
+    tr = A.transcript_append_scalars(A.transcript_init(), TAG_SHARD_SEED,
+                                     [statement_digest(spec), spec["family"], spec["index"]])
+    lo = spec["index"] << 22
+    tr = A.transcript_append_scalars(tr, TAG_SHARD_TS_WINDOW, [lo, lo + (1 << spec["log_rows"])])
+    limbs = []
+    for cm in cms:
+        limbs += g1_limbs(cm)
+    tr = A.transcript_append_scalars(tr, TAG_COMMITMENT, limbs)
+    tr, g = A.transcript_challenge(tr, TAG_LOOKUP_CHALLENGE)
+    tr, beta = A.transcript_challenge(tr, TAG_LOOKUP_CHALLENGE)
+    return tr, g, beta
+
+
 def prove_shard(ctx, spec, cols):
     """One shard's hot path; cols are device tensors. Returns the commitments,
     the GKR proof, the base point, the opened values and the opening proof."""
     n_vars = spec["log_rows"]
     ptrs = [t.data_ptr() for t in cols]
     cms = ctx.commit_batch_device(ptrs, n_vars)
-    tr = A.transcript_append_scalars(A.transcript_init(), TAG_SHARD_SEED, [spec["index"], spec["family"]])
-    limbs = []
-    for cm in cms:
-        limbs += g1_limbs(cm)
-    tr = A.transcript_append_scalars(tr, TAG_COMMITMENT, limbs)
-    tr, gamma = A.transcript_challenge(tr, 33)  # LOOKUP_CHALLENGE: the circuit's external challenge
+    tr, g, beta = shard_transcript(spec, cms)
     blob = shard_circuit(n_vars, spec["cols"])
-    ch = {0: gamma}
+    ch = {0: g, 1: beta}
     values = ctx.gkr_forward(blob, ptrs, ch, on_device=True)
     proof, tr, point = ctx.gkr_prove(blob, values, ch, tr, with_point=True)
     values.free()

@@ -87,6 +87,18 @@ def test_every_virtual_table_at_16_vars(ctx):
     run_case(ctx, c, 77)
 
 
+def test_wide_layers(ctx):
+    """40 committed columns: the halving list's 80 tables need narrower
+    thread blocks to keep every thread's operand slots in shared memory."""
+    import circuits as C
+
+    c = C.Circuit(5, 40)
+    c.add_layer([C.product(2, C.col(j), C.col((j + 1) % 40)) for j in range(40)],
+                enforcing=[C.linear([(1, C.col(j)) for j in range(40)], 3)])
+    c.add_layer([C.tree_product(C.col(j)) for j in range(40)], halving=True)
+    run_case(ctx, c, 41)
+
+
 def test_shard_circuit_reduced(ctx):
     """The single-execution-shard circuit shape at 2^10 rows."""
     import circuits as C

@@ -36,29 +36,29 @@ def oracle_shard(spec, cols_ints, srs, tau):
         out = O.buf(64)
         assert O.lib().oracle_commit(srs, ctypes.c_size_t(n), b"".join(O.fe(x) for x in c), nv, 4, out) == 0
         cms.append(out.raw)
+    # The shard transcript's schedule (verifier-core statement.rs:548-572).
     snap = O.new_snapshot()
-    O.transcript_op(snap, 2, 39, O.fe(spec["index"]) + O.fe(spec["family"]), 2)
+    lo = spec["index"] << 22
+    seed = [shard.statement_digest(spec), spec["family"], spec["index"]]
+    O.transcript_op(snap, 2, 39, b"".join(O.fe(x) for x in seed), 3)
+    O.transcript_op(snap, 2, 40, O.fe(lo) + O.fe(lo + n), 2)
     limbs = []
     for cm in cms:
         limbs += shard.g1_limbs(cm)
     O.transcript_op(snap, 2, 3, b"".join(O.fe(x) for x in limbs), len(limbs))
-    gamma = O.fe_int(O.transcript_op(snap, 4, 33))
+    g = O.fe_int(O.transcript_op(snap, 4, 33))
+    beta = O.fe_int(O.transcript_op(snap, 4, 33))
     blob = shard.shard_circuit(nv, spec["cols"])
-    import circuits as C
-
-    # proof length and top layer for the oracle call
-    depth = 1 + nv
     proof_elems = 4 * nv + spec["cols"] + sum(4 * (nv - 1 - k) + 2 * spec["cols"] for k in range(nv))
-    slots = (ctypes.c_uint32 * 1)(0)
+    slots = (ctypes.c_uint32 * 2)(0, 1)
     s = (ctypes.c_uint8 * O.SNAP).from_buffer(snap)
     pr = O.buf(32 * proof_elems)
     top = O.buf(32 * spec["cols"])
     base = b"".join(O.fe(x) for c in cols_ints for x in c)
-    assert O.lib().oracle_gkr_prove(blob, ctypes.c_size_t(len(blob)), base, slots, O.fe(gamma), ctypes.c_size_t(1),
-                                     s, pr, top) == 0
+    assert O.lib().oracle_gkr_prove(blob, ctypes.c_size_t(len(blob)), base, slots, O.fe(g) + O.fe(beta),
+                                     ctypes.c_size_t(2), s, pr, top) == 0
     proof = [O.fe_int(pr.raw[32 * i:32 * i + 32]) for i in range(proof_elems)]
-    # The base point: replay of the last (lowest) list, a halving list when nv >= 1.
-    return cms, proof, snap, gamma
+    return cms, proof, snap, g
 
 
 def test_shard_pipeline_matches_oracle(env):
