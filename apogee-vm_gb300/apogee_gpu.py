@@ -93,6 +93,7 @@ class GkrValues:
     def __init__(self, ctx, handle):
         self.ctx = ctx
         self.handle = handle
+        ctx._values.add(self)
 
     def read(self, layer: int, col: int):
         L = lib()
@@ -105,9 +106,12 @@ class GkrValues:
         return from_mont_bytes(out.raw)
 
     def free(self):
-        if self.handle:
+        # Values live on their context's device memory: free them while the
+        # context is open (Context.close frees any still alive first).
+        if self.handle and self.ctx._h:
             lib().apg_gkr_values_free(self.handle)
-            self.handle = None
+        self.handle = None
+        self.ctx._values.discard(self)
 
     def __del__(self):
         try:
@@ -152,6 +156,9 @@ class Context:
     """One device context: a CUDA stream, scratch memory and a resident SRS."""
 
     def __init__(self, device: int = 0):
+        import weakref
+
+        self._values = weakref.WeakSet()
         self._h = ctypes.c_void_p()
         st = lib().apg_ctx_create(device, ctypes.byref(self._h))
         if st != 0:
@@ -159,6 +166,8 @@ class Context:
 
     def close(self):
         if self._h:
+            for v in list(self._values):
+                v.free()
             lib().apg_ctx_destroy(self._h)
             self._h = ctypes.c_void_p()
 

@@ -259,7 +259,8 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
     for (int k = 0; k < nd; ++k) APG_CUDA(cudaMemcpyAsync(&finals[k], src[k], 32, cudaMemcpyDeviceToHost, c.stream));
   } else {
     const Fr* base = n >= 2 ? lvl[(n - 1) & 1] : nullptr;
-    launch(c, k_final_bind, 1, 64, 0, (const Fr* const*)d_src, base, (size_t)2, n <= 1 ? 1 : 0, nd, to_dev(chal),
+    launch(c, k_final_bind, (unsigned)((nd + 63) / 64), 64, 0, (const Fr* const*)d_src, base, (size_t)2,
+           n <= 1 ? 1 : 0, nd, to_dev(chal),
            d_fin);
     APG_CUDA(cudaMemcpyAsync(finals.data(), d_fin, 32 * (size_t)nd, cudaMemcpyDeviceToHost, c.stream));
   }

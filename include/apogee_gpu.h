@@ -230,6 +230,7 @@ int apg_gkr_forward(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, co
 int apg_gkr_values_read(apg_gkr_values* values, size_t layer, size_t col, uint8_t* out);
 /* Entries per column of layer `layer`. */
 size_t apg_gkr_values_len(apg_gkr_values* values, size_t layer);
+/* Free forward's values; call it before destroying their context. */
 void apg_gkr_values_free(apg_gkr_values* values);
 /* Bytes of the proof apg_gkr_prove writes for this circuit (0 if malformed). */
 size_t apg_gkr_proof_len(const uint8_t* circuit, size_t circuit_len);
