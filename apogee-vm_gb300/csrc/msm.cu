@@ -421,6 +421,23 @@ __global__ void k_sum(const Xyzz* in, int M, Xyzz* out) {
   if (threadIdx.x == 0) st_xyzz(&out[sp], sh[0]);
 }
 
+// First stage of a wide sum: block b of space sp folds in[sp*M + b*256 ..
+// +256) into part[sp*gridDim.x + b], two points a thread then a tree.
+__global__ void k_sum_blocks(const Xyzz* in, int M, Xyzz* part) {
+  __shared__ Xyzz sh[128];
+  const int sp = blockIdx.y, b = blockIdx.x;
+  const int k0 = b * 256 + threadIdx.x, k1 = k0 + 128;
+  Xyzz acc = k0 < M ? ld_xyzz(&in[(size_t)sp * M + k0]) : xyzz_inf();
+  if (k1 < M) acc = xyzz_add(acc, ld_xyzz(&in[(size_t)sp * M + k1]));
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int off = 64; off > 0; off >>= 1) {
+    if (threadIdx.x < (unsigned)off) sh[threadIdx.x] = xyzz_add(sh[threadIdx.x], sh[threadIdx.x + off]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) st_xyzz(&part[(size_t)sp * gridDim.x + b], sh[0]);
+}
+
 // tsum[level*spaces + sp] holds level sums; combine by Horner in `fan`, then
 // combine spaces (windows) by Horner in 2^c, normalise and write 64 bytes.
 __global__ void k_finish(const Xyzz* tsum, int levels, int spaces, int fan_log, int c, uint32_t* out64) {
@@ -622,7 +639,15 @@ void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* 
     int G = (M + kLevelFan - 1) / kLevelFan;
     Xyzz* outR = (l & 1) ? lvlB : lvlA;
     launch(c, k_level, blocks_for<int>((size_t)spaces * G, 64), 64, 0, lvl_in, M, spaces, kLevelFan, outT, outR);
-    launch(c, k_sum, spaces, 128, 0, (const Xyzz*)outT, G, tsum + (size_t)l * spaces);
+    if (G > 256) {
+      // Wide levels: a two-stage tree keeps the serial chain short.
+      const int nblk = (G + 255) / 256;
+      Xyzz* part = c.scratch[S_TMP3].as<Xyzz>((size_t)spaces * nblk);
+      launch(c, k_sum_blocks, dim3(nblk, spaces), 128, 0, (const Xyzz*)outT, G, part);
+      launch(c, k_sum, spaces, 128, 0, (const Xyzz*)part, nblk, tsum + (size_t)l * spaces);
+    } else {
+      launch(c, k_sum, spaces, 128, 0, (const Xyzz*)outT, G, tsum + (size_t)l * spaces);
+    }
     lvl_in = outR;
     M = G;
   }

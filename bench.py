@@ -217,6 +217,59 @@ def run_msm_only(args):
     return 0
 
 
+def run_profile_case(args):
+    """One lean hot-path case for profilers: `zerocheck` (a*b over two
+    2^log2n columns, no witness digest), `gkr` (the 12-list shard circuit at
+    2^log2n rows, forward + prove) or `open` (one Mercury opening at
+    2^log2n). Prints the per-kernel timers as JSON."""
+    import numpy as np
+    import torch
+
+    import apogee_gpu as A
+    import circuits as Cm
+    import shard
+
+    local = env_int("LOCAL_RANK", 0)
+    torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
+    n = args.log2n
+    ctx = A.Context(local)
+    if args.profile_case == "open":
+        ctx.srs_generate((TAU_SEED * 0x9E3779B97F4A7C15) % A.P_R, 1 << n)
+        ctx.srs_prepare()
+    cols = shard.device_columns(torch, 1 << n, 2 if args.profile_case != "gkr" else 8, SEED, dev, ctx)
+    rng = random.Random(SEED)
+    blob = Cm.shard_circuit(n, 8).to_blob() if args.profile_case == "gkr" else None
+    u = [rng.randrange(A.P_R) for _ in range(n)]
+    cm = ctx.commit_device(cols[0].data_ptr(), n) if args.profile_case == "open" else None
+
+    def once():
+        if args.profile_case == "zerocheck":
+            ctx.prove_zerocheck([(1, 0, 1)], [c.data_ptr() for c in cols], n, A.transcript_init(), on_device=True)
+        elif args.profile_case == "gkr":
+            v = ctx.gkr_forward(blob, [c.data_ptr() for c in cols], {0: 5}, on_device=True)
+            ctx.gkr_prove(blob, v, {0: 5}, A.transcript_init())
+            v.free()
+        else:
+            ctx.batch_open([cols[0].data_ptr()], n, [cm], u, A.transcript_init(), on_device=True)
+
+    for _ in range(args.warmup):
+        once()
+    ctx.set_timing(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        once()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / args.steps
+    timers = {name: ctx.timer(i) for i, name in enumerate(["msm_accumulate", "msm_total", "sumcheck_round",
+                                                            "gkr_forward", "mercury_pass"])}
+    print(json.dumps({"case": args.profile_case, "log2n": n, "ms_per_call": dt * 1e3,
+                      "timers_ms_launches": timers}), flush=True)
+    ctx.close()
+    return 0
+
+
 def run_shard_workloads(ctx, local, contexts=6, serve_budget_gb=150):
     """Configs 1-5 beside the headline: the small plain case, one execution
     shard, the largest shard's commit + batched opening, the 207-shard mix
@@ -484,11 +537,15 @@ def main():
     ap.add_argument("--only-msm", action="store_true", help="lean uniform-scalar MSM case for profiling")
     ap.add_argument("--no-shards", dest="shards", action="store_false",
                     help="skip the per-config shard timings and the 207-shard mix / serving run")
+    ap.add_argument("--profile-case", choices=["zerocheck", "gkr", "open"], default=None,
+                    help="run one lean sumcheck / GKR / opening case for profilers")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.only_msm:
         return run_msm_only(args)
+    if args.profile_case:
+        return run_profile_case(args)
     return run_gpu(args)
 
 
