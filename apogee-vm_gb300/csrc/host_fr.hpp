@@ -6,9 +6,7 @@
 // crates/sumcheck/src/lib.rs:294-305).
 //
 // Fr is kept in Montgomery form over four 64-bit limbs (R = 2^256), the same
-// bytes the device and the reference hold. The product is separated operand
-// scanning: a full 512-bit schoolbook product, then four word-by-word
-// Montgomery reductions.
+// bytes the device and the reference hold.
 #pragma once
 #include <array>
 #include <cstdint>
@@ -88,32 +86,43 @@ inline F fsub(const F& a, const F& b) {
 
 inline F fneg(const F& a) { return a.zero() ? a : fsub(fzero(), a); }
 
-inline F fmul(const F& a, const F& b) {
-  uint64_t t[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+// Coarsely integrated operand scanning, fully unrolled: per limb of b one
+// multiply-accumulate row then one reduction row, the running value kept in
+// five words (it stays below 2p < 2^255 between rows).
+inline F fmul(const F& A, const F& B) {
+  const uint64_t* a = A.w;
+  uint64_t t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, c, m;
+  u128 s;
   for (int i = 0; i < 4; ++i) {
-    uint64_t carry = 0;
-    for (int j = 0; j < 4; ++j) {
-      u128 s = (u128)a.w[i] * b.w[j] + t[i + j] + carry;
-      t[i + j] = (uint64_t)s;
-      carry = (uint64_t)(s >> 64);
-    }
-    t[i + 4] = carry;
+    const uint64_t bi = B.w[i];
+    s = (u128)a[0] * bi + t0;
+    t0 = (uint64_t)s;
+    c = (uint64_t)(s >> 64);
+    s = (u128)a[1] * bi + t1 + c;
+    t1 = (uint64_t)s;
+    c = (uint64_t)(s >> 64);
+    s = (u128)a[2] * bi + t2 + c;
+    t2 = (uint64_t)s;
+    c = (uint64_t)(s >> 64);
+    s = (u128)a[3] * bi + t3 + c;
+    t3 = (uint64_t)s;
+    t4 += (uint64_t)(s >> 64);
+    m = t0 * kPInv;
+    s = (u128)m * kP[0] + t0;
+    c = (uint64_t)(s >> 64);
+    s = (u128)m * kP[1] + t1 + c;
+    t0 = (uint64_t)s;
+    c = (uint64_t)(s >> 64);
+    s = (u128)m * kP[2] + t2 + c;
+    t1 = (uint64_t)s;
+    c = (uint64_t)(s >> 64);
+    s = (u128)m * kP[3] + t3 + c;
+    t2 = (uint64_t)s;
+    c = (uint64_t)(s >> 64);
+    t3 = t4 + c;
+    t4 = 0;
   }
-  for (int i = 0; i < 4; ++i) {
-    uint64_t m = t[i] * kPInv;
-    uint64_t carry = 0;
-    for (int j = 0; j < 4; ++j) {
-      u128 s = (u128)m * kP[j] + t[i + j] + carry;
-      t[i + j] = (uint64_t)s;
-      carry = (uint64_t)(s >> 64);
-    }
-    for (int k = i + 4; carry && k < 9; ++k) {
-      u128 s = (u128)t[k] + carry;
-      t[k] = (uint64_t)s;
-      carry = (uint64_t)(s >> 64);
-    }
-  }
-  F r{{t[4], t[5], t[6], t[7]}};
+  F r{{t0, t1, t2, t3}};
   cond_sub_p(r.w);
   return r;
 }
