@@ -309,9 +309,12 @@ static void release_lane(Ctx& c) {
   c.lane.reset();
 }
 
-// k commits of one size over the resident SRS, alternating between the
-// context's two lanes. Columns come from device pointers or, when `host` is
-// set, from host memory copied on the lane that commits them.
+// k commits of one size over the resident SRS. Columns go in groups (one
+// sort, accumulation and bucket reduction per group) that alternate between
+// the context's two lanes, so one group's latency-bound reduction (and the
+// next group's copies) overlap another's bucket accumulation. Columns come
+// from device pointers or, when `host` is set, from host memory copied on the
+// lane that commits them.
 static int commit_batch_lanes(Ctx& c, const void* const* cols, bool host, size_t k, size_t num_vars, uint8_t* out) {
   if (!cols || !out) return APG_ERR_INVALID_ARGUMENT;
   if (!mercury_num_vars_ok(num_vars)) return APG_ERR_UNSUPPORTED_NUM_VARS;
@@ -328,16 +331,21 @@ static int commit_batch_lanes(Ctx& c, const void* const* cols, bool host, size_t
   APG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   APG_CUDA(cudaEventRecord(ev, c.stream));
   APG_CUDA(cudaStreamWaitEvent(L.stream, ev, 0));
-  for (size_t j = 0; j < k; ++j) {
-    Ctx& X = *lanes[j & 1];
+  const size_t group = std::max<size_t>(1, (k + 3) / 4);
+  std::vector<const void*> ptrs(cols, cols + k);
+  std::vector<size_t> lens(k, n);
+  for (size_t j0 = 0, gi = 0; j0 < k; j0 += group, ++gi) {
+    Ctx& X = *lanes[gi & 1];
+    const size_t m = std::min(group, k - j0);
     const SrsTable* t = commit_table(X, n);
-    const void* src = cols[j];
     if (host) {
-      void* buf = X.scratch[S_SCALARS].get(32 * n);
-      APG_CUDA(cudaMemcpyAsync(buf, cols[j], 32 * n, cudaMemcpyHostToDevice, X.stream));
-      src = buf;
+      uint8_t* buf = X.scratch[S_SCALARS].as<uint8_t>(32 * n * group);
+      for (size_t j = 0; j < m; ++j) {
+        APG_CUDA(cudaMemcpyAsync(buf + 32 * n * j, cols[j0 + j], 32 * n, cudaMemcpyHostToDevice, X.stream));
+        ptrs[j0 + j] = buf + 32 * n * j;
+      }
     }
-    msm_device(X, nullptr, t, src, false, false, n, d_out + 64 * j, nullptr);
+    msm_multi(X, nullptr, t, ptrs.data() + j0, lens.data() + j0, m, false, false, d_out + 64 * j0);
   }
   APG_CUDA(cudaEventRecord(ev, L.stream));
   APG_CUDA(cudaStreamWaitEvent(c.stream, ev, 0));

@@ -197,6 +197,11 @@ struct MsmPlan {
 MsmPlan msm_plan(size_t n, bool small_scalars, const SrsTable* table);
 void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* scalars, bool small_scalars,
                 bool scalars_canonical, size_t n, uint8_t* out64_device, uint8_t* host_out);
+// k MSMs over the same bases (lens[j] scalars each, device pointers); result
+// j is written to d_out + 64 * j. Columns are processed in groups that share
+// one sort, one accumulation and one bucket reduction.
+void msm_multi(Ctx& c, const Affine* bases, const SrsTable* table, const void* const* scalars, const size_t* lens,
+               size_t k, bool small_scalars, bool scalars_canonical, uint8_t* d_out);
 const SrsTable* srs_table(Ctx& c, int cbits, size_t need);
 double probe_fq_mul_rate(Ctx& c, double target_ms);
 

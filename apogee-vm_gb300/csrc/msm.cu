@@ -1,20 +1,27 @@
 // Pippenger MSM on sm_103a (replaces crates/curve/src/msm.rs:48-311).
 //
-// Pipeline, all on the context's stream:
-//  1. k_recode      one thread per scalar: Montgomery -> canonical, signed
+// Pipeline for a group of columns over the same bases, all on the context's
+// stream (msm_group):
+//  1. k_digits      one thread per scalar: Montgomery -> canonical, signed
 //                   c-bit digits in [-2^(c-1), 2^(c-1)] (the reference's
-//                   recoding rule, msm.rs:180-198), one packed entry per
-//                   nonzero digit and a histogram of bucket occupancy.
-//  2. scan+scatter  a counting sort of the entries by bucket.
-//  3. k_accumulate  load-balanced bucket accumulation: every thread owns a
-//                   fixed-length segment of the sorted list and folds each run
-//                   of equal buckets into an XYZZ accumulator with mixed adds;
-//                   runs cut by a segment edge are stitched by k_fixup.
-//  4. k_level/k_sum bucket reduction sum_k k*B_k as a tree of running sums.
-//  5. k_finish      combine windows (Horner) or, with a precomputed SRS window
-//                   table, nothing: there every window shares one bucket set
-//                   because the table already holds 2^(c*w) * P_i.
-//  6. normalise to the canonical affine encoding.
+//                   recoding rule, msm.rs:180-198) and a histogram of bucket
+//                   occupancy with warp-aggregated atomics.
+//  2. scan          exclusive scan of the histogram (bucket starts).
+//  3. k_digits      the same digits again, each placed as a 4-byte reference
+//                   at its bucket's cursor: a counting sort without an
+//                   intermediate entry list.
+//  4. k_bucket_acc  persistent, load-balanced bucket accumulation: one wave of
+//                   threads, each folding an equal slice of the sorted list
+//                   run by run into XYZZ accumulators with mixed adds; runs cut
+//                   by a slice edge are stitched by k_fold_edges.
+//  5. k_level/k_sum bucket reduction sum_k k*B_k as a tree of running sums,
+//                   every column's bucket range at once.
+//  6. k_finish_cols per column, combine windows (Horner) or, with a
+//                   precomputed SRS window table, nothing: there every window
+//                   shares one bucket set because the table already holds
+//                   2^(c*w) * P_i; then the canonical affine encoding.
+// The allocation-free variant at the end of this file keeps the first
+// single-MSM form of the pipeline (k_recode, k_scatter, k_accumulate, k_finish).
 #include "common.cuh"
 
 namespace apg {
@@ -461,6 +468,197 @@ __global__ void k_finish(const Xyzz* tsum, int levels, int spaces, int fan_log, 
   }
 }
 
+// ---- the grouped pipeline -----------------------------------------------------
+//
+// A group is up to kMaxCols scalar columns against one set of bases (an SRS
+// window table or generic bases). Bucket keys are (col * spaces + space) * K +
+// |d| - 1, with spaces = 1 over a window table and one space per window
+// otherwise, so every column owns a key range and one counting sort, one
+// accumulation and one bucket reduction serve the whole group: the
+// latency-bound reduction is paid once per group instead of once per column.
+// The sorted list holds 4-byte references (bit 31 negate, bits 30..0 base
+// index); after the scatter the cursor array holds every bucket's end, which
+// is all the accumulation needs to find its runs.
+
+constexpr int kMaxCols = 32;
+
+struct MsmCols {
+  const void* s[kMaxCols];
+  uint32_t len[kMaxCols];
+};
+
+// Digits of one scalar, counted (SCATTER = false) or placed (SCATTER = true).
+// Lanes of a warp that hit the same bucket share one atomic: the leader adds
+// the group's size and hands each peer its rank, so a bucket that a large
+// share of the scalars hit (digit 1 from {0,1} columns and from the carries of
+// 32-bit values) costs one atomic per warp, not one per scalar.
+template <bool SMALL, bool SCATTER>
+__global__ void __launch_bounds__(256) k_digits(MsmCols cols, int c, int windows, int precomp, uint32_t tab_n,
+                                                int canonical_in, uint32_t* cursor, uint32_t* sorted,
+                                                uint32_t* flags) {
+  const uint32_t col = blockIdx.y;
+  const uint32_t n = cols.len[col];
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31u;
+  if (i - lane >= n) return;  // the whole warp lies past the column's end
+  const bool live = i < n;
+  uint32_t limbs[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) limbs[k] = 0;
+  if (live) {
+    if (SMALL) {
+      limbs[0] = reinterpret_cast<const uint32_t*>(cols.s[col])[i];
+    } else {
+      Fr s = ld_fe(reinterpret_cast<const Fr*>(cols.s[col]) + i);
+      if (!SCATTER && !fe_lt_mod<FrConsts>(s.v)) raise_flag(flags, DEV_NONCANONICAL);
+      if (!canonical_in) s = fe_from_mont(s);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) limbs[k] = s.v[k];
+    }
+  }
+  const uint32_t K = 1u << (c - 1);
+  const uint32_t mask = (1u << c) - 1;
+  const uint32_t spaces = precomp ? 1u : (uint32_t)windows;
+  const uint32_t key0 = col * spaces * K;
+  uint32_t carry = 0;
+  for (int w = 0; w < windows; ++w) {
+    const int off = w * c;
+    uint32_t raw = 0;
+    if (off < 256) {
+      const int limb = off >> 5, sh = off & 31;
+      uint64_t v = limbs[limb] >> sh;
+      if (limb + 1 < 8) v |= (uint64_t)limbs[limb + 1] << (32 - sh);
+      raw = (uint32_t)v & mask;
+    }
+    const uint32_t coef = raw + carry;
+    uint32_t mag, neg = 0;
+    if (w == windows - 1 || coef < K) {
+      mag = coef;
+      carry = 0;
+    } else {
+      mag = (1u << c) - coef;  // digit coef - 2^c < 0
+      neg = 1;
+      carry = 1;
+    }
+    if (!live) mag = 0;
+    if (mag > K) {  // unreachable for values below r; never index past the bucket range
+      if (!SCATTER) raise_flag(flags, DEV_NONCANONICAL);
+      mag = 0;
+    }
+    const unsigned active = __ballot_sync(0xffffffffu, mag != 0);
+    if (mag) {
+      const uint32_t key = key0 + (precomp ? 0u : (uint32_t)w * K) + mag - 1;
+      const unsigned peers = __match_any_sync(active, key);
+      const int leader = __ffs(peers) - 1;
+      if (SCATTER) {
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(&cursor[key], (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        const uint32_t idx = precomp ? (uint32_t)w * tab_n + i : i;
+        sorted[base + (uint32_t)__popc(peers & ((1u << lane) - 1u))] = (neg << 31) | idx;
+      } else if ((int)lane == leader) {
+        atomicAdd(&cursor[key], (uint32_t)__popc(peers));
+      }
+    }
+  }
+}
+
+// Persistent bucket accumulation: the grid is one wave of resident threads
+// and thread s folds the s-th of nseg equal slices of the sorted list, so the
+// work is balanced however the digits are distributed. Runs are found from
+// the bucket ends; a run cut by a slice edge leaves as an item for
+// k_fold_edges exactly as in k_accumulate.
+__global__ void __launch_bounds__(128) k_bucket_acc(const uint32_t* sorted, const uint32_t* ends, uint32_t nbins,
+                                                    const uint32_t* total, size_t nseg, const Affine* bases,
+                                                    Xyzz* buckets, uint32_t* okeys, Xyzz* opts, uint8_t* opres) {
+  const size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const size_t E = *total;
+  const size_t seg = (E + nseg - 1) / nseg;
+  const size_t lo = s * seg;
+  if (lo >= E) {
+    put_item(okeys, opts, opres, 2 * s, kNoKey, nullptr);
+    put_item(okeys, opts, opres, 2 * s + 1, kNoKey, nullptr);
+    return;
+  }
+  const size_t hi = min(lo + seg, E);
+  // The bucket holding position lo: the first key whose end lies past it.
+  uint32_t a = 0, b = nbins - 1;
+  while (a < b) {
+    const uint32_t m = (a + b) >> 1;
+    if (ends[m] > lo) b = m;
+    else a = m + 1;
+  }
+  uint32_t cur = a;
+  size_t run_end = ends[cur];
+  const bool starts_before = lo > (cur ? (size_t)ends[cur - 1] : 0);
+  const uint32_t first = cur;
+  bool first_run = true, head_written = false;
+  Xyzz acc = xyzz_inf();
+  for (size_t i = lo; i < hi; ++i) {
+    if (i == run_end) {
+      if (first_run && starts_before) {
+        put_item(okeys, opts, opres, 2 * s, cur, &acc);
+        head_written = true;
+      } else {
+        st_xyzz(&buckets[cur], acc);
+      }
+      first_run = false;
+      do {
+        run_end = ends[++cur];
+      } while (run_end <= i);
+      acc = xyzz_inf();
+    }
+    const uint32_t e = sorted[i];
+    Affine p = ld_affine(&bases[e & 0x7fffffffu]);
+    if (e >> 31) p.y = fe_neg(p.y);
+    if (!aff_is_inf(p)) acc = xyzz_add_affine(acc, p);
+  }
+  const bool continues = hi < run_end;
+  if (first_run && starts_before) {
+    put_item(okeys, opts, opres, 2 * s, cur, &acc);
+    head_written = true;
+    put_item(okeys, opts, opres, 2 * s + 1, cur, nullptr);
+  } else {
+    if (continues) {
+      put_item(okeys, opts, opres, 2 * s + 1, cur, &acc);
+    } else {
+      st_xyzz(&buckets[cur], acc);
+      put_item(okeys, opts, opres, 2 * s + 1, cur, nullptr);
+    }
+  }
+  if (!head_written) put_item(okeys, opts, opres, 2 * s, first, nullptr);
+}
+
+// One thread per column: Horner over the reduction levels (in `fan`) and the
+// column's spaces (windows, in 2^c), then the canonical affine bytes.
+__global__ void k_finish_cols(const Xyzz* tsum, int levels, int spaces_total, int spaces_per_col, int ncols,
+                              int fan_log, int c, uint32_t* out64) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncols) return;
+  Xyzz total = xyzz_inf();
+  for (int w = spaces_per_col - 1; w >= 0; --w) {
+    if (w != spaces_per_col - 1)
+      for (int j = 0; j < c; ++j) total = xyzz_dbl(total);
+    const int sp = col * spaces_per_col + w;
+    Xyzz s = xyzz_inf();
+    for (int l = levels - 1; l >= 0; --l) {
+      if (l != levels - 1)
+        for (int j = 0; j < fan_log; ++j) s = xyzz_dbl(s);
+      s = xyzz_add(s, ld_xyzz(&tsum[(size_t)l * spaces_total + sp]));
+    }
+    total = xyzz_add(total, s);
+  }
+  const Affine a = xyzz_to_affine(total);
+  const Fq x = fe_from_mont(a.x), y = fe_from_mont(a.y);
+  uint32_t* o = out64 + 16 * (size_t)col;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    o[k] = x.v[k];
+    o[8 + k] = y.v[k];
+  }
+}
+
 template <class T>
 inline unsigned blocks_for(size_t n, int threads) {
   return (unsigned)((n + threads - 1) / threads);
@@ -534,6 +732,8 @@ const SrsTable* srs_table(Ctx& c, int cbits, size_t need) {
   t.c = cbits;
   t.windows = window_count(254, cbits);
   t.n = n;
+  // Sorted references carry the table index in 31 bits.
+  if ((size_t)t.windows * n >= ((size_t)1 << 31)) throw Error(APG_ERR_OUT_OF_MEMORY, "SRS window table too large");
   APG_CUDA(cudaMalloc(&t.tab, (size_t)t.windows * n * sizeof(Affine)));
   launch(c, k_window_table, blocks_for<int>(n, 128), 128, 0, (const Affine*)c.srs, n, cbits, t.windows, t.tab);
   APG_CUDA(cudaStreamSynchronize(c.stream));
@@ -555,35 +755,42 @@ MsmPlan msm_plan(size_t n, bool small_scalars, const SrsTable* table) {
   return p;
 }
 
-void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* scalars, bool small_scalars,
-                bool scalars_canonical, size_t n, uint8_t* out64_device, uint8_t* host_out) {
-  if (n == 0) {
-    if (out64_device) APG_CUDA(cudaMemsetAsync(out64_device, 0, 64, c.stream));
-    if (host_out) memset(host_out, 0, 64);
-    return;
-  }
-  MsmPlan p = msm_plan(n, small_scalars, table);
-  const int K = 1 << (p.c - 1);
-  const int spaces = p.precomp ? 1 : p.windows;
-  const size_t nbins = (size_t)spaces * K;
-  const size_t E = (size_t)p.windows * n;
-  const Affine* src = p.precomp ? table->tab : bases;
-  const size_t tab_n = p.precomp ? table->n : 0;
+namespace {
 
-  uint64_t* entries = c.scratch[S_ENTRIES].as<uint64_t>(E);
-  uint64_t* sorted = c.scratch[S_SORTED].as<uint64_t>(E);
+// Threads of k_bucket_acc resident on the whole device (one wave).
+size_t acc_resident_threads(Ctx& c) {
+  static std::once_flag once;
+  static int per_sm = 0;
+  std::call_once(once, [] {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bucket_acc, 128, 0) != cudaSuccess || per_sm < 1)
+      per_sm = 1;
+  });
+  return (size_t)c.sm_count * (size_t)per_sm * 128;
+}
+
+constexpr size_t kMaxBins = (size_t)(kScanBlock - 1) * kScanBlock * kScanItems;  // one pass of the 3-kernel scan
+constexpr size_t kMaxGroupEntries = (size_t)1 << 28;                           // 1 GiB of sorted references
+
+// One group: columns share the plan, the bases and one pass of every kernel.
+void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols& cols, int ncols, size_t nmax,
+               const MsmPlan& p, bool small_scalars, bool scalars_canonical, uint8_t* d_out) {
+  const uint32_t K = 1u << (p.c - 1);
+  const int spaces_per_col = p.precomp ? 1 : p.windows;
+  const int S = spaces_per_col * ncols;
+  const size_t nbins = (size_t)S * K;
+  size_t emax = 0;
+  for (int j = 0; j < ncols; ++j) emax += (size_t)p.windows * cols.len[j];
+  const Affine* src = p.precomp ? table->tab : bases;
+  const uint32_t tab_n = p.precomp ? (uint32_t)table->n : 0;
+
   uint32_t* counts = c.scratch[S_COUNTS].as<uint32_t>(nbins + 1);
   const size_t scan_blocks = (nbins + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems);
-  if (scan_blocks > (size_t)kScanBlock - 1) throw Error(APG_ERR_INVALID_ARGUMENT, "too many buckets");
   uint32_t* blk = c.scratch[S_SCANBLK].as<uint32_t>(kScanBlock + 1);
   uint32_t* total = c.scratch[S_OFFSETS].as<uint32_t>(1);
+  uint32_t* sorted = c.scratch[S_SORTED].as<uint32_t>(std::max<size_t>(emax, 1));
   Xyzz* buckets = c.scratch[S_BUCKETS].as<Xyzz>(nbins);
 
-  // Segments: enough threads to fill the chip several times over.
-  const size_t target_threads = (size_t)c.sm_count * 1024;
-  const int seg_len = (int)std::max<size_t>(4, std::min<size_t>(256, E / std::max<size_t>(target_threads, 1)));
-  const size_t nseg = (E + seg_len - 1) / seg_len;
-  // Edge-run item lists, ping-pong between two sets of (keys, points, present).
+  const size_t nseg = std::max<size_t>(1, std::min(acc_resident_threads(c), (emax + 15) / 16));
   constexpr int kFoldLen = 8;
   uint32_t* ikeys[2] = {c.scratch[S_HEAD].as<uint32_t>(2 * nseg), c.scratch[S_TAIL].as<uint32_t>(2 * nseg)};
   Xyzz* ipts[2] = {c.scratch[S_TMP0].as<Xyzz>(2 * nseg), c.scratch[S_TMP1].as<Xyzz>(2 * nseg)};
@@ -592,33 +799,39 @@ void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* 
   int fan_log = 0;
   while ((1 << fan_log) < kLevelFan) ++fan_log;
   int levels = 0;
-  for (int M = K;; M = (M + kLevelFan - 1) / kLevelFan) {
+  for (int M = (int)K;; M = (M + kLevelFan - 1) / kLevelFan) {
     ++levels;
     if (M <= kLevelFan) break;
   }
-  Xyzz* tsum = c.scratch[S_TSUM].as<Xyzz>((size_t)levels * spaces);
-  const int G0 = (K + kLevelFan - 1) / kLevelFan;
-  Xyzz* outT = c.scratch[S_LEVEL_T].as<Xyzz>((size_t)spaces * G0);
-  Xyzz* lvlA = c.scratch[S_LEVEL_A].as<Xyzz>((size_t)spaces * G0);
-  Xyzz* lvlB = c.scratch[S_LEVEL_B].as<Xyzz>((size_t)spaces * G0);
-  uint32_t* res = c.scratch[S_RESULT].as<uint32_t>(16);
+  Xyzz* tsum = c.scratch[S_TSUM].as<Xyzz>((size_t)levels * S);
+  const int G0 = ((int)K + kLevelFan - 1) / kLevelFan;
+  Xyzz* outT = c.scratch[S_LEVEL_T].as<Xyzz>((size_t)S * G0);
+  Xyzz* lvlA = c.scratch[S_LEVEL_A].as<Xyzz>((size_t)S * G0);
+  Xyzz* lvlB = c.scratch[S_LEVEL_B].as<Xyzz>((size_t)S * G0);
 
   cudaEvent_t t_total = c.timer_begin();
   APG_CUDA(cudaMemsetAsync(counts, 0, (nbins + 1) * sizeof(uint32_t), c.stream));
   APG_CUDA(cudaMemsetAsync(buckets, 0, nbins * sizeof(Xyzz), c.stream));
+  const dim3 dgrid(blocks_for<int>(std::max<size_t>(nmax, 1), 256), (unsigned)ncols);
+  const int canon = scalars_canonical ? 1 : 0;
   if (small_scalars)
-    launch(c, k_recode<true>, blocks_for<int>(n, 256), 256, 0, scalars, n, p.c, p.windows, (int)p.precomp, tab_n,
-           1, entries, counts, c.d_flags);
+    launch(c, k_digits<true, false>, dgrid, 256, 0, cols, p.c, p.windows, (int)p.precomp, tab_n, canon, counts,
+           (uint32_t*)nullptr, c.d_flags);
   else
-    launch(c, k_recode<false>, blocks_for<int>(n, 256), 256, 0, scalars, n, p.c, p.windows, (int)p.precomp,
-           tab_n, scalars_canonical ? 1 : 0, entries, counts, c.d_flags);
+    launch(c, k_digits<false, false>, dgrid, 256, 0, cols, p.c, p.windows, (int)p.precomp, tab_n, canon, counts,
+           (uint32_t*)nullptr, c.d_flags);
   launch(c, k_scan_local, (unsigned)scan_blocks, kScanBlock, 0, counts, nbins, blk);
   launch(c, k_scan_blocks, 1, kScanBlock, 0, blk, (int)scan_blocks);
   launch(c, k_scan_add, blocks_for<int>(nbins, 256), 256, 0, counts, nbins, (const uint32_t*)blk, total);
-  launch(c, k_scatter, blocks_for<int>(E, 256), 256, 0, (const uint64_t*)entries, E, counts, sorted);
+  if (small_scalars)
+    launch(c, k_digits<true, true>, dgrid, 256, 0, cols, p.c, p.windows, (int)p.precomp, tab_n, canon, counts, sorted,
+           c.d_flags);
+  else
+    launch(c, k_digits<false, true>, dgrid, 256, 0, cols, p.c, p.windows, (int)p.precomp, tab_n, canon, counts,
+           sorted, c.d_flags);
   cudaEvent_t t_acc = c.timer_begin();
-  launch(c, k_accumulate, blocks_for<int>(nseg, 128), 128, 0, (const uint64_t*)sorted, (const uint32_t*)total,
-         seg_len, nseg, src, buckets, ikeys[0], ipts[0], ipres[0]);
+  launch(c, k_bucket_acc, blocks_for<int>(nseg, 128), 128, 0, (const uint32_t*)sorted, (const uint32_t*)counts,
+         (uint32_t)nbins, (const uint32_t*)total, nseg, src, buckets, ikeys[0], ipts[0], ipres[0]);
   c.timer_end(APG_TIMER_MSM_ACCUMULATE, t_acc);
   {
     size_t len = 2 * nseg;
@@ -632,31 +845,77 @@ void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* 
       len = 2 * fseg;
     }
   }
-
   const Xyzz* lvl_in = buckets;
-  int M = K;
+  int M = (int)K;
   for (int l = 0; l < levels; ++l) {
-    int G = (M + kLevelFan - 1) / kLevelFan;
+    const int G = (M + kLevelFan - 1) / kLevelFan;
     Xyzz* outR = (l & 1) ? lvlB : lvlA;
-    launch(c, k_level, blocks_for<int>((size_t)spaces * G, 64), 64, 0, lvl_in, M, spaces, kLevelFan, outT, outR);
+    launch(c, k_level, blocks_for<int>((size_t)S * G, 64), 64, 0, lvl_in, M, S, kLevelFan, outT, outR);
     if (G > 256) {
       // Wide levels: a two-stage tree keeps the serial chain short.
       const int nblk = (G + 255) / 256;
-      Xyzz* part = c.scratch[S_TMP3].as<Xyzz>((size_t)spaces * nblk);
-      launch(c, k_sum_blocks, dim3(nblk, spaces), 128, 0, (const Xyzz*)outT, G, part);
-      launch(c, k_sum, spaces, 128, 0, (const Xyzz*)part, nblk, tsum + (size_t)l * spaces);
+      Xyzz* part = c.scratch[S_TMP3].as<Xyzz>((size_t)S * nblk);
+      launch(c, k_sum_blocks, dim3(nblk, S), 128, 0, (const Xyzz*)outT, G, part);
+      launch(c, k_sum, S, 128, 0, (const Xyzz*)part, nblk, tsum + (size_t)l * S);
     } else {
-      launch(c, k_sum, spaces, 128, 0, (const Xyzz*)outT, G, tsum + (size_t)l * spaces);
+      launch(c, k_sum, S, 128, 0, (const Xyzz*)outT, G, tsum + (size_t)l * S);
     }
     lvl_in = outR;
     M = G;
   }
-  launch(c, k_finish, 1, 32, 0, (const Xyzz*)tsum, levels, spaces, fan_log, p.c,
-         out64_device ? (uint32_t*)out64_device : res);
+  launch(c, k_finish_cols, blocks_for<int>(ncols, 32), 32, 0, (const Xyzz*)tsum, levels, S, spaces_per_col, ncols,
+         fan_log, p.c, (uint32_t*)d_out);
   c.timer_end(APG_TIMER_MSM_TOTAL, t_total);
+}
+
+}  // namespace
+
+void msm_multi(Ctx& c, const Affine* bases, const SrsTable* table, const void* const* scalars, const size_t* lens,
+               size_t k, bool small_scalars, bool scalars_canonical, uint8_t* d_out) {
+  size_t j = 0;
+  while (j < k) {
+    // Grow the group while the plan, the bucket range and the sorted list fit.
+    size_t nmax = 0, emax = 0;
+    MsmPlan p{};
+    size_t g = 0;
+    while (j + g < k && g < (size_t)kMaxCols) {
+      const size_t n = lens[j + g];
+      if (n >= ((size_t)1 << 31)) throw Error(APG_ERR_INVALID_ARGUMENT, "MSM longer than 2^31 - 1 points");
+      const size_t nm = std::max(nmax, n);
+      const MsmPlan q = msm_plan(std::max<size_t>(nm, 1), small_scalars, table);
+      const size_t spaces = q.precomp ? 1 : (size_t)q.windows;
+      const size_t bins = (g + 1) * spaces * ((size_t)1 << (q.c - 1));
+      size_t e = 0;
+      for (size_t t = 0; t <= g; ++t) e += (size_t)q.windows * lens[j + t];
+      if (g > 0 && (bins > kMaxBins || e > kMaxGroupEntries || q.c != p.c || q.windows != p.windows)) break;
+      if (bins > kMaxBins) throw Error(APG_ERR_INVALID_ARGUMENT, "too many buckets");
+      p = q;
+      nmax = nm;
+      emax = e;
+      ++g;
+    }
+    (void)emax;
+    MsmCols cols{};
+    for (size_t t = 0; t < g; ++t) {
+      cols.s[t] = scalars[j + t];
+      cols.len[t] = (uint32_t)lens[j + t];
+    }
+    msm_group(c, bases, table, cols, (int)g, nmax, p, small_scalars, scalars_canonical, d_out + 64 * j);
+    j += g;
+  }
+}
+
+void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* scalars, bool small_scalars,
+                bool scalars_canonical, size_t n, uint8_t* out64_device, uint8_t* host_out) {
+  if (n == 0) {
+    if (out64_device) APG_CUDA(cudaMemsetAsync(out64_device, 0, 64, c.stream));
+    if (host_out) memset(host_out, 0, 64);
+    return;
+  }
+  uint8_t* d_out = out64_device ? out64_device : c.scratch[S_RESULT].as<uint8_t>(64);
+  msm_multi(c, bases, table, &scalars, &n, 1, small_scalars, scalars_canonical, d_out);
   if (host_out) {
-    APG_CUDA(cudaMemcpyAsync(host_out, out64_device ? (void*)out64_device : (void*)res, 64, cudaMemcpyDeviceToHost,
-                             c.stream));
+    APG_CUDA(cudaMemcpyAsync(host_out, d_out, 64, cudaMemcpyDeviceToHost, c.stream));
     c.check_flags();
   }
 }

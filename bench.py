@@ -183,8 +183,9 @@ def run_reference(args):
 
 
 def run_msm_only(args):
-    """A lean case for profiling: warm-up and timed 2^log2n uniform-scalar SRS
-    MSMs and nothing else (no end-to-end leg, no CPU baseline)."""
+    """A lean case for profiling: warm-up and timed 2^log2n SRS MSMs over
+    uniform or mixed scalars and nothing else (no end-to-end leg, no CPU
+    baseline)."""
     import numpy as np
     import torch
 
@@ -199,7 +200,8 @@ def run_msm_only(args):
     ctx.srs_prepare()
     cols = []
     for j in range(args.cols):
-        t = torch.from_numpy(synth.uniform_column(n, SEED + j).view(np.int32).reshape(-1)).to(f"cuda:{local}")
+        gen = synth.mixed_column if args.scalars == "mixed" else synth.uniform_column
+        t = torch.from_numpy(gen(n, SEED + j).view(np.int32).reshape(-1)).to(f"cuda:{local}")
         ctx.fr_to_mont_device(t.data_ptr(), n)
         cols.append(t)
     ptrs = [t.data_ptr() for t in cols]
@@ -211,7 +213,8 @@ def run_msm_only(args):
         ctx.commit_batch_device(ptrs, args.log2n)
     torch.cuda.synchronize()
     dt = (time.perf_counter() - t0) / args.steps
-    print(json.dumps({"msm_only": True, "log2n": args.log2n, "cols": args.cols, "ms_per_step": dt * 1e3,
+    print(json.dumps({"msm_only": True, "scalars": args.scalars, "log2n": args.log2n, "cols": args.cols,
+                      "ms_per_step": dt * 1e3,
                       "points_per_s": args.cols * n / dt}), flush=True)
     ctx.close()
     return 0
@@ -534,7 +537,8 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--log2n", type=int, default=22)
     ap.add_argument("--cols", type=int, default=16)
-    ap.add_argument("--only-msm", action="store_true", help="lean uniform-scalar MSM case for profiling")
+    ap.add_argument("--only-msm", action="store_true", help="lean SRS MSM case for profiling")
+    ap.add_argument("--scalars", choices=["uniform", "mixed"], default="uniform", help="scalars of --only-msm")
     ap.add_argument("--no-shards", dest="shards", action="store_false",
                     help="skip the per-config shard timings and the 207-shard mix / serving run")
     ap.add_argument("--profile-case", choices=["zerocheck", "gkr", "open"], default=None,

@@ -199,3 +199,63 @@ def test_commit_large_known_tau(ctx):
     for c in reversed(coeffs):
         acc = (acc * tau + c) % O.P_R
     assert cm == O.g1_mul(O.G1_GEN, acc)
+
+
+def _f_tau(coeffs, tau):
+    acc = 0
+    for c in reversed(coeffs):
+        acc = (acc * tau + c) % O.P_R
+    return acc
+
+
+def _column(kind, n, rng):
+    import synth
+
+    if kind == "zeros":
+        return [0] * n
+    if kind == "ones":
+        return [1] * n
+    if kind == "bits":
+        return [rng.getrandbits(1) for _ in range(n)]
+    if kind == "u32":
+        return [rng.getrandbits(32) for _ in range(n)]
+    if kind == "identical":
+        return [rng.randrange(O.P_R)] * n
+    if kind == "mixed":
+        return synth.to_ints(synth.mixed_column(n, rng.getrandbits(32)))
+    return [rng.randrange(O.P_R) for _ in range(n)]
+
+
+@pytest.mark.parametrize("nv", [12, 16])
+def test_commit_batch_groups_known_tau(ctx, nv):
+    """Columns of every digit shape committed together share one sort,
+    accumulation and bucket reduction per group (nine columns: three groups
+    over both lanes); each commitment must equal [f(tau)]G, and the host and
+    device batch entry points must agree with single commits."""
+    import apogee_gpu as A
+
+    tau = 0xBA7C4 + nv
+    n = 1 << nv
+    ctx.srs_generate(tau, n)
+    rng = random.Random(nv)
+    kinds = ["zeros", "ones", "bits", "u32", "identical", "mixed", "uniform", "mixed", "ones"]
+    cols = [_column(k, n, rng) for k in kinds]
+    blobs = [A.to_mont_bytes(c) for c in cols]
+    cms = ctx.commit_batch(blobs, nv)
+    for kind, c, cm in zip(kinds, cols, cms):
+        assert cm == O.g1_mul(O.G1_GEN, _f_tau(c, tau)), kind
+    assert [ctx.commit(b, nv) for b in blobs[:3]] == cms[:3]
+
+
+def test_commit_batch_many_small_columns(ctx):
+    """130 columns of 4 values: groups of 33 split at the 32-column limit."""
+    import apogee_gpu as A
+
+    tau = 0x77
+    nv = 2
+    ctx.srs_generate(tau, 1 << nv)
+    rng = random.Random(130)
+    cols = [_column(["uniform", "u32", "bits", "zeros"][j % 4], 4, rng) for j in range(130)]
+    cms = ctx.commit_batch([A.to_mont_bytes(c) for c in cols], nv)
+    for c, cm in zip(cols, cms):
+        assert cm == O.g1_mul(O.G1_GEN, _f_tau(c, tau))
