@@ -37,15 +37,7 @@ int guarded(apg_ctx* ctx, F&& f) {
 // Mercury's instance rule (crates/pcs-verify/src/lib.rs:97-102).
 bool mercury_num_vars_ok(size_t nv) { return nv >= 2 && nv <= 54 && nv % 2 == 0; }
 
-// The table a commit of n points reads: a narrow-window one for small
-// instances (cheap bucket reduction), the wide one otherwise.
-const SrsTable* commit_table(Ctx& c, size_t n) {
-  if (n <= ((size_t)1 << 14)) {
-    const SrsTable* t = srs_table(c, 8, n);
-    if (t) return t;
-  }
-  return srs_table(c, 16, n);
-}
+const SrsTable* commit_table(Ctx& c, size_t n) { return srs_table_for(c, n); }
 
 int commit_common(Ctx& c, const void* evals, bool on_device, bool small, size_t num_vars, uint8_t* out) {
   if (!out || (!evals && num_vars > 0)) return APG_ERR_INVALID_ARGUMENT;
@@ -240,7 +232,8 @@ int apg_srs_prepare(apg_ctx* ctx, int cbits) {
     if (!c.srs) return (int)APG_ERR_NO_SRS;
     if (cbits == 0) {
       srs_table(c, 8, std::min(c.srs_n, (size_t)1 << 14));
-      srs_table(c, 16, c.srs_n);
+      if (c.srs_n > ((size_t)1 << 14)) srs_table(c, 16, c.srs_n);
+      if (c.srs_n >= kWideTableMin) srs_table(c, 20, c.srs_n);
     } else {
       if (cbits < 2 || cbits > 20) return (int)APG_ERR_INVALID_ARGUMENT;
       srs_table(c, cbits, c.srs_n);

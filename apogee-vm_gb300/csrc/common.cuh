@@ -203,6 +203,12 @@ void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* 
 void msm_multi(Ctx& c, const Affine* bases, const SrsTable* table, const void* const* scalars, const size_t* lens,
                size_t k, bool small_scalars, bool scalars_canonical, uint8_t* d_out);
 const SrsTable* srs_table(Ctx& c, int cbits, size_t need);
+// The table an MSM of the first n SRS powers reads: 8-bit windows up to 2^14
+// points (a cheap bucket reduction), 16-bit windows below kWideTableMin and
+// 20-bit windows from there (13 windows instead of 16; the 2^19 buckets a
+// column are amortised over at least 2^20 points). Null if the SRS is short.
+constexpr size_t kWideTableMin = (size_t)1 << 20;
+const SrsTable* srs_table_for(Ctx& c, size_t n);
 double probe_fq_mul_rate(Ctx& c, double target_ms);
 
 }  // namespace apg

@@ -212,9 +212,7 @@ void srs_commit(Ctx& c, const Fr* d, size_t len, uint8_t out[64]) {
     memset(out, 0, 64);
     return;
   }
-  const SrsTable* t = nullptr;
-  if (len <= ((size_t)1 << 14)) t = srs_table(c, 8, len);
-  if (!t) t = srs_table(c, 16, len);
+  const SrsTable* t = srs_table_for(c, len);
   if (!t) throw Error(APG_ERR_SRS_TOO_SMALL, "the SRS holds fewer powers than the polynomial has coefficients");
   msm_device(c, nullptr, t, d, false, false, len, nullptr, out);
 }

@@ -741,6 +741,18 @@ const SrsTable* srs_table(Ctx& c, int cbits, size_t need) {
   return &c.tables.back();
 }
 
+const SrsTable* srs_table_for(Ctx& c, size_t n) {
+  if (n <= ((size_t)1 << 14)) {
+    const SrsTable* t = srs_table(c, 8, n);
+    if (t) return t;
+  }
+  if (n >= kWideTableMin) {
+    const SrsTable* t = srs_table(c, 20, n);
+    if (t) return t;
+  }
+  return srs_table(c, 16, n);
+}
+
 MsmPlan msm_plan(size_t n, bool small_scalars, const SrsTable* table) {
   MsmPlan p;
   if (table) {

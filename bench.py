@@ -60,6 +60,13 @@ def algorithmic_imad_accumulate(n):
     return n * windows * 10 * 264
 
 
+def own_windows(n):
+    """Signed-digit windows of the SRS window table an n-point commit reads
+    (8-bit up to 2^14 points, 16-bit below 2^20, 20-bit from 2^20)."""
+    c = 8 if n <= 1 << 14 else (16 if n < 1 << 20 else 20)
+    return -(-255 // c)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during a timed region."""
 
@@ -479,6 +486,7 @@ def run_gpu(args):
     peak_imad = fq_rate * 264
     algo = algorithmic_imad_accumulate(n)
     achieved = algo / (acc_ms / acc_n / 1e3)
+    own = n * own_windows(n) * 10 * 264
     traffic = load_traffic().get("msm_accumulate_2p22", {}).get("dram_bytes_per_launch")
     roofline = {
         "bound": "int", "kernel": "k_accumulate (bucket accumulation, 2^22 uniform scalars)",
@@ -486,6 +494,9 @@ def run_gpu(args):
         "traffic": traffic, "peak_source": "measured on this device: dependency-free Fq Montgomery products x 264",
         "kernel_ms": acc_ms / acc_n, "msm_ms": tot_ms / tot_n,
         "msm_uniform_points_per_s": n / (tot_ms / tot_n / 1e3), "algorithmic_imad_per_launch": algo,
+        "algorithmic_basis": f"reference work: {reference_window_windows(n)[1]} windows x n mixed adds",
+        "own_imad_per_launch": own, "own_windows": own_windows(n),
+        "own_frac": own / (acc_ms / acc_n / 1e3) / peak_imad,
     }
 
     shards = None

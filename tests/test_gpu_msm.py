@@ -226,12 +226,12 @@ def _column(kind, n, rng):
     return [rng.randrange(O.P_R) for _ in range(n)]
 
 
-@pytest.mark.parametrize("nv", [12, 16])
+@pytest.mark.parametrize("nv", [12, 16, 20])
 def test_commit_batch_groups_known_tau(ctx, nv):
     """Columns of every digit shape committed together share one sort,
     accumulation and bucket reduction per group (nine columns: three groups
-    over both lanes); each commitment must equal [f(tau)]G, and the host and
-    device batch entry points must agree with single commits."""
+    over both lanes; at 2^20 the 20-bit window table); each commitment must
+    equal [f(tau)]G, and single commits must agree with the batch."""
     import apogee_gpu as A
 
     tau = 0xBA7C4 + nv
@@ -239,6 +239,8 @@ def test_commit_batch_groups_known_tau(ctx, nv):
     ctx.srs_generate(tau, n)
     rng = random.Random(nv)
     kinds = ["zeros", "ones", "bits", "u32", "identical", "mixed", "uniform", "mixed", "ones"]
+    if nv >= 20:
+        kinds = ["mixed", "uniform", "u32", "ones", "bits"]
     cols = [_column(k, n, rng) for k in kinds]
     blobs = [A.to_mont_bytes(c) for c in cols]
     cms = ctx.commit_batch(blobs, nv)
