@@ -20,15 +20,29 @@ struct Affine {
   Fq x, y;
 };
 
-// The curve formulas call one out-of-line Fq product: a point addition inlines
-// ten of them, and ten inlined copies of a 300-instruction multiply overflow
-// the instruction cache of a bucket-accumulation loop.
-#ifdef APG_INLINE_CURVE_MUL
-__device__ __forceinline__ Fq cmul(const Fq& a, const Fq& b) { return fe_mul(a, b); }
-#else
+// The curve formulas call out-of-line Fq products: a point addition inlines
+// ten of them, and ten inlined copies of a multiply overflow the instruction
+// cache of a bucket-accumulation loop. The paired forms compute two
+// independent products in one call, so their dependency chains interleave:
+// each formula is written as pairs of products that do not depend on each
+// other.
+struct Fq2 {
+  Fq a, b;
+};
 static __device__ __noinline__ Fq cmul(const Fq a, const Fq b) { return fe_mul(a, b); }
-#endif
-__device__ __forceinline__ Fq csqr(const Fq& a) { return cmul(a, a); }
+static __device__ __noinline__ Fq csqr(const Fq a) { return fe_sqr(a); }
+static __device__ __noinline__ Fq2 cmul2(const Fq a, const Fq b, const Fq c, const Fq d) {
+  Fq2 r;
+  r.a = fe_mul(a, b);
+  r.b = fe_mul(c, d);
+  return r;
+}
+static __device__ __noinline__ Fq2 csqr2(const Fq a, const Fq b) {
+  Fq2 r;
+  r.a = fe_sqr(a);
+  r.b = fe_sqr(b);
+  return r;
+}
 
 struct Xyzz {
   Fq x, y, zz, zzz;
@@ -90,50 +104,51 @@ __device__ __forceinline__ Xyzz xyzz_dbl(const Xyzz& p) {
   return r;
 }
 
-// madd-2008-s: acc + (x2, y2), the affine point assumed finite.
+// madd-2008-s: acc + (x2, y2), the affine point assumed finite. The 8M + 2S
+// go as four product pairs and one square pair.
 __device__ __forceinline__ Xyzz xyzz_add_affine(const Xyzz& p, const Affine& a) {
   if (xyzz_is_inf(p)) return xyzz_from_affine(a);
-  Fq u2 = cmul(a.x, p.zz);
-  Fq s2 = cmul(a.y, p.zzz);
-  Fq pp_ = fe_sub(u2, p.x);
-  Fq r = fe_sub(s2, p.y);
+  const Fq2 us = cmul2(a.x, p.zz, a.y, p.zzz);  // U2, S2
+  const Fq pp_ = fe_sub(us.a, p.x);
+  const Fq r = fe_sub(us.b, p.y);
   if (fe_is_zero(pp_)) {
     if (fe_is_zero(r)) return xyzz_dbl_affine(a);
     return xyzz_inf();
   }
-  Fq pp = csqr(pp_);
-  Fq ppp = cmul(pp_, pp);
-  Fq q = cmul(p.x, pp);
+  const Fq2 sq = csqr2(pp_, r);                    // PP, R^2
+  const Fq2 pq = cmul2(pp_, sq.a, p.x, sq.a);      // PPP, Q
+  const Fq2 zz = cmul2(p.zz, sq.a, p.zzz, pq.a);  // ZZ3, ZZZ3
   Xyzz o;
-  o.x = fe_sub(fe_sub(fe_sub(csqr(r), ppp), q), q);
-  o.y = fe_sub(cmul(r, fe_sub(q, o.x)), cmul(p.y, ppp));
-  o.zz = cmul(p.zz, pp);
-  o.zzz = cmul(p.zzz, ppp);
+  o.x = fe_sub(fe_sub(fe_sub(sq.b, pq.a), pq.b), pq.b);
+  const Fq2 yy = cmul2(r, fe_sub(pq.b, o.x), p.y, pq.a);
+  o.y = fe_sub(yy.a, yy.b);
+  o.zz = zz.a;
+  o.zzz = zz.b;
   return o;
 }
 
-// add-2008-s.
+// add-2008-s (12M + 2S as six product pairs and one square pair).
 __device__ __forceinline__ Xyzz xyzz_add(const Xyzz& p, const Xyzz& q) {
   if (xyzz_is_inf(p)) return q;
   if (xyzz_is_inf(q)) return p;
-  Fq u1 = cmul(p.x, q.zz);
-  Fq u2 = cmul(q.x, p.zz);
-  Fq s1 = cmul(p.y, q.zzz);
-  Fq s2 = cmul(q.y, p.zzz);
-  Fq pp_ = fe_sub(u2, u1);
-  Fq r = fe_sub(s2, s1);
+  const Fq2 u = cmul2(p.x, q.zz, q.x, p.zz);    // U1, U2
+  const Fq2 s = cmul2(p.y, q.zzz, q.y, p.zzz);  // S1, S2
+  const Fq pp_ = fe_sub(u.b, u.a);
+  const Fq r = fe_sub(s.b, s.a);
   if (fe_is_zero(pp_)) {
     if (fe_is_zero(r)) return xyzz_dbl(p);
     return xyzz_inf();
   }
-  Fq pp = csqr(pp_);
-  Fq ppp = cmul(pp_, pp);
-  Fq qq = cmul(u1, pp);
+  const Fq2 sq = csqr2(pp_, r);                        // PP, R^2
+  const Fq2 pq = cmul2(pp_, sq.a, u.a, sq.a);          // PPP, Q
+  const Fq2 zp = cmul2(p.zz, q.zz, p.zzz, q.zzz);      // ZZ1 ZZ2, ZZZ1 ZZZ2
+  const Fq2 zz = cmul2(zp.a, sq.a, zp.b, pq.a);        // ZZ3, ZZZ3
   Xyzz o;
-  o.x = fe_sub(fe_sub(fe_sub(csqr(r), ppp), qq), qq);
-  o.y = fe_sub(cmul(r, fe_sub(qq, o.x)), cmul(s1, ppp));
-  o.zz = cmul(cmul(p.zz, q.zz), pp);
-  o.zzz = cmul(cmul(p.zzz, q.zzz), ppp);
+  o.x = fe_sub(fe_sub(fe_sub(sq.b, pq.a), pq.b), pq.b);
+  const Fq2 yy = cmul2(r, fe_sub(pq.b, o.x), s.a, pq.a);
+  o.y = fe_sub(yy.a, yy.b);
+  o.zz = zz.a;
+  o.zzz = zz.b;
   return o;
 }
 
