@@ -217,6 +217,28 @@ void srs_commit(Ctx& c, const Fr* d, size_t len, uint8_t out[64]) {
   msm_device(c, nullptr, t, d, false, false, len, nullptr, out);
 }
 
+// Two independent SRS MSMs in one group (one sort, accumulation and bucket
+// reduction for both).
+void srs_commit2(Ctx& c, const Fr* d0, size_t len0, const Fr* d1, size_t len1, uint8_t out0[64],
+                 uint8_t out1[64]) {
+  if (len0 == 0 || len1 == 0) {
+    srs_commit(c, d0, len0, out0);
+    srs_commit(c, d1, len1, out1);
+    return;
+  }
+  const SrsTable* t = srs_table_for(c, std::max(len0, len1));
+  if (!t) throw Error(APG_ERR_SRS_TOO_SMALL, "the SRS holds fewer powers than the polynomial has coefficients");
+  const void* ptrs[2] = {d0, d1};
+  const size_t lens[2] = {len0, len1};
+  uint8_t* d_out = c.scratch[S_RESULT].as<uint8_t>(128);
+  msm_multi(c, nullptr, t, ptrs, lens, 2, false, false, d_out);
+  uint8_t both[128];
+  APG_CUDA(cudaMemcpyAsync(both, d_out, 128, cudaMemcpyDeviceToHost, c.stream));
+  c.check_flags();
+  memcpy(out0, both, 64);
+  memcpy(out1, both + 64, 64);
+}
+
 // acc_j = sum_{k >= j} x_k r^(k - j) for every position, in place or not.
 void suffix_horner(Ctx& c, const Fr* in, Fr* out, size_t stride, size_t count, size_t cols, const F& r,
                    int depth = 0) {
@@ -372,8 +394,7 @@ int mercury_open_impl(Ctx& c, const Fr* d_f, size_t nv, const uint8_t cm[64], co
   APG_CUDA(cudaMemcpyAsync(g, acc, 32 * b, cudaMemcpyDeviceToDevice, c.stream));
   const Fr* q = acc + b;
   const size_t nq = n - b;
-  srs_commit(c, q, nq, pts[1]);
-  srs_commit(c, g, b, pts[2]);
+  srs_commit2(c, q, nq, g, b, pts[1], pts[2]);
   tr.absorb_g1(T_PCS_OPENING, &pts[1][0], 2);
   F gamma = tr.challenge(T_MERCURY_GAMMA);
 
@@ -401,8 +422,7 @@ int mercury_open_impl(Ctx& c, const Fr* d_f, size_t nv, const uint8_t cm[64], co
     launch(c, k_sym_out, nb(b, 256), 256, 0, (const Fr*)TG, b, dv(fadd(h_alpha, fmul(gamma, v))), S, c.d_flags);
     launch(c, k_reverse, nb(b, 256), 256, 0, (const Fr*)g, b, D);
   }
-  srs_commit(c, S, b - 1, pts[3]);
-  srs_commit(c, D, b, pts[4]);
+  srs_commit2(c, S, b - 1, D, b, pts[3], pts[4]);
   tr.absorb_g1(T_PCS_OPENING, &pts[3][0], 2);
   F z;
   do {
