@@ -122,6 +122,7 @@ void apg_ctx_destroy(apg_ctx* ctx) {
       if (t.owned) cudaFree(t.tab);
     if (c.srs && c.srs_owned) cudaFree(c.srs);
     if (c.d_flags) cudaFree(c.d_flags);
+    if (c.pinned) cudaFreeHost(c.pinned);
     if (c.stream) cudaStreamDestroy(c.stream);
   }
   delete ctx;

@@ -80,7 +80,7 @@ struct SrsTable {
 enum ScratchSlot {
   S_ENTRIES, S_SORTED, S_COUNTS, S_OFFSETS, S_SCANBLK, S_BUCKETS, S_HEAD, S_TAIL, S_FLAGS, S_LEVEL_A,
   S_LEVEL_B, S_LEVEL_T, S_TSUM, S_RESULT, S_BASES, S_SCALARS, S_TMP0, S_TMP1, S_TMP2, S_TMP3, S_TMP4,
-  S_TMP5, S_TMP6, S_TMP7, S_COUNT
+  S_TMP5, S_TMP6, S_TMP7, S_ROUND, S_COUNT
 };
 
 // Per-kernel CUDA-event timers (ids are public: APG_TIMER_* in the header).
@@ -134,6 +134,14 @@ struct Ctx {
   // latency-bound tail (and the next column's copy) overlaps another's
   // bucket accumulation.
   std::unique_ptr<Ctx> lane;
+
+  // A small pinned host buffer for per-round device-to-host reads (a true
+  // asynchronous copy, no staging through pageable memory).
+  void* pinned = nullptr;
+  void* host_pinned() {
+    if (!pinned) APG_CUDA(cudaMallocHost(&pinned, 4096));
+    return pinned;
+  }
 
   // Bracket work on the stream with a timer's events (no-op unless enabled).
   cudaEvent_t timer_begin() {

@@ -31,6 +31,8 @@ struct RoundArgs {
   size_t npairs;
   int slots_step0;           // first step slot
   int n_val_slots;           // nd + nv
+  unsigned* done;            // blocks finished this round (zero between rounds)
+  Fr* out;                   // the round's 4 sums, written by the last block
 };
 
 __device__ __forceinline__ const Fr* table_in(const RoundArgs& A, int k) {
@@ -94,23 +96,36 @@ __global__ void __launch_bounds__(kRoundThreads) k_round(RoundArgs A, DevProgram
     if (threadIdx.x == 0) st_fe(&partials[(size_t)blockIdx.x * 4 + x], red[0]);
     __syncthreads();
   }
-}
-
-// Sum `nblocks` groups of 4 partials into out[0..4).
-__global__ void k_round_total(const Fr* partials, int nblocks, Fr* out) {
-  __shared__ Fr red[256];
+  // The last block to finish adds every block's partials (the partials are
+  // published before the ticket is taken) and re-arms the counter.
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(A.done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
   for (int x = 0; x < 4; ++x) {
     Fr a = fe_zero<FrConsts>();
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) a = fe_add(a, ld_fe(&partials[(size_t)b * 4 + x]));
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+      const uint4* q = reinterpret_cast<const uint4*>(&partials[(size_t)b * 4 + x]);
+      const uint4 u0 = __ldcg(q), u1 = __ldcg(q + 1);
+      Fr v;
+      v.v[0] = u0.x, v.v[1] = u0.y, v.v[2] = u0.z, v.v[3] = u0.w;
+      v.v[4] = u1.x, v.v[5] = u1.y, v.v[6] = u1.z, v.v[7] = u1.w;
+      a = fe_add(a, v);
+    }
     red[threadIdx.x] = a;
     __syncthreads();
     for (int off = blockDim.x / 2; off > 0; off >>= 1) {
       if (threadIdx.x < (unsigned)off) red[threadIdx.x] = fe_add(red[threadIdx.x], red[threadIdx.x + off]);
       __syncthreads();
     }
-    if (threadIdx.x == 0) st_fe(&out[x], red[0]);
+    if (threadIdx.x == 0) st_fe(&A.out[x], red[0]);
     __syncthreads();
   }
+  if (threadIdx.x == 0) *A.done = 0;
 }
 
 // Tables of length 2 -> their bound value (the last round's fold).
@@ -218,6 +233,9 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
   const int max_blocks = c.sm_count * 8;
   Fr* partials = c.scratch[S_TMP6].as<Fr>((size_t)max_blocks * 4);
   Fr* d_out = c.scratch[S_RESULT].as<Fr>(4);
+  unsigned* done = c.scratch[S_ROUND].as<unsigned>(1);
+  APG_CUDA(cudaMemsetAsync(done, 0, sizeof(unsigned), c.stream));
+  F* v = reinterpret_cast<F*>(c.host_pinned());
   DevProgram P = prog;
   P.cached_slot0 = n_val;
 
@@ -238,13 +256,13 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
     A.npairs = (size_t)1 << (n - r - 1);
     A.slots_step0 = n_val + n_cached;
     A.n_val_slots = n_val;
+    A.done = done;
+    A.out = d_out;
     VirtualRound V = virtual_round(point, n);
     const int blocks = (int)std::min<size_t>((A.npairs + threads - 1) / threads, (size_t)max_blocks);
     cudaEvent_t t0 = c.timer_begin();
     launch(c, k_round, blocks, threads, smem, A, P, V, partials);
     c.timer_end(APG_TIMER_SUMCHECK_ROUND, t0);
-    launch(c, k_round_total, 1, 256, 0, (const Fr*)partials, blocks, d_out);
-    F v[4];
     APG_CUDA(cudaMemcpyAsync(v, d_out, 128, cudaMemcpyDeviceToHost, c.stream));
     APG_CUDA(cudaStreamSynchronize(c.stream));
     auto g = host::cubic_through(v);
