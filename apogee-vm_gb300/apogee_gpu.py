@@ -222,6 +222,16 @@ class Context:
     def srs_prepare(self, cbits: int = 0):
         self._check(lib().apg_srs_prepare(self._h, cbits))
 
+    def msm_autotune(self, d_sample: int, n_sample: int, min_log2n: int, max_log2n: int, cands=(8, 12, 16, 20)):
+        """Time SRS commits of each size class with each candidate window
+        width over a device sample (Fr in memory) and keep the fastest.
+        Returns {log2n: width} (0 where the class was skipped)."""
+        arr = (ctypes.c_int * len(cands))(*cands)
+        out = (ctypes.c_int * (max_log2n - min_log2n + 1))()
+        self._check(lib().apg_msm_autotune(self._h, ctypes.c_void_p(d_sample), ctypes.c_size_t(n_sample),
+                                           min_log2n, max_log2n, arr, ctypes.c_size_t(len(cands)), out))
+        return {min_log2n + i: out[i] for i in range(len(out))}
+
     # ---- MSM ----------------------------------------------------------------
     def msm(self, bases: bytes, scalars: bytes) -> bytes:
         """curve::msm::msm: bases 64-byte canonical points, scalars Fr in-memory bytes."""

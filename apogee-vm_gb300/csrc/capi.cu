@@ -154,6 +154,7 @@ int apg_srs_share(apg_ctx* dst, apg_ctx* src) {
   if (!dst || !src || dst == src) return APG_ERR_INVALID_ARGUMENT;
   if (dst->c.device != src->c.device) return APG_ERR_INVALID_ARGUMENT;
   std::vector<SrsTable> tabs;
+  int tuned[64];
   Affine* srs;
   size_t n;
   {
@@ -162,6 +163,7 @@ int apg_srs_share(apg_ctx* dst, apg_ctx* src) {
     srs = src->c.srs;
     n = src->c.srs_n;
     tabs.assign(src->c.tables.begin(), src->c.tables.end());
+    memcpy(tuned, src->c.tuned_c, sizeof(tuned));
     cudaStreamSynchronize(src->c.stream);
   }
   return guarded(dst, [&](Ctx& c) {
@@ -173,6 +175,18 @@ int apg_srs_share(apg_ctx* dst, apg_ctx* src) {
       t.owned = false;
       c.tables.push_back(t);
     }
+    memcpy(c.tuned_c, tuned, sizeof(tuned));
+    return (int)APG_OK;
+  });
+}
+
+int apg_msm_autotune(apg_ctx* ctx, const void* d_sample, size_t n_sample, int min_log2n, int max_log2n,
+                     const int* cands, size_t n_cands, int* chosen_out) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (!d_sample || !cands || n_cands == 0 || min_log2n < 0 || max_log2n < min_log2n || max_log2n > 40)
+      return (int)APG_ERR_INVALID_ARGUMENT;
+    if (!c.srs) return (int)APG_ERR_NO_SRS;
+    msm_autotune(c, d_sample, n_sample, min_log2n, max_log2n, cands, n_cands, chosen_out);
     return (int)APG_OK;
   });
 }
@@ -288,6 +302,7 @@ static Ctx& lane_of(Ctx& c) {
   L.srs = c.srs;
   L.srs_n = c.srs_n;
   L.srs_owned = false;
+  memcpy(L.tuned_c, c.tuned_c, sizeof(c.tuned_c));
   return L;
 }
 

@@ -125,6 +125,9 @@ struct Ctx {
   size_t srs_n = 0;
   bool srs_owned = true;  // false: borrowed from another context (apg_srs_share)
   std::vector<SrsTable> tables;
+  // Window width chosen by apg_msm_autotune per size class (index: ceil of
+  // log2 of the point count); 0 = the default rule of srs_table_for.
+  int tuned_c[64] = {0};
   DevBuf scratch[S_COUNT];
   uint32_t* d_flags = nullptr;  // device error flags (DeviceFlag bits)
   uint64_t launches = 0;        // kernels launched on this context
@@ -217,6 +220,11 @@ const SrsTable* srs_table(Ctx& c, int cbits, size_t need);
 // column are amortised over at least 2^20 points). Null if the SRS is short.
 constexpr size_t kWideTableMin = (size_t)1 << 20;
 const SrsTable* srs_table_for(Ctx& c, size_t n);
+// Time SRS commits of the first 2^k sample scalars for k in [kmin, kmax] with
+// each candidate width and record the fastest in c.tuned_c (see
+// apg_msm_autotune).
+void msm_autotune(Ctx& c, const void* d_sample, size_t sample_len, int kmin, int kmax, const int* cands,
+                  size_t ncands, int* chosen);
 double probe_fq_mul_rate(Ctx& c, double target_ms);
 
 }  // namespace apg

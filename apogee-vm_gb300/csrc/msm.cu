@@ -746,7 +746,18 @@ const SrsTable* srs_table(Ctx& c, int cbits, size_t need) {
   return &c.tables.back();
 }
 
+static int ceil_log2(size_t n) {
+  int k = 0;
+  while (((size_t)1 << k) < n) ++k;
+  return k;
+}
+
 const SrsTable* srs_table_for(Ctx& c, size_t n) {
+  const int cls = ceil_log2(n);
+  if (cls < 64 && c.tuned_c[cls]) {
+    const SrsTable* t = srs_table(c, c.tuned_c[cls], n);
+    if (t) return t;
+  }
   if (n <= ((size_t)1 << 14)) {
     const SrsTable* t = srs_table(c, 8, n);
     if (t) return t;
@@ -756,6 +767,44 @@ const SrsTable* srs_table_for(Ctx& c, size_t n) {
     if (t) return t;
   }
   return srs_table(c, 16, n);
+}
+
+void msm_autotune(Ctx& c, const void* d_sample, size_t sample_len, int kmin, int kmax, const int* cands,
+                  size_t ncands, int* chosen) {
+  cudaEvent_t e0, e1;
+  APG_CUDA(cudaEventCreate(&e0));
+  APG_CUDA(cudaEventCreate(&e1));
+  uint8_t* d_out = c.scratch[S_TMP4].as<uint8_t>(64);
+  for (int k = kmin; k <= kmax; ++k) {
+    const size_t n = (size_t)1 << k;
+    int best_c = 0;
+    float best_ms = 0;
+    if (k < 64 && n <= sample_len && n <= c.srs_n) {
+      for (size_t j = 0; j < ncands; ++j) {
+        const int cb = cands[j];
+        if (cb < 2 || cb > 20) continue;
+        if (cb < 12 && n > ((size_t)1 << 16)) continue;  // narrow tables cover a 2^16 prefix
+        const SrsTable* t = srs_table(c, cb, n);
+        if (!t) continue;
+        msm_device(c, nullptr, t, d_sample, false, false, n, d_out, nullptr);  // warm-up
+        APG_CUDA(cudaEventRecord(e0, c.stream));
+        for (int r = 0; r < 2; ++r) msm_device(c, nullptr, t, d_sample, false, false, n, d_out, nullptr);
+        APG_CUDA(cudaEventRecord(e1, c.stream));
+        APG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        APG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (!best_c || ms < best_ms) {
+          best_c = cb;
+          best_ms = ms;
+        }
+      }
+      c.check_flags();
+      c.tuned_c[k] = best_c;
+    }
+    if (chosen) chosen[k - kmin] = best_c;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
 }
 
 MsmPlan msm_plan(size_t n, bool small_scalars, const SrsTable* table) {

@@ -288,7 +288,18 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
 // A device copy of a resolved gate list.
 void upload_program(Ctx& c, const HostProgram& hp, DevProgram& P, int slot_cap) {
   (void)slot_cap;
-  const size_t gb = hp.gates.size() * sizeof(DevGate);
+  // Mark unit coefficients and weights so the device skips their products.
+  std::vector<DevGate> gates = hp.gates;
+  const host::F one = host::fone();
+  for (auto& g : gates) {
+    g.ones = 0;
+    for (uint32_t i = 0; i < 32 && g.cf_off + i < hp.coeffs.size(); ++i)
+      if (hp.coeffs[g.cf_off + i] == one) g.ones |= 1u << i;
+  }
+  P.weight_ones = 0;
+  for (size_t j = 0; j < 32 && j < hp.weights.size(); ++j)
+    if (hp.weights[j] == one) P.weight_ones |= 1u << j;
+  const size_t gb = gates.size() * sizeof(DevGate);
   const size_t ob = hp.ops.size() * sizeof(uint16_t);
   const size_t cb = hp.coeffs.size() * 32;
   const size_t wb = hp.weights.size() * 32;
@@ -302,7 +313,7 @@ void upload_program(Ctx& c, const HostProgram& hp, DevProgram& P, int slot_cap) 
     off = at + n;
     return d + at;
   };
-  P.gates = (const DevGate*)put(hp.gates.data(), gb);
+  P.gates = (const DevGate*)put(gates.data(), gb);
   P.ops = (const uint16_t*)put(hp.ops.data(), ob);
   P.coeffs = (const Fr*)put(hp.coeffs.data(), cb);
   P.weights = (const Fr*)put(hp.weights.data(), wb);

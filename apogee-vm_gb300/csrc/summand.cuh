@@ -33,6 +33,7 @@ struct DevGate {
   uint16_t p1, p2;   // shape: Linear t; Affine t, u; Quadratic t, u
   uint32_t op_off;   // first operand slot index in ops[]
   uint32_t cf_off;   // first coefficient in coeffs[]
+  uint32_t ones;     // bit i: coefficient cf_off + i is 1 (its product is skipped)
 };
 
 // A resolved list on the device. Gates [0, n_cached) fill the cached slots in
@@ -45,6 +46,7 @@ struct DevProgram {
   int n_cached;
   int n_weighted;
   int cached_slot0;     // slot of cached entry 0
+  uint32_t weight_ones; // bit j: weight j is 1 (lambda^0 always is)
 };
 
 __device__ __forceinline__ Fr sm_ld(const uint32_t* sm, int slot) {
@@ -63,10 +65,22 @@ __device__ __forceinline__ void sm_st(uint32_t* sm, int slot, const Fr& a) {
 
 __device__ __forceinline__ Fr ld_g(const Fr* p) { return ld_fe(p); }
 
-// Affine form sum_{i<t} c[i] * x_i + c[t], operands ops[0..t).
-__device__ __forceinline__ Fr affine_form(const uint32_t* sm, const uint16_t* ops, const Fr* c, int t) {
+// The interpreter calls one out-of-line Fr product: its gate kinds would
+// otherwise inline a dozen multiplies and overflow the instruction cache of
+// the round loop (no_instruction was the top stall of the round kernel).
+static __device__ __noinline__ Fr rmul(const Fr a, const Fr b) { return fe_mul(a, b); }
+
+// c[i] * x, skipping the product when bit i of `ones` marks c[i] = 1.
+__device__ __forceinline__ Fr cmul_coef(const Fr* c, int i, uint32_t ones, const Fr& x) {
+  return (i < 32 && ((ones >> i) & 1u)) ? x : rmul(ld_g(&c[i]), x);
+}
+
+// Affine form sum_{i<t} c[i] * x_i + c[t], operands ops[0..t); `ones` is
+// the one-mask of c[0..].
+__device__ __forceinline__ Fr affine_form(const uint32_t* sm, const uint16_t* ops, const Fr* c, int t,
+                                          uint32_t ones) {
   Fr acc = ld_g(&c[t]);
-  for (int i = 0; i < t; ++i) acc = fe_add(acc, fe_mul(ld_g(&c[i]), sm_ld(sm, ops[i])));
+  for (int i = 0; i < t; ++i) acc = fe_add(acc, cmul_coef(c, i, ones, sm_ld(sm, ops[i])));
   return acc;
 }
 
@@ -76,30 +90,30 @@ static __device__ __noinline__ Fr eval_gate_dev(const DevProgram& P, int g, cons
   const Fr* c = P.coeffs + G.cf_off;
   switch (G.kind) {
     case G_LINEAR:
-      return affine_form(sm, ops, c, G.p1);
+      return affine_form(sm, ops, c, G.p1, G.ones);
     case G_PRODUCT:
-      return fe_mul(fe_mul(ld_g(&c[0]), sm_ld(sm, ops[0])), sm_ld(sm, ops[1]));
+      return rmul(cmul_coef(c, 0, G.ones, sm_ld(sm, ops[0])), sm_ld(sm, ops[1]));
     case G_MASK: {
       Fr x = sm_ld(sm, ops[0]), m = sm_ld(sm, ops[1]);
-      return fe_sub(fe_add(fe_mul(x, m), fe_one<FrConsts>()), m);
+      return fe_sub(fe_add(rmul(x, m), fe_one<FrConsts>()), m);
     }
     case G_AFFINE: {
       const int t = G.p1, u = G.p2;
-      Fr l = affine_form(sm, ops, c, t);
-      Fr r = affine_form(sm, ops + t, c + t + 1, u);
-      return fe_mul(l, r);
+      Fr l = affine_form(sm, ops, c, t, G.ones);
+      Fr r = affine_form(sm, ops + t, c + t + 1, u, t + 1 < 32 ? G.ones >> (t + 1) : 0u);
+      return rmul(l, r);
     }
     case G_TREE_PRODUCT:
-      return fe_mul(sm_ld(sm, ops[0]), sm_ld(sm, ops[1]));
+      return rmul(sm_ld(sm, ops[0]), sm_ld(sm, ops[1]));
     case G_TREE_CROSS:
-      return fe_add(fe_mul(sm_ld(sm, ops[0]), sm_ld(sm, ops[3])), fe_mul(sm_ld(sm, ops[1]), sm_ld(sm, ops[2])));
+      return fe_add(rmul(sm_ld(sm, ops[0]), sm_ld(sm, ops[3])), rmul(sm_ld(sm, ops[1]), sm_ld(sm, ops[2])));
     case G_QUADRATIC: {
       const int t = G.p1, u = G.p2;
       Fr acc = ld_g(&c[0]);
-      for (int i = 0; i < t; ++i) acc = fe_add(acc, fe_mul(ld_g(&c[1 + i]), sm_ld(sm, ops[i])));
+      for (int i = 0; i < t; ++i) acc = fe_add(acc, cmul_coef(c, 1 + i, G.ones, sm_ld(sm, ops[i])));
       for (int j = 0; j < u; ++j) {
-        Fr yz = fe_mul(sm_ld(sm, ops[t + 2 * j]), sm_ld(sm, ops[t + 2 * j + 1]));
-        acc = fe_add(acc, fe_mul(ld_g(&c[1 + t + j]), yz));
+        Fr yz = rmul(sm_ld(sm, ops[t + 2 * j]), sm_ld(sm, ops[t + 2 * j + 1]));
+        acc = fe_add(acc, cmul_coef(c, 1 + t + j, G.ones, yz));
       }
       return acc;
     }
@@ -113,7 +127,7 @@ __device__ __forceinline__ Fr eval_summand(const DevProgram& P, uint32_t* sm) {
   Fr acc = fe_zero<FrConsts>();
   for (int j = 0; j < P.n_weighted; ++j) {
     Fr v = eval_gate_dev(P, P.n_cached + j, sm);
-    acc = fe_add(acc, fe_mul(v, ld_g(&P.weights[j])));
+    acc = fe_add(acc, cmul_coef(P.weights, j, P.weight_ones, v));
   }
   return acc;
 }

@@ -36,6 +36,7 @@ METRIC = "G1 MSM points/s at 2^22"
 UNIT = "points/s"
 SEED = 20260903
 TAU_SEED = 0x7A75_5EED
+TUNE_WIDTHS = (8, 12, 16, 18, 20)  # window widths the autotuner tries per size class
 
 
 def env_int(name, default):
@@ -61,10 +62,13 @@ def algorithmic_fqmul_accumulate(n):
     return n * windows * 10
 
 
-def own_windows(n):
-    """Signed-digit windows of the SRS window table an n-point commit reads
-    (8-bit up to 2^14 points, 16-bit below 2^20, 20-bit from 2^20)."""
-    c = 8 if n <= 1 << 14 else (16 if n < 1 << 20 else 20)
+def own_windows(n, tuned=None):
+    """Signed-digit windows of the SRS window table an n-point commit reads:
+    the autotuner's width for the size class when it chose one, else the
+    library's default rule (8-bit up to 2^14 points, 16-bit below 2^20,
+    20-bit from 2^20)."""
+    lg = max(0, (n - 1).bit_length())
+    c = (tuned or {}).get(lg) or (8 if n <= 1 << 14 else (16 if n < 1 << 20 else 20))
     return -(-255 // c)
 
 
@@ -242,6 +246,8 @@ def run_profile_case(args):
     dev = f"cuda:{local}"
     n = args.log2n
     ctx = A.Context(local)
+    if args.profile_case == "shard":
+        return run_profile_shard(args, ctx, torch, dev)
     if args.profile_case == "open":
         ctx.srs_generate((TAU_SEED * 0x9E3779B97F4A7C15) % A.P_R, 1 << n)
         ctx.srs_prepare()
@@ -274,6 +280,52 @@ def run_profile_case(args):
                                                             "gkr_forward", "mercury_pass"])}
     print(json.dumps({"case": args.profile_case, "log2n": n, "ms_per_call": dt * 1e3,
                       "timers_ms_launches": timers}), flush=True)
+    ctx.close()
+    return 0
+
+
+def run_profile_shard(args, ctx, torch, dev):
+    """One shard of 2^log2n rows x --cols columns proved phase by phase
+    (commit, forward, GKR proof, batched opening), host wall time per phase
+    with the device drained between phases."""
+    import apogee_gpu as A
+    import shard
+
+    n = args.log2n
+    ctx.srs_generate((TAU_SEED * 0x9E3779B97F4A7C15) % A.P_R, 1 << n)
+    ctx.srs_prepare()
+    spec = {"index": 3, "family": 1, "log_rows": n, "cols": args.cols}
+    cols = shard.device_columns(torch, 1 << n, args.cols, SEED, dev, ctx)
+    ptrs = [t.data_ptr() for t in cols]
+    blob = shard.shard_circuit(n, args.cols)
+    phases = {"commit": 0.0, "forward": 0.0, "gkr_prove": 0.0, "batch_open": 0.0}
+
+    def once(acc):
+        def tick(name, t0):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            if acc:
+                phases[name] += t1 - t0
+            return t1
+        t = time.perf_counter()
+        cms = ctx.commit_batch_device(ptrs, n)
+        t = tick("commit", t)
+        tr, g, beta = shard.shard_transcript(spec, cms)
+        v = ctx.gkr_forward(blob, ptrs, {0: g, 1: beta}, on_device=True)
+        t = tick("forward", t)
+        _, tr, point = ctx.gkr_prove(blob, v, {0: g, 1: beta}, tr, with_point=True)
+        v.free()
+        t = tick("gkr_prove", t)
+        ctx.batch_open(ptrs, n, cms, A.from_mont_bytes(point), tr, on_device=True)
+        tick("batch_open", t)
+
+    for _ in range(args.warmup):
+        once(False)
+    for _ in range(args.steps):
+        once(True)
+    out = {k: v * 1e3 / args.steps for k, v in phases.items()}
+    print(json.dumps({"case": "shard", "log2n": n, "cols": args.cols, "ms_per_phase": out,
+                      "ms_total": sum(out.values())}), flush=True)
     ctx.close()
     return 0
 
@@ -406,6 +458,12 @@ def run_gpu(args):
     tau = (TAU_SEED * 0x9E3779B97F4A7C15) % A.P_R
     ctx.srs_generate(tau, n)
     ctx.srs_prepare()
+    # Window widths per size class from the library's autotuner, on a sample
+    # column drawn like the workload's (untimed setup).
+    tsample = torch.from_numpy(synth.mixed_column(n, SEED + 4242).view(np.int32).reshape(-1)).to(f"cuda:{local}")
+    ctx.fr_to_mont_device(tsample.data_ptr(), n)
+    tuned = ctx.msm_autotune(tsample.data_ptr(), n, 8, log2n, cands=TUNE_WIDTHS)
+    del tsample
 
     # Inputs: k mixed columns per rank, canonical on the host, Montgomery on
     # the device and in a pinned host mirror for the end-to-end leg.
@@ -451,7 +509,7 @@ def run_gpu(args):
     # End to end through the public API with host buffers.
     for _ in range(1):
         ctx.commit_batch_host(hptrs, log2n)
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = max(1, args.steps)
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -483,7 +541,7 @@ def run_gpu(args):
     fq_rate = ctx.probe_fq_mul_rate(300.0)
     algo = algorithmic_fqmul_accumulate(n)
     achieved = algo / (acc_ms / acc_n / 1e3)
-    own = n * own_windows(n) * 10
+    own = n * own_windows(n, tuned) * 10
     traffic = ACC_TRAFFIC_BYTES.get(log2n)
     roofline = {
         "bound": "int", "kernel": f"k_bucket_acc (bucket accumulation, 2^{log2n} uniform scalars)",
@@ -494,7 +552,7 @@ def run_gpu(args):
         "msm_uniform_points_per_s": n / (tot_ms / tot_n / 1e3), "algorithmic_fqmul_per_launch": algo,
         "algorithmic_basis": f"reference work: {reference_window_windows(n)[1]} windows x n mixed adds x 10 Fq-mul",
         "achieved_timad32_equiv": achieved * 264 / 1e12,
-        "own_fqmul_per_launch": own, "own_windows": own_windows(n),
+        "own_fqmul_per_launch": own, "own_windows": own_windows(n, tuned),
         "own_frac": own / (acc_ms / acc_n / 1e3) / fq_rate,
     }
 
@@ -528,6 +586,7 @@ def run_gpu(args):
             "config": {"workload": f"commit: {k} columns x 2^{log2n} Fr per GPU, mixed VM-trace distribution "
                                    "(25% {0,1}, 60% u32, 15% uniform Fr), seeded-tau SRS",
                        "msm_points": n, "columns_per_gpu": k, "parallelism": f"replicas x{world}",
+                       "msm_window_bits": {str(lg): c for lg, c in tuned.items()},
                        "l2": "inputs 2 GiB per GPU > 129 MB L2, no flush needed"},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
             "gpu_launches": launches, "shard_workloads": shards,
@@ -551,8 +610,8 @@ def main():
     ap.add_argument("--scalars", choices=["uniform", "mixed"], default="uniform", help="scalars of --only-msm")
     ap.add_argument("--no-shards", dest="shards", action="store_false",
                     help="skip the per-config shard timings and the 207-shard mix / serving run")
-    ap.add_argument("--profile-case", choices=["zerocheck", "gkr", "open"], default=None,
-                    help="run one lean sumcheck / GKR / opening case for profilers")
+    ap.add_argument("--profile-case", choices=["zerocheck", "gkr", "open", "shard"], default=None,
+                    help="run one lean sumcheck / GKR / opening / whole-shard case for profilers")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -96,6 +96,17 @@ int apg_srs_share(apg_ctx* dst, apg_ctx* src);
  * (window width `cbits`, 0 = the library's choice). Optional: the first
  * commit builds it. Costs windows x n x 64 bytes of device memory. */
 int apg_srs_prepare(apg_ctx* ctx, int cbits);
+/* No reference counterpart (the reference derives its window from n alone,
+ * crates/curve/src/msm.rs:112-118). The window-width autotuner: for each size
+ * class 2^k, min_log2n <= k <= max_log2n, time commits of the first 2^k of
+ * the n_sample device scalars (Fr in memory, drawn like the columns to be
+ * committed) with every candidate width (bits, 2..20; widths below 12 only
+ * up to 2^16 points), building the window tables it needs, and keep the
+ * fastest for this context's later commits and openings (shared contexts and
+ * lanes inherit it). chosen_out (nullable) receives max_log2n - min_log2n + 1
+ * widths, 0 where a class exceeds the sample or the SRS. */
+int apg_msm_autotune(apg_ctx* ctx, const void* d_sample, size_t n_sample, int min_log2n, int max_log2n,
+                     const int* cands, size_t n_cands, int* chosen_out);
 
 /* ---- MSM (crates/curve/src/msm.rs) ------------------------------------- */
 

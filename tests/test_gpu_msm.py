@@ -261,3 +261,32 @@ def test_commit_batch_many_small_columns(ctx):
     cms = ctx.commit_batch([A.to_mont_bytes(c) for c in cols], nv)
     for c, cm in zip(cols, cms):
         assert cm == O.g1_mul(O.G1_GEN, _f_tau(c, tau))
+
+
+def test_autotune_choice_keeps_commitments(ctx):
+    """The window-width autotuner only changes speed: after it records a
+    width per size class, commits (alone and batched) still equal [f(tau)]G,
+    and every chosen width is one of the candidates."""
+    import numpy as np
+    import torch
+
+    import apogee_gpu as A
+    import synth
+
+    tau = 0xA070
+    nv = 12
+    n = 1 << nv
+    ctx.srs_generate(tau, n)
+    sample = torch.from_numpy(synth.mixed_column(n, 3).view(np.int32).reshape(-1)).to("cuda:0")
+    ctx.fr_to_mont_device(sample.data_ptr(), n)
+    chosen = ctx.msm_autotune(sample.data_ptr(), n, 8, 13, cands=(8, 12, 16))
+    assert set(chosen) == set(range(8, 14))
+    assert chosen[13] == 0  # beyond the sample and the SRS
+    assert all(chosen[k] in (8, 12, 16) for k in range(8, 13))
+    rng = random.Random(77)
+    for k in (8, 10, 12):
+        cols = [_column(kind, 1 << k, rng) for kind in ("mixed", "uniform", "u32")]
+        cms = ctx.commit_batch([A.to_mont_bytes(c) for c in cols], k)
+        for c, cm in zip(cols, cms):
+            assert cm == O.g1_mul(O.G1_GEN, _f_tau(c, tau))
+        assert ctx.commit(A.to_mont_bytes(cols[0]), k) == cms[0]
