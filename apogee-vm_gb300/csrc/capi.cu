@@ -123,6 +123,7 @@ void apg_ctx_destroy(apg_ctx* ctx) {
     if (c.srs && c.srs_owned) cudaFree(c.srs);
     if (c.d_flags) cudaFree(c.d_flags);
     if (c.pinned) cudaFreeHost(c.pinned);
+    if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
     if (c.stream) cudaStreamDestroy(c.stream);
   }
   delete ctx;
@@ -341,21 +342,35 @@ static int commit_batch_lanes(Ctx& c, const void* const* cols, bool host, size_t
   APG_CUDA(cudaEventRecord(ev, c.stream));
   APG_CUDA(cudaStreamWaitEvent(L.stream, ev, 0));
   const size_t group = std::max<size_t>(1, (k + 3) / 4);
+  const size_t ngroups = (k + group - 1) / group;
   std::vector<const void*> ptrs(cols, cols + k);
   std::vector<size_t> lens(k, n);
+  // Host columns land in one device buffer through a copy stream of their
+  // own, group after group, so the copies run back to back at full bandwidth
+  // and each group's MSMs start as soon as its own columns are in.
+  std::vector<cudaEvent_t> landed;
+  if (host) {
+    if (!c.copy_stream) APG_CUDA(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+    uint8_t* buf = c.scratch[S_SCALARS].as<uint8_t>(32 * n * k);
+    APG_CUDA(cudaStreamWaitEvent(c.copy_stream, ev, 0));  // the buffer's previous users are done
+    landed.resize(ngroups, nullptr);
+    for (size_t gi = 0; gi < ngroups; ++gi) {
+      for (size_t j = gi * group; j < std::min(k, (gi + 1) * group); ++j) {
+        APG_CUDA(cudaMemcpyAsync(buf + 32 * n * j, cols[j], 32 * n, cudaMemcpyHostToDevice, c.copy_stream));
+        ptrs[j] = buf + 32 * n * j;
+      }
+      APG_CUDA(cudaEventCreateWithFlags(&landed[gi], cudaEventDisableTiming));
+      APG_CUDA(cudaEventRecord(landed[gi], c.copy_stream));
+    }
+  }
   for (size_t j0 = 0, gi = 0; j0 < k; j0 += group, ++gi) {
     Ctx& X = *lanes[gi & 1];
     const size_t m = std::min(group, k - j0);
     const SrsTable* t = commit_table(X, n);
-    if (host) {
-      uint8_t* buf = X.scratch[S_SCALARS].as<uint8_t>(32 * n * group);
-      for (size_t j = 0; j < m; ++j) {
-        APG_CUDA(cudaMemcpyAsync(buf + 32 * n * j, cols[j0 + j], 32 * n, cudaMemcpyHostToDevice, X.stream));
-        ptrs[j0 + j] = buf + 32 * n * j;
-      }
-    }
+    if (host) APG_CUDA(cudaStreamWaitEvent(X.stream, landed[gi], 0));
     msm_multi(X, nullptr, t, ptrs.data() + j0, lens.data() + j0, m, false, false, d_out + 64 * j0);
   }
+  for (auto e : landed) cudaEventDestroy(e);
   APG_CUDA(cudaEventRecord(ev, L.stream));
   APG_CUDA(cudaStreamWaitEvent(c.stream, ev, 0));
   APG_CUDA(cudaEventDestroy(ev));

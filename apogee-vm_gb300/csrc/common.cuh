@@ -137,6 +137,8 @@ struct Ctx {
   // latency-bound tail (and the next column's copy) overlaps another's
   // bucket accumulation.
   std::unique_ptr<Ctx> lane;
+  // Host-to-device copies of batch commits' host columns.
+  cudaStream_t copy_stream = nullptr;
 
   // A small pinned host buffer for per-round device-to-host reads (a true
   // asynchronous copy, no staging through pageable memory).
@@ -218,8 +220,11 @@ const SrsTable* srs_table(Ctx& c, int cbits, size_t need);
 // points (a cheap bucket reduction), 16-bit windows below kWideTableMin and
 // 20-bit windows from there (13 windows instead of 16; the 2^19 buckets a
 // column are amortised over at least 2^20 points). Null if the SRS is short.
+// `tuned`: use the width apg_msm_autotune chose for the size class, if any
+// (commits of the caller's columns); openings commit uniformly random
+// quotient polynomials, for which the default rule is the uniform-scalar one.
 constexpr size_t kWideTableMin = (size_t)1 << 20;
-const SrsTable* srs_table_for(Ctx& c, size_t n);
+const SrsTable* srs_table_for(Ctx& c, size_t n, bool tuned = true);
 // Time SRS commits of the first 2^k sample scalars for k in [kmin, kmax] with
 // each candidate width and record the fastest in c.tuned_c (see
 // apg_msm_autotune).

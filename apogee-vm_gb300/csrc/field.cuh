@@ -324,22 +324,122 @@ __device__ __forceinline__ bool fe_lt_mod(const uint32_t a[8]) {
   return false;
 }
 
-// a^(m-2) by a fixed square-and-multiply over the exponent's bits.
+// 1/a by the binary extended Euclidean algorithm on the Montgomery value A =
+// aR: with u = A, v = m, x1 = 1, x2 = 0 it keeps A*x1 = u and A*x2 = v (mod m),
+// halves whichever of u, v is even (halving x mod m alongside) and otherwise
+// subtracts the smaller from the larger, until u or v is 1; then x = A^-1 =
+// a^-1 R^-1 and a^-1 R = x * R^3 (one Montgomery product with R^3 = R2 * R2
+// reduced once). Variable time (the inputs are public values). Every step
+// strictly shrinks u * v < 2^510 or makes u or v even, so at most about 1020
+// steps run; the loop is also capped. 0 maps to 0.
 template <class C>
-__device__ __noinline__ Fe<C> fe_inverse(const Fe<C>& a) {
+__device__ __forceinline__ void inv_half(uint32_t x[8]) {  // x/2 mod m for x < m
   const uint32_t p[8] = {C::P0, C::P1, C::P2, C::P3, C::P4, C::P5, C::P6, C::P7};
-  uint32_t e[8];
+  uint32_t t[8];
+  if (x[0] & 1u) {  // x + m < 2^255: no carry out of 256 bits
+    uint64_t c = 0;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) e[i] = p[i];
-  e[0] -= 2;  // P0 is odd and > 2 for both moduli: no borrow
-  Fe<C> acc = fe_one<C>();
-  for (int i = 7; i >= 0; --i) {
-    for (int b = 31; b >= 0; --b) {
-      acc = fe_sqr(acc);
-      if ((e[i] >> b) & 1) acc = fe_mul(acc, a);
+    for (int i = 0; i < 8; ++i) {
+      c += (uint64_t)x[i] + p[i];
+      t[i] = (uint32_t)c;
+      c >>= 32;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) t[i] = x[i];
+  }
+#pragma unroll
+  for (int i = 0; i < 7; ++i) x[i] = __funnelshift_r(t[i], t[i + 1], 1);
+  x[7] = t[7] >> 1;
+}
+
+template <class C>
+__device__ __forceinline__ void inv_sub_mod(uint32_t x[8], const uint32_t y[8]) {  // x - y mod m
+  const uint32_t p[8] = {C::P0, C::P1, C::P2, C::P3, C::P4, C::P5, C::P6, C::P7};
+  int64_t b = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    b += (int64_t)x[i] - y[i];
+    x[i] = (uint32_t)b;
+    b >>= 32;
+  }
+  if (b) {
+    uint64_t c = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      c += (uint64_t)x[i] + p[i];
+      x[i] = (uint32_t)c;
+      c >>= 32;
     }
   }
-  return acc;
+}
+
+__device__ __forceinline__ void inv_sub_plain(uint32_t x[8], const uint32_t y[8]) {  // x - y, x >= y
+  int64_t b = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    b += (int64_t)x[i] - y[i];
+    x[i] = (uint32_t)b;
+    b >>= 32;
+  }
+}
+
+template <class C>
+__device__ __noinline__ Fe<C> fe_inverse(const Fe<C>& a) {
+  if (fe_is_zero(a)) return a;
+  const uint32_t p[8] = {C::P0, C::P1, C::P2, C::P3, C::P4, C::P5, C::P6, C::P7};
+  uint32_t u[8], v[8], x1[8], x2[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    u[i] = a.v[i];
+    v[i] = p[i];
+    x1[i] = 0;
+    x2[i] = 0;
+  }
+  x1[0] = 1;
+  auto is_one = [](const uint32_t* w) {
+    uint32_t o = w[0] ^ 1u;
+#pragma unroll
+    for (int i = 1; i < 8; ++i) o |= w[i];
+    return o == 0;
+  };
+  for (int guard = 0; guard < 4096 && !is_one(u) && !is_one(v); ++guard) {
+    if (!(u[0] & 1u)) {
+#pragma unroll
+      for (int i = 0; i < 7; ++i) u[i] = __funnelshift_r(u[i], u[i + 1], 1);
+      u[7] >>= 1;
+      inv_half<C>(x1);
+    } else if (!(v[0] & 1u)) {
+#pragma unroll
+      for (int i = 0; i < 7; ++i) v[i] = __funnelshift_r(v[i], v[i + 1], 1);
+      v[7] >>= 1;
+      inv_half<C>(x2);
+    } else {
+      bool ge = true;  // u >= v
+#pragma unroll
+      for (int i = 7; i >= 0; --i) {
+        if (u[i] != v[i]) {
+          ge = u[i] > v[i];
+          break;
+        }
+      }
+      if (ge) {
+        inv_sub_plain(u, v);
+        inv_sub_mod<C>(x1, x2);
+      } else {
+        inv_sub_plain(v, u);
+        inv_sub_mod<C>(x2, x1);
+      }
+    }
+  }
+  Fe<C> x;
+  const bool from_u = is_one(u);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x.v[i] = from_u ? x1[i] : x2[i];
+  Fe<C> r2;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r2.v[i] = C::R2(i);
+  return fe_mul(x, fe_mul(r2, r2));
 }
 
 template <class C>

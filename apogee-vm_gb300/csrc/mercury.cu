@@ -212,7 +212,7 @@ void srs_commit(Ctx& c, const Fr* d, size_t len, uint8_t out[64]) {
     memset(out, 0, 64);
     return;
   }
-  const SrsTable* t = srs_table_for(c, len);
+  const SrsTable* t = srs_table_for(c, len, false);
   if (!t) throw Error(APG_ERR_SRS_TOO_SMALL, "the SRS holds fewer powers than the polynomial has coefficients");
   msm_device(c, nullptr, t, d, false, false, len, nullptr, out);
 }
@@ -226,7 +226,7 @@ void srs_commit2(Ctx& c, const Fr* d0, size_t len0, const Fr* d1, size_t len1, u
     srs_commit(c, d1, len1, out1);
     return;
   }
-  const SrsTable* t = srs_table_for(c, std::max(len0, len1));
+  const SrsTable* t = srs_table_for(c, std::max(len0, len1), false);
   if (!t) throw Error(APG_ERR_SRS_TOO_SMALL, "the SRS holds fewer powers than the polynomial has coefficients");
   const void* ptrs[2] = {d0, d1};
   const size_t lens[2] = {len0, len1};

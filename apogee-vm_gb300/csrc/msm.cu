@@ -635,6 +635,33 @@ __global__ void __launch_bounds__(128, APG_ACC_MIN_BLOCKS) k_bucket_acc(const ui
   if (!head_written) put_item(okeys, opts, opres, 2 * s, first, nullptr);
 }
 
+// Bucket reduction of a small bucket set (K <= kSmallK), one block per space:
+// thread t holds B_t (weight t + 1); a suffix scan turns it into
+// S_t = sum_{k >= t} B_k, and sum_k (k + 1) B_k = sum_t S_t is a tree sum, so
+// the dependent chain is 2 log2 K additions instead of the running-sum levels.
+constexpr int kSmallK = 256;
+
+__global__ void __launch_bounds__(kSmallK) k_reduce_small(const Xyzz* buckets, int K, Xyzz* out) {
+  __shared__ Xyzz shx[kSmallK];
+  const int sp = blockIdx.x, t = threadIdx.x;
+  Xyzz v = ld_xyzz(&buckets[(size_t)sp * K + t]);
+  shx[t] = v;
+  __syncthreads();
+  for (int off = 1; off < K; off <<= 1) {
+    const bool has = t + off < K;
+    Xyzz nb = has ? shx[t + off] : xyzz_inf();
+    __syncthreads();
+    if (has) v = xyzz_add(v, nb);
+    shx[t] = v;
+    __syncthreads();
+  }
+  for (int off = K / 2; off > 0; off >>= 1) {
+    if (t < off) shx[t] = xyzz_add(shx[t], shx[t + off]);
+    __syncthreads();
+  }
+  if (t == 0) st_xyzz(&out[sp], shx[0]);
+}
+
 // One thread per column: Horner over the reduction levels (in `fan`) and the
 // column's spaces (windows, in 2^c), then the canonical affine bytes.
 __global__ void k_finish_cols(const Xyzz* tsum, int levels, int spaces_total, int spaces_per_col, int ncols,
@@ -752,9 +779,9 @@ static int ceil_log2(size_t n) {
   return k;
 }
 
-const SrsTable* srs_table_for(Ctx& c, size_t n) {
+const SrsTable* srs_table_for(Ctx& c, size_t n, bool tuned) {
   const int cls = ceil_log2(n);
-  if (cls < 64 && c.tuned_c[cls]) {
+  if (tuned && cls < 64 && c.tuned_c[cls]) {
     const SrsTable* t = srs_table(c, c.tuned_c[cls], n);
     if (t) return t;
   }
@@ -911,9 +938,13 @@ void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols
       len = 2 * fseg;
     }
   }
+  if ((int)K <= kSmallK) {
+    launch(c, k_reduce_small, (unsigned)S, (unsigned)K, 0, (const Xyzz*)buckets, (int)K, tsum);
+    levels = 1;
+  }
   const Xyzz* lvl_in = buckets;
   int M = (int)K;
-  for (int l = 0; l < levels; ++l) {
+  for (int l = 0; l < levels && (int)K > kSmallK; ++l) {
     const int G = (M + kLevelFan - 1) / kLevelFan;
     Xyzz* outR = (l & 1) ? lvlB : lvlA;
     launch(c, k_level, blocks_for<int>((size_t)S * G, 64), 64, 0, lvl_in, M, S, kLevelFan, outT, outR);
