@@ -150,6 +150,13 @@ __global__ void k_eq_table(const Fr* r, int n, size_t len, Fr* out) {
   st_fe(&out[y], acc);
 }
 
+// out[y] = lo[y mod 2^nlo] * hi[y >> nlo]: eq(r, y) split at bit nlo.
+__global__ void k_eq_combine(const Fr* lo, const Fr* hi, int nlo, size_t len, Fr* out) {
+  size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (y >= len) return;
+  st_fe(&out[y], fe_mul(ld_fe(&lo[y & (((size_t)1 << nlo) - 1)]), ld_fe(&hi[y >> nlo])));
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -164,11 +171,26 @@ static Fr to_dev(const F& a) {
   return r;
 }
 
+// eq(r, y) for every y < 2^|r|. Up to 12 variables each entry is its own
+// product of |r| factors; beyond, the two halves' tables (2^(n/2) entries
+// each) are built that way and every entry is one product of the two.
 void build_eq_table(Ctx& c, const std::vector<F>& r, Fr* out) {
-  const size_t len = (size_t)1 << r.size();
-  Fr* d_r = c.scratch[S_TMP4].as<Fr>(std::max<size_t>(r.size(), 1));
-  if (!r.empty()) APG_CUDA(cudaMemcpyAsync(d_r, r.data(), 32 * r.size(), cudaMemcpyHostToDevice, c.stream));
-  launch(c, k_eq_table, (unsigned)((len + 255) / 256), 256, 0, (const Fr*)d_r, (int)r.size(), len, out);
+  const int n = (int)r.size();
+  const size_t len = (size_t)1 << n;
+  const int nlo = n / 2, nhi = n - nlo;
+  const bool split = n > 12;
+  const size_t lo_len = (size_t)1 << nlo, hi_len = (size_t)1 << nhi;
+  Fr* d_r = c.scratch[S_TMP4].as<Fr>(std::max<size_t>(n, 1) + (split ? lo_len + hi_len : 0));
+  if (n) APG_CUDA(cudaMemcpyAsync(d_r, r.data(), 32 * (size_t)n, cudaMemcpyHostToDevice, c.stream));
+  if (!split) {
+    launch(c, k_eq_table, (unsigned)((len + 255) / 256), 256, 0, (const Fr*)d_r, n, len, out);
+    return;
+  }
+  Fr* lo = d_r + n;
+  Fr* hi = lo + lo_len;
+  launch(c, k_eq_table, (unsigned)((lo_len + 255) / 256), 256, 0, (const Fr*)d_r, nlo, lo_len, lo);
+  launch(c, k_eq_table, (unsigned)((hi_len + 255) / 256), 256, 0, (const Fr*)(d_r + nlo), nhi, hi_len, hi);
+  launch(c, k_eq_combine, (unsigned)((len + 255) / 256), 256, 0, (const Fr*)lo, (const Fr*)hi, nlo, len, out);
 }
 
 static VirtualRound virtual_round(const std::vector<F>& point, int nvars) {

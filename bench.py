@@ -207,6 +207,13 @@ def run_msm_only(args):
     ctx = A.Context(local)
     ctx.srs_generate((TAU_SEED * 0x9E3779B97F4A7C15) % A.P_R, n)
     ctx.srs_prepare()
+    tsample = torch.from_numpy(synth.mixed_column(n, SEED + 4242).view(np.int32).reshape(-1)).to(f"cuda:{local}")
+    ctx.fr_to_mont_device(tsample.data_ptr(), n)
+    # A fixed --window-bits keeps a profiled run's width independent of the
+    # autotuner, whose timings a profiler distorts.
+    cands = (args.window_bits,) if args.window_bits else TUNE_WIDTHS
+    tuned = ctx.msm_autotune(tsample.data_ptr(), n, args.log2n, args.log2n, cands=cands)
+    del tsample
     cols = []
     for j in range(args.cols):
         gen = synth.mixed_column if args.scalars == "mixed" else synth.uniform_column
@@ -223,7 +230,7 @@ def run_msm_only(args):
     torch.cuda.synchronize()
     dt = (time.perf_counter() - t0) / args.steps
     print(json.dumps({"msm_only": True, "scalars": args.scalars, "log2n": args.log2n, "cols": args.cols,
-                      "ms_per_step": dt * 1e3,
+                      "window_bits": tuned[args.log2n], "ms_per_step": dt * 1e3,
                       "points_per_s": args.cols * n / dt}), flush=True)
     ctx.close()
     return 0
@@ -608,6 +615,7 @@ def main():
     ap.add_argument("--cols", type=int, default=16)
     ap.add_argument("--only-msm", action="store_true", help="lean SRS MSM case for profiling")
     ap.add_argument("--scalars", choices=["uniform", "mixed"], default="uniform", help="scalars of --only-msm")
+    ap.add_argument("--window-bits", type=int, default=0, help="--only-msm: fixed window width instead of autotuning")
     ap.add_argument("--no-shards", dest="shards", action="store_false",
                     help="skip the per-config shard timings and the 207-shard mix / serving run")
     ap.add_argument("--profile-case", choices=["zerocheck", "gkr", "open", "shard"], default=None,

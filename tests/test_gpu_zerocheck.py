@@ -59,7 +59,7 @@ def run_case(ctx, terms, cols, nv, seed):
     return rounds, finals
 
 
-@pytest.mark.parametrize("nv", [0, 1, 2, 3, 5, 8, 11])
+@pytest.mark.parametrize("nv", [0, 1, 2, 3, 5, 8, 11, 13, 14])
 def test_zerocheck_matches_oracle(ctx, nv):
     rng = random.Random(nv)
     n = 1 << nv
