@@ -527,16 +527,16 @@ int mercury_batch_open_impl(Ctx& c, const Fr* const* d_cols, size_t k, size_t nv
     Fr* p;
     ~Guard() { cudaFreeAsync(p, c.stream); }
   } guard{c, work};
-  Fr *eq1 = work, *eq2 = eq1 + b, *h = eq2 + b, *w = h + b, *fstar = w + k, *tmp = fstar + n;
-  // Each column's value at u, through the same restriction h: f(u) = <eq2, h>.
+  Fr *eq1 = work, *eq2 = eq1 + b, *h = eq2 + b, *w = h + b, *fstar = w + k;
+  // Each column's value at u, through the same restriction h: f(u) = <eq2, h>;
+  // the k values land in w and come back in one read.
   build_eq_table(c, u1, eq1);
   build_eq_table(c, u2, eq2);
-  vs.assign(k, fzero());
   for (size_t col = 0; col < k; ++col) {
     launch(c, k_row_dot, nb(b * 32, 256), 256, 0, d_cols[col], (const Fr*)eq1, b, b, h);
-    launch(c, k_dot, 1, 256, 0, (const Fr*)eq2, (const Fr*)h, b, tmp);
-    vs[col] = read_fr(c, tmp);
+    launch(c, k_dot, 1, 256, 0, (const Fr*)eq2, (const Fr*)h, b, w + col);
   }
+  vs = read_frs(c, w, k);
   tr.absorb_g1(T_COMMITMENT, cms, k);
   std::vector<F> claim = u;
   claim.insert(claim.end(), vs.begin(), vs.end());

@@ -972,7 +972,7 @@ void msm_multi(Ctx& c, const Affine* bases, const SrsTable* table, const void* c
   size_t j = 0;
   while (j < k) {
     // Grow the group while the plan, the bucket range and the sorted list fit.
-    size_t nmax = 0, emax = 0;
+    size_t nmax = 0;
     MsmPlan p{};
     size_t g = 0;
     while (j + g < k && g < (size_t)kMaxCols) {
@@ -988,10 +988,8 @@ void msm_multi(Ctx& c, const Affine* bases, const SrsTable* table, const void* c
       if (bins > kMaxBins) throw Error(APG_ERR_INVALID_ARGUMENT, "too many buckets");
       p = q;
       nmax = nm;
-      emax = e;
       ++g;
     }
-    (void)emax;
     MsmCols cols{};
     for (size_t t = 0; t < g; ++t) {
       cols.s[t] = scalars[j + t];

@@ -33,13 +33,17 @@ struct RoundArgs {
   int n_val_slots;           // nd + nv
   unsigned* done;            // blocks finished this round (zero between rounds)
   Fr* out;                   // the round's 4 sums, written by the last block
+  int xsplit;                // one thread per (pair, node X) instead of per pair
 };
 
 __device__ __forceinline__ const Fr* table_in(const RoundArgs& A, int k) {
   return A.in_is_src ? A.src[k] : A.in_base + (size_t)k * A.in_len;
 }
 
-__device__ __forceinline__ void load_line(const RoundArgs& A, int k, size_t i, Fr& lo, Fr& hi) {
+// Pair i of table k: (lo, hi) = entries (2i, 2i + 1) of this round's level,
+// folded from the previous level with c first when the round binds (the
+// folded pair is stored when `store` is set).
+__device__ __forceinline__ void load_line(const RoundArgs& A, int k, size_t i, Fr& lo, Fr& hi, bool store = true) {
   const Fr* t = table_in(A, k);
   if (!A.bind) {
     lo = ld_fe(&t[2 * i]);
@@ -49,9 +53,17 @@ __device__ __forceinline__ void load_line(const RoundArgs& A, int k, size_t i, F
   Fr a0 = ld_fe(&t[4 * i]), a1 = ld_fe(&t[4 * i + 1]), a2 = ld_fe(&t[4 * i + 2]), a3 = ld_fe(&t[4 * i + 3]);
   lo = fe_add(a0, fe_mul(A.c, fe_sub(a1, a0)));
   hi = fe_add(a2, fe_mul(A.c, fe_sub(a3, a2)));
+  if (!store) return;
   Fr* o = A.out_base + (size_t)k * (A.in_len / 2);
   st_fe(&o[2 * i], lo);
   st_fe(&o[2 * i + 1], hi);
+}
+
+// lo + x * (hi - lo) for a node x in 0..3.
+__device__ __forceinline__ Fr at_node(const Fr& lo, const Fr& step, int x) {
+  Fr v = lo;
+  for (int j = 0; j < x; ++j) v = fe_add(v, step);
+  return v;
 }
 
 __global__ void __launch_bounds__(kRoundThreads) k_round(RoundArgs A, DevProgram P, VirtualRound V, Fr* partials) {
@@ -61,6 +73,38 @@ __global__ void __launch_bounds__(kRoundThreads) k_round(RoundArgs A, DevProgram
 #pragma unroll
   for (int x = 0; x < 4; ++x) acc[x] = fe_zero<FrConsts>();
   const size_t stride = (size_t)gridDim.x * blockDim.x;
+  if (A.xsplit) {
+    // Small rounds: thread t evaluates pair t / 4 at node X = t % 4 alone, so
+    // the four evaluations of a pair run side by side (latency, not work, is
+    // what bounds a round with few pairs). Threads 4j..4j+3 of a block share
+    // a pair; the X = 0 thread stores the folded level.
+    const int x = threadIdx.x & 3;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t / 4 < A.npairs; t += stride) {
+      const size_t i = t / 4;
+      Fr lo, hi;
+      for (int k = 0; k < A.nd; ++k) {
+        load_line(A, k, i, lo, hi, x == 0);
+        sm_st(sm, k, at_node(lo, fe_sub(hi, lo), x));
+      }
+      for (int v = 0; v < A.nv; ++v) {
+        virtual_line_dev(V, A.vkinds[v], i, lo, hi);  // hi is the step here
+        sm_st(sm, A.nd + v, at_node(lo, hi, x));
+      }
+      Fr e_lo, e_hi;
+      load_line(A, A.nd, i, e_lo, e_hi, x == 0);
+      const Fr e = at_node(e_lo, fe_sub(e_hi, e_lo), x);
+      acc[0] = fe_add(acc[0], fe_mul(e, eval_summand(P, sm)));
+    }
+    // Reduce over threads of the same node: strides that are multiples of 4.
+    red[threadIdx.x] = acc[0];
+    __syncthreads();
+    for (int off = blockDim.x / 2; off >= 4; off >>= 1) {
+      if (threadIdx.x < (unsigned)off) red[threadIdx.x] = fe_add(red[threadIdx.x], red[threadIdx.x + off]);
+      __syncthreads();
+    }
+    if (threadIdx.x < 4) st_fe(&partials[(size_t)blockIdx.x * 4 + threadIdx.x], red[threadIdx.x]);
+    __syncthreads();
+  } else {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < A.npairs; i += stride) {
     Fr lo, hi;
     for (int k = 0; k < A.nd; ++k) {
@@ -95,6 +139,7 @@ __global__ void __launch_bounds__(kRoundThreads) k_round(RoundArgs A, DevProgram
     }
     if (threadIdx.x == 0) st_fe(&partials[(size_t)blockIdx.x * 4 + x], red[0]);
     __syncthreads();
+  }
   }
   // The last block to finish adds every block's partials (the partials are
   // published before the ticket is taken) and re-arms the counter.
@@ -257,7 +302,7 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
   Fr* d_out = c.scratch[S_RESULT].as<Fr>(4);
   unsigned* done = c.scratch[S_ROUND].as<unsigned>(1);
   APG_CUDA(cudaMemsetAsync(done, 0, sizeof(unsigned), c.stream));
-  F* v = reinterpret_cast<F*>(c.host_pinned());
+  F* sums = reinterpret_cast<F*>(c.host_pinned());
   DevProgram P = prog;
   P.cached_slot0 = n_val;
 
@@ -281,13 +326,17 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
     A.done = done;
     A.out = d_out;
     VirtualRound V = virtual_round(point, n);
-    const int blocks = (int)std::min<size_t>((A.npairs + threads - 1) / threads, (size_t)max_blocks);
+    // Rounds too small to fill the device evaluate the four nodes of a pair
+    // on four threads.
+    A.xsplit = A.npairs * 4 <= (size_t)threads * max_blocks ? 1 : 0;
+    const size_t work = A.xsplit ? A.npairs * 4 : A.npairs;
+    const int blocks = (int)std::min<size_t>((work + threads - 1) / threads, (size_t)max_blocks);
     cudaEvent_t t0 = c.timer_begin();
     launch(c, k_round, blocks, threads, smem, A, P, V, partials);
     c.timer_end(APG_TIMER_SUMCHECK_ROUND, t0);
-    APG_CUDA(cudaMemcpyAsync(v, d_out, 128, cudaMemcpyDeviceToHost, c.stream));
+    APG_CUDA(cudaMemcpyAsync(sums, d_out, 128, cudaMemcpyDeviceToHost, c.stream));
     APG_CUDA(cudaStreamSynchronize(c.stream));
-    auto g = host::cubic_through(v);
+    auto g = host::cubic_through(sums);
     tr.absorb(host::T_SUMCHECK_ROUND, g.data(), 4);
     chal = tr.challenge(host::T_SUMCHECK_CHALLENGE);
     rounds.push_back(g);

@@ -328,11 +328,14 @@ def run_profile_shard(args, ctx, torch, dev):
 
     for _ in range(args.warmup):
         once(False)
+    ctx.set_timing(True)
     for _ in range(args.steps):
         once(True)
     out = {k: v * 1e3 / args.steps for k, v in phases.items()}
+    timers = {name: ctx.timer(i) for i, name in enumerate(["msm_accumulate", "msm_total", "sumcheck_round",
+                                                            "gkr_forward", "mercury_pass"])}
     print(json.dumps({"case": "shard", "log2n": n, "cols": args.cols, "ms_per_phase": out,
-                      "ms_total": sum(out.values())}), flush=True)
+                      "ms_total": sum(out.values()), "timers_ms_launches": timers}), flush=True)
     ctx.close()
     return 0
 

@@ -102,8 +102,9 @@ int apg_srs_prepare(apg_ctx* ctx, int cbits);
  * the n_sample device scalars (Fr in memory, drawn like the columns to be
  * committed) with every candidate width (bits, 2..20; widths below 12 only
  * up to 2^16 points), building the window tables it needs, and keep the
- * fastest for this context's later commits and openings (shared contexts and
- * lanes inherit it). chosen_out (nullable) receives max_log2n - min_log2n + 1
+ * fastest for this context's later commits (shared contexts and lanes inherit
+ * it; openings keep the default widths, their quotient polynomials being
+ * uniformly random). chosen_out (nullable) receives max_log2n - min_log2n + 1
  * widths, 0 where a class exceeds the sample or the SRS. */
 int apg_msm_autotune(apg_ctx* ctx, const void* d_sample, size_t n_sample, int min_log2n, int max_log2n,
                      const int* cands, size_t n_cands, int* chosen_out);
