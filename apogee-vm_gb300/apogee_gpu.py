@@ -260,6 +260,33 @@ class Context:
         self._check(lib().apg_commit_u32(self._h, arr, ctypes.c_size_t(num_vars), out))
         return out.raw
 
+    def commit_stack(self, cols, num_vars) -> bytes:
+        """pcs::commit_stack: cols are Fr in-memory byte strings, num_vars one
+        variable count per column (an int applies to every column)."""
+        k = len(cols)
+        nvs = [num_vars] * k if isinstance(num_vars, int) else list(num_vars)
+        ptrs = (ctypes.c_char_p * k)(*cols)
+        nv_arr = (ctypes.c_size_t * max(k, 1))(*nvs)
+        out = ctypes.create_string_buffer(64)
+        self._check(lib().apg_commit_stack(self._h, ptrs, nv_arr, ctypes.c_size_t(k), out))
+        return out.raw
+
+    def commit_stack_device(self, d_ptrs, num_vars) -> bytes:
+        k = len(d_ptrs)
+        nvs = [num_vars] * k if isinstance(num_vars, int) else list(num_vars)
+        arr = (ctypes.c_void_p * max(k, 1))(*d_ptrs)
+        nv_arr = (ctypes.c_size_t * max(k, 1))(*nvs)
+        out = ctypes.create_string_buffer(64)
+        self._check(lib().apg_commit_stack_device(self._h, arr, nv_arr, ctypes.c_size_t(k), out))
+        return out.raw
+
+    def commit_narrow(self, data: bytes, bits: int, num_vars: int) -> bytes:
+        """pcs::commit of a narrow backing: `data` holds 2^num_vars values of
+        `bits` bits (1: bit-packed u64 limbs; 8/16/32: little-endian)."""
+        out = ctypes.create_string_buffer(64)
+        self._check(lib().apg_commit_narrow(self._h, data, ctypes.c_int(bits), ctypes.c_size_t(num_vars), out))
+        return out.raw
+
     def commit_batch(self, cols, num_vars: int) -> list:
         k = len(cols)
         ptrs = (ctypes.c_char_p * k)(*cols)

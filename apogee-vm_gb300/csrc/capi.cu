@@ -280,6 +280,91 @@ int apg_commit_device(apg_ctx* ctx, const void* d_evals, size_t num_vars, uint8_
   return guarded(ctx, [&](Ctx& c) { return commit_common(c, d_evals, true, false, num_vars, out); });
 }
 
+// pcs::commit_stack (crates/pcs/src/lib.rs:256-277): column j over the powers
+// from j * 2^n, all columns into one bucket set, one result. The reference's
+// refusal order: EmptyBatch, SrsTooSmall (k * 2^n powers), MixedColumnSizes.
+static int commit_stack_common(Ctx& c, const void* const* cols, const size_t* num_vars, size_t k, bool on_device,
+                               uint8_t* out) {
+  if (!out) return APG_ERR_INVALID_ARGUMENT;
+  if (k == 0) return APG_ERR_EMPTY_BATCH;
+  if (!cols || !num_vars) return APG_ERR_INVALID_ARGUMENT;
+  if (!c.srs) return APG_ERR_NO_SRS;
+  const size_t width = num_vars[0];
+  if (width > 40) return APG_ERR_SRS_TOO_SMALL;
+  const size_t n = (size_t)1 << width;
+  if (c.srs_n / k < n) {
+    c.last_error = "the SRS holds fewer powers than the stack has slots";
+    return APG_ERR_SRS_TOO_SMALL;
+  }
+  for (size_t j = 0; j < k; ++j) {
+    if (num_vars[j] != width) {
+      c.last_error = "stacked columns of different sizes";
+      return APG_ERR_MIXED_COLUMN_SIZES;
+    }
+    if (!cols[j]) return APG_ERR_INVALID_ARGUMENT;
+  }
+  const SrsTable* t = srs_table_for(c, n * k);
+  if (!t) throw Error(APG_ERR_INTERNAL, "no SRS window table");
+  std::vector<const void*> ptrs(cols, cols + k);
+  if (!on_device) {
+    uint8_t* buf = c.scratch[S_SCALARS].as<uint8_t>(32 * n * k);
+    for (size_t j = 0; j < k; ++j) {
+      APG_CUDA(cudaMemcpyAsync(buf + 32 * n * j, cols[j], 32 * n, cudaMemcpyHostToDevice, c.stream));
+      ptrs[j] = buf + 32 * n * j;
+    }
+  }
+  std::vector<size_t> lens(k, n), offs(k);
+  for (size_t j = 0; j < k; ++j) offs[j] = j * n;
+  MsmBatchOpts o;
+  o.offs = offs.data();
+  o.stack = true;
+  uint8_t* d_out = c.scratch[S_RESULT].as<uint8_t>(64);
+  msm_multi(c, nullptr, t, ptrs.data(), lens.data(), k, false, false, d_out, o);
+  APG_CUDA(cudaMemcpyAsync(out, d_out, 64, cudaMemcpyDeviceToHost, c.stream));
+  c.check_flags();
+  return APG_OK;
+}
+
+int apg_commit_stack(apg_ctx* ctx, const uint8_t* const* cols, const size_t* num_vars, size_t k, uint8_t out[64]) {
+  return guarded(ctx, [&](Ctx& c) {
+    return commit_stack_common(c, (const void* const*)cols, num_vars, k, false, out);
+  });
+}
+
+int apg_commit_stack_device(apg_ctx* ctx, const void* const* d_cols, const size_t* num_vars, size_t k,
+                            uint8_t out[64]) {
+  return guarded(ctx, [&](Ctx& c) { return commit_stack_common(c, d_cols, num_vars, k, true, out); });
+}
+
+int apg_commit_narrow(apg_ctx* ctx, const void* vals, int bits, size_t num_vars, uint8_t out[64]) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (!out || !vals || (bits != 1 && bits != 8 && bits != 16 && bits != 32)) return (int)APG_ERR_INVALID_ARGUMENT;
+    if (!mercury_num_vars_ok(num_vars)) {
+      c.last_error = "unsupported num_vars";
+      return (int)APG_ERR_UNSUPPORTED_NUM_VARS;
+    }
+    if (!c.srs) return (int)APG_ERR_NO_SRS;
+    const size_t n = (size_t)1 << num_vars;
+    if (c.srs_n < n) {
+      c.last_error = "the SRS holds fewer powers than the column has evaluations";
+      return (int)APG_ERR_SRS_TOO_SMALL;
+    }
+    const size_t bytes = bits == 1 ? 8 * ((n + 63) / 64) : n * (size_t)bits / 8;
+    void* buf = c.scratch[S_SCALARS].get(bytes);
+    APG_CUDA(cudaMemcpyAsync(buf, vals, bytes, cudaMemcpyHostToDevice, c.stream));
+    const SrsTable* t = commit_table(c, n);
+    if (!t) throw Error(APG_ERR_INTERNAL, "no SRS window table");
+    const void* ptr = buf;
+    MsmBatchOpts o;
+    o.bits = bits;
+    uint8_t* d_out = c.scratch[S_RESULT].as<uint8_t>(64);
+    msm_multi(c, nullptr, t, &ptr, &n, 1, true, false, d_out, o);
+    APG_CUDA(cudaMemcpyAsync(out, d_out, 64, cudaMemcpyDeviceToHost, c.stream));
+    c.check_flags();
+    return (int)APG_OK;
+  });
+}
+
 // The context's second lane, borrowing its SRS and every window table built
 // so far (refreshed per batch so the lane never builds a table of its own).
 static Ctx& lane_of(Ctx& c) {

@@ -213,8 +213,14 @@ void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* 
 // k MSMs over the same bases (lens[j] scalars each, device pointers); result
 // j is written to d_out + 64 * j. Columns are processed in groups that share
 // one sort, one accumulation and one bucket reduction.
+struct MsmBatchOpts {
+  const size_t* offs = nullptr;  // first base of each column (nullable: all 0)
+  bool stack = false;            // one result: the sum of every column's MSM
+  int bits = 32;                 // width of small scalars: 32, 16, 8 or 1 (bit-packed u64)
+};
 void msm_multi(Ctx& c, const Affine* bases, const SrsTable* table, const void* const* scalars, const size_t* lens,
-               size_t k, bool small_scalars, bool scalars_canonical, uint8_t* d_out);
+               size_t k, bool small_scalars, bool scalars_canonical, uint8_t* d_out,
+               const MsmBatchOpts& o = MsmBatchOpts());
 const SrsTable* srs_table(Ctx& c, int cbits, size_t need);
 // The table an MSM of the first n SRS powers reads: 8-bit windows up to 2^14
 // points (a cheap bucket reduction), 16-bit windows below kWideTableMin and

@@ -485,7 +485,24 @@ constexpr int kMaxCols = 32;
 struct MsmCols {
   const void* s[kMaxCols];
   uint32_t len[kMaxCols];
+  uint32_t off[kMaxCols];  // first base of the column (a stack's slot j starts at j * 2^n)
+  int shared;              // 1: every column feeds one bucket set (one result, the sum)
+  int bits;                // small scalars: 32, 16, 8 or 1 (bit-packed in u64 limbs)
 };
+
+// Scalar i of a small-scalar column of the given width.
+__device__ __forceinline__ uint32_t small_scalar(const void* col, uint32_t i, int bits) {
+  switch (bits) {
+    case 1:
+      return (uint32_t)((reinterpret_cast<const uint64_t*>(col)[i >> 6] >> (i & 63)) & 1u);
+    case 8:
+      return reinterpret_cast<const uint8_t*>(col)[i];
+    case 16:
+      return reinterpret_cast<const uint16_t*>(col)[i];
+    default:
+      return reinterpret_cast<const uint32_t*>(col)[i];
+  }
+}
 
 // Digits of one scalar, counted (SCATTER = false) or placed (SCATTER = true).
 // Lanes of a warp that hit the same bucket share one atomic: the leader adds
@@ -507,7 +524,7 @@ __global__ void __launch_bounds__(256) k_digits(MsmCols cols, int c, int windows
   for (int k = 0; k < 8; ++k) limbs[k] = 0;
   if (live) {
     if (SMALL) {
-      limbs[0] = reinterpret_cast<const uint32_t*>(cols.s[col])[i];
+      limbs[0] = small_scalar(cols.s[col], i, cols.bits);
     } else {
       Fr s = ld_fe(reinterpret_cast<const Fr*>(cols.s[col]) + i);
       if (!SCATTER && !fe_lt_mod<FrConsts>(s.v)) raise_flag(flags, DEV_NONCANONICAL);
@@ -519,7 +536,8 @@ __global__ void __launch_bounds__(256) k_digits(MsmCols cols, int c, int windows
   const uint32_t K = 1u << (c - 1);
   const uint32_t mask = (1u << c) - 1;
   const uint32_t spaces = precomp ? 1u : (uint32_t)windows;
-  const uint32_t key0 = col * spaces * K;
+  const uint32_t key0 = cols.shared ? 0u : col * spaces * K;
+  const uint32_t base_i = cols.off[col] + i;
   uint32_t carry = 0;
   for (int w = 0; w < windows; ++w) {
     const int off = w * c;
@@ -554,7 +572,7 @@ __global__ void __launch_bounds__(256) k_digits(MsmCols cols, int c, int windows
         uint32_t base = 0;
         if ((int)lane == leader) base = atomicAdd(&cursor[key], (uint32_t)__popc(peers));
         base = __shfl_sync(peers, base, leader);
-        const uint32_t idx = precomp ? (uint32_t)w * tab_n + i : i;
+        const uint32_t idx = precomp ? (uint32_t)w * tab_n + base_i : base_i;
         sorted[base + (uint32_t)__popc(peers & ((1u << lane) - 1u))] = (neg << 31) | idx;
       } else if ((int)lane == leader) {
         atomicAdd(&cursor[key], (uint32_t)__popc(peers));
@@ -688,6 +706,32 @@ __global__ void k_finish_cols(const Xyzz* tsum, int levels, int spaces_total, in
   for (int k = 0; k < 8; ++k) {
     o[k] = x.v[k];
     o[8 + k] = y.v[k];
+  }
+}
+
+// out64 = the sum of m canonical affine points in64[0..m) (a stack whose
+// columns took more than one group).
+__global__ void k_add_points(const uint32_t* in64, int m, uint32_t* out64) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  Xyzz acc = xyzz_inf();
+  for (int j = 0; j < m; ++j) {
+    Affine a;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      a.x.v[k] = in64[16 * j + k];
+      a.y.v[k] = in64[16 * j + 8 + k];
+    }
+    if (aff_is_inf(a)) continue;
+    a.x = fe_to_mont(a.x);
+    a.y = fe_to_mont(a.y);
+    acc = xyzz_add(acc, xyzz_from_affine(a));
+  }
+  const Affine r = xyzz_to_affine(acc);
+  const Fq x = fe_from_mont(r.x), y = fe_from_mont(r.y);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    out64[k] = x.v[k];
+    out64[8 + k] = y.v[k];
   }
 }
 
@@ -869,7 +913,8 @@ void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols
                const MsmPlan& p, bool small_scalars, bool scalars_canonical, uint8_t* d_out) {
   const uint32_t K = 1u << (p.c - 1);
   const int spaces_per_col = p.precomp ? 1 : p.windows;
-  const int S = spaces_per_col * ncols;
+  const int nout = cols.shared ? 1 : ncols;  // results: one per column, or the stack's sum
+  const int S = spaces_per_col * nout;
   const size_t nbins = (size_t)S * K;
   size_t emax = 0;
   for (int j = 0; j < ncols; ++j) emax += (size_t)p.windows * cols.len[j];
@@ -960,7 +1005,7 @@ void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols
     lvl_in = outR;
     M = G;
   }
-  launch(c, k_finish_cols, blocks_for<int>(ncols, 32), 32, 0, (const Xyzz*)tsum, levels, S, spaces_per_col, ncols,
+  launch(c, k_finish_cols, blocks_for<int>(nout, 32), 32, 0, (const Xyzz*)tsum, levels, S, spaces_per_col, nout,
          fan_log, p.c, (uint32_t*)d_out);
   c.timer_end(APG_TIMER_MSM_TOTAL, t_total);
 }
@@ -968,7 +1013,12 @@ void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols
 }  // namespace
 
 void msm_multi(Ctx& c, const Affine* bases, const SrsTable* table, const void* const* scalars, const size_t* lens,
-               size_t k, bool small_scalars, bool scalars_canonical, uint8_t* d_out) {
+               size_t k, bool small_scalars, bool scalars_canonical, uint8_t* d_out, const MsmBatchOpts& o) {
+  // A stack sums its columns: every group writes one partial result, added
+  // at the end when there is more than one.
+  uint8_t* partial = nullptr;
+  size_t ngroups = 0;
+  if (o.stack) partial = c.scratch[S_TMP7].as<uint8_t>(64 * ((k + kMaxCols - 1) / kMaxCols + k));
   size_t j = 0;
   while (j < k) {
     // Grow the group while the plan, the bucket range and the sorted list fit.
@@ -994,9 +1044,19 @@ void msm_multi(Ctx& c, const Affine* bases, const SrsTable* table, const void* c
     for (size_t t = 0; t < g; ++t) {
       cols.s[t] = scalars[j + t];
       cols.len[t] = (uint32_t)lens[j + t];
+      cols.off[t] = o.offs ? (uint32_t)o.offs[j + t] : 0u;
     }
-    msm_group(c, bases, table, cols, (int)g, nmax, p, small_scalars, scalars_canonical, d_out + 64 * j);
+    cols.shared = o.stack ? 1 : 0;
+    cols.bits = o.bits;
+    uint8_t* dst = o.stack ? partial + 64 * ngroups : d_out + 64 * j;
+    msm_group(c, bases, table, cols, (int)g, nmax, p, small_scalars, scalars_canonical, dst);
+    ++ngroups;
     j += g;
+  }
+  if (o.stack) {
+    if (ngroups == 0) APG_CUDA(cudaMemsetAsync(d_out, 0, 64, c.stream));
+    else if (ngroups == 1) APG_CUDA(cudaMemcpyAsync(d_out, partial, 64, cudaMemcpyDeviceToDevice, c.stream));
+    else launch(c, k_add_points, 1, 32, 0, (const uint32_t*)partial, (int)ngroups, (uint32_t*)d_out);
   }
 }
 

@@ -159,6 +159,24 @@ int apg_commit_device(apg_ctx* ctx, const void* d_evals, size_t num_vars, uint8_
 /* As apg_commit_batch over device-resident columns; the k MSMs run back to
  * back on the context's stream and the call returns once all are done. */
 int apg_commit_batch_device(apg_ctx* ctx, const void* const* d_cols, size_t k, size_t num_vars, uint8_t* out);
+/* pcs::commit_stack (crates/pcs/src/lib.rs:256-277): the commitment of the
+ * stack whose evaluations [j*2^n, (j+1)*2^n) are column j, read as
+ * coefficients over the resident SRS (the stack is never materialised: column
+ * j is an MSM over the powers from j*2^n, every column into one bucket set).
+ * num_vars[j] is column j's variable count, n = num_vars[0]; columns are host
+ * Fr in memory. Errors, in the reference's order: APG_ERR_EMPTY_BATCH
+ * (k = 0), APG_ERR_SRS_TOO_SMALL (fewer than k*2^n powers),
+ * APG_ERR_MIXED_COLUMN_SIZES. */
+int apg_commit_stack(apg_ctx* ctx, const uint8_t* const* cols, const size_t* num_vars, size_t k, uint8_t out[64]);
+/* As apg_commit_stack with the columns in device memory. */
+int apg_commit_stack_device(apg_ctx* ctx, const void* const* d_cols, const size_t* num_vars, size_t k,
+                            uint8_t out[64]);
+/* pcs::commit of a narrow backing (column_msm, crates/pcs/src/lib.rs:280-298):
+ * 2^num_vars unsigned values of `bits` bits (8, 16 or 32: little-endian
+ * integers; 1: bit-packed in u64 limbs, value i at bit i % 64 of limb i / 64,
+ * like PolyBacking::U1) committed through the small-scalar path, never lifted
+ * to Fr; host memory. Errors as apg_commit. */
+int apg_commit_narrow(apg_ctx* ctx, const void* vals, int bits, size_t num_vars, uint8_t out[64]);
 
 /* ---- Mercury opening (crates/pcs/src/lib.rs) ----------------------------- */
 

@@ -290,3 +290,55 @@ def test_autotune_choice_keeps_commitments(ctx):
         for c, cm in zip(cols, cms):
             assert cm == O.g1_mul(O.G1_GEN, _f_tau(c, tau))
         assert ctx.commit(A.to_mont_bytes(cols[0]), k) == cms[0]
+
+
+def test_commit_stack_known_tau(ctx):
+    """pcs::commit_stack: the stack's commitment is [F(tau)]G for F the
+    concatenation of the columns, read as coefficients; 40 columns of 4 take
+    two groups whose partial sums are added; the reference's refusal order."""
+    import apogee_gpu as A
+
+    tau = 0x57AC
+    ctx.srs_generate(tau, 1 << 10)
+    rng = random.Random(5)
+    for nv, k, kinds in ((8, 3, ("mixed", "uniform", "bits")), (2, 40, ("uniform", "u32", "zeros", "ones"))):
+        cols = [_column(kinds[j % len(kinds)], 1 << nv, rng) for j in range(k)]
+        concat = [v for c in cols for v in c]
+        cm = ctx.commit_stack([A.to_mont_bytes(c) for c in cols], nv)
+        assert cm == O.g1_mul(O.G1_GEN, _f_tau(concat, tau)), (nv, k)
+    one = A.to_mont_bytes([1, 2, 3, 4])
+    with pytest.raises(A.PcsError) as e:
+        ctx.commit_stack([], 2)
+    assert e.value.variant == "EmptyBatch"
+    with pytest.raises(A.PcsError) as e:  # needs 3 * 2^9 > 2^10 powers: checked before the sizes
+        ctx.commit_stack([one, one, one], [9, 2, 2])
+    assert e.value.variant == "SrsTooSmall"
+    with pytest.raises(A.PcsError) as e:
+        ctx.commit_stack([one, A.to_mont_bytes([1] * 8)], [2, 3])
+    assert e.value.variant == "MixedColumnSizes"
+
+
+@pytest.mark.parametrize("bits", [1, 8, 16, 32])
+def test_commit_narrow_backings(ctx, bits):
+    """A narrow column commits through the small-scalar path, never lifted to
+    Fr, and equals the commitment of the same values as Fr: [f(tau)]G."""
+    import struct
+
+    import apogee_gpu as A
+
+    tau = 0xB175 + bits
+    nv = 12
+    n = 1 << nv
+    ctx.srs_generate(tau, n)
+    rng = random.Random(bits)
+    vals = [rng.getrandbits(bits) for _ in range(n)]
+    if bits == 1:
+        limbs = [0] * (n // 64)
+        for i, v in enumerate(vals):
+            limbs[i // 64] |= v << (i % 64)
+        data = struct.pack(f"<{len(limbs)}Q", *limbs)
+    else:
+        data = struct.pack({8: f"<{n}B", 16: f"<{n}H", 32: f"<{n}I"}[bits], *vals)
+    cm = ctx.commit_narrow(data, bits, nv)
+    assert cm == O.g1_mul(O.G1_GEN, _f_tau(vals, tau))
+    assert cm == ctx.commit(A.to_mont_bytes(vals), nv)
