@@ -222,7 +222,8 @@ constexpr int kFwdThreads = 64;
 __global__ void __launch_bounds__(kFwdThreads) k_forward(DevProgram P, int w, int nv, VirtualKinds vk,
                                                          const Fr* const* cols, size_t rows, int halving,
                                                          int width, Fr* out) {
-  extern __shared__ uint32_t sm[];
+  extern __shared__ uint32_t sm_raw[];
+  const Slots sm = thread_slots(sm_raw);
   size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (y >= rows) return;
   for (int x = 0; x < w; ++x) {
@@ -291,7 +292,7 @@ GkrValues* gkr_forward_impl(Ctx& c, const uint8_t* blob, size_t blob_len, const 
     APG_CUDA(cudaMemcpyAsync(d_cols, cols.data(), sizeof(Fr*) * w, cudaMemcpyHostToDevice, c.stream));
     const size_t slots_n = (size_t)P.cached_slot0 + L.cached.size();
     int threads = kFwdThreads;
-    while (threads > 32 && std::max<size_t>(slots_n, 1) * 32 * threads > 200 * 1024) threads /= 2;
+    while (threads > 8 && std::max<size_t>(slots_n, 1) * 32 * threads > 200 * 1024) threads /= 2;
     const size_t smem = std::max<size_t>(slots_n, 1) * 32 * threads;
     if (smem > 200 * 1024) throw Error(APG_ERR_BAD_CIRCUIT, "gate list too wide for one thread block");
     APG_CUDA(cudaFuncSetAttribute(k_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));

@@ -16,6 +16,7 @@ namespace apg {
 namespace {
 
 constexpr int kRoundThreads = 128;
+constexpr int kWarpModeGates = 16;  // weighted gates from which a list goes one pair per warp
 
 struct RoundArgs {
   int nd;                    // data tables (eq is separate)
@@ -66,8 +67,43 @@ __device__ __forceinline__ Fr at_node(const Fr& lo, const Fr& step, int x) {
   return v;
 }
 
+// After every block has published its 4 partial sums: the last block to
+// finish (it takes the last ticket) adds them all into A.out and re-arms the
+// counter for the next round.
+__device__ __forceinline__ void round_total(const RoundArgs& A, const Fr* partials, Fr* red) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(A.done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int x = 0; x < 4; ++x) {
+    Fr a = fe_zero<FrConsts>();
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+      const uint4* q = reinterpret_cast<const uint4*>(&partials[(size_t)b * 4 + x]);
+      const uint4 u0 = __ldcg(q), u1 = __ldcg(q + 1);
+      Fr v;
+      v.v[0] = u0.x, v.v[1] = u0.y, v.v[2] = u0.z, v.v[3] = u0.w;
+      v.v[4] = u1.x, v.v[5] = u1.y, v.v[6] = u1.z, v.v[7] = u1.w;
+      a = fe_add(a, v);
+    }
+    red[threadIdx.x] = a;
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+      if (threadIdx.x < (unsigned)off) red[threadIdx.x] = fe_add(red[threadIdx.x], red[threadIdx.x + off]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) st_fe(&A.out[x], red[0]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *A.done = 0;
+}
+
 __global__ void __launch_bounds__(kRoundThreads) k_round(RoundArgs A, DevProgram P, VirtualRound V, Fr* partials) {
-  extern __shared__ uint32_t sm[];
+  extern __shared__ uint32_t sm_raw[];
+  const Slots sm = thread_slots(sm_raw);
   __shared__ Fr red[kRoundThreads];
   Fr acc[4];
 #pragma unroll
@@ -141,36 +177,72 @@ __global__ void __launch_bounds__(kRoundThreads) k_round(RoundArgs A, DevProgram
     __syncthreads();
   }
   }
-  // The last block to finish adds every block's partials (the partials are
-  // published before the ticket is taken) and re-arms the counter.
-  __shared__ bool last;
-  if (threadIdx.x == 0) {
-    __threadfence();
-    last = atomicAdd(A.done, 1u) == gridDim.x - 1;
+  round_total(A, partials, red);
+}
+
+// Wide gate lists (many gates, many tables): one warp per pair. The pair's
+// tables sit once in the warp's shared slots (values, then cached entries,
+// then steps, then eq's value and step), written lane-parallel; at each node
+// the lanes split the gates and the warp adds their weighted values.
+__global__ void __launch_bounds__(kRoundThreads) k_round_warp(RoundArgs A, DevProgram P, VirtualRound V,
+                                                              Fr* partials) {
+  extern __shared__ uint32_t sm_raw[];
+  __shared__ Fr red[kRoundThreads];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int per_warp = A.slots_step0 + A.n_val_slots + 2;
+  const Slots S{sm_raw + (size_t)warp * per_warp * 8, 1};
+  const int eq_slot = per_warp - 2;
+  Fr acc[4];
+#pragma unroll
+  for (int x = 0; x < 4; ++x) acc[x] = fe_zero<FrConsts>();
+  const size_t wstride = (size_t)gridDim.x * nwarps;
+  for (size_t i = (size_t)blockIdx.x * nwarps + warp; i < A.npairs; i += wstride) {
+    Fr lo, hi;
+    for (int k = lane; k <= A.nd; k += 32) {
+      load_line(A, k, i, lo, hi);
+      sm_st(S, k < A.nd ? k : eq_slot, lo);
+      sm_st(S, k < A.nd ? A.slots_step0 + k : eq_slot + 1, fe_sub(hi, lo));
+    }
+    for (int v = lane; v < A.nv; v += 32) {
+      virtual_line_dev(V, A.vkinds[v], i, lo, hi);  // hi is the step here
+      sm_st(S, A.nd + v, lo);
+      sm_st(S, A.slots_step0 + A.nd + v, hi);
+    }
+    __syncwarp();
+    for (int x = 0; x < 4; ++x) {
+      if (lane == 0)
+        for (int g = 0; g < P.n_cached; ++g) sm_st(S, P.cached_slot0 + g, eval_gate_dev(P, g, S));
+      __syncwarp();
+      Fr part = fe_zero<FrConsts>();
+      for (int j = lane; j < P.n_weighted; j += 32)
+        part = fe_add(part, cmul_coef(P.weights, j, P.weight_ones, eval_gate_dev(P, P.n_cached + j, S)));
+      for (int off = 16; off > 0; off >>= 1) {
+        Fr o;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) o.v[w] = __shfl_xor_sync(0xffffffffu, part.v[w], off);
+        part = fe_add(part, o);
+      }
+      if (lane == 0) acc[x] = fe_add(acc[x], fe_mul(sm_ld(S, eq_slot), part));
+      __syncwarp();
+      if (x < 3) {
+        for (int k = lane; k < A.n_val_slots; k += 32) sm_st(S, k, fe_add(sm_ld(S, k), sm_ld(S, A.slots_step0 + k)));
+        if (lane == 0) sm_st(S, eq_slot, fe_add(sm_ld(S, eq_slot), sm_ld(S, eq_slot + 1)));
+      }
+      __syncwarp();
+    }
   }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
+  // Per node: the block's warps' sums (lane 0 of each), then the cross-block total.
   for (int x = 0; x < 4; ++x) {
-    Fr a = fe_zero<FrConsts>();
-    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
-      const uint4* q = reinterpret_cast<const uint4*>(&partials[(size_t)b * 4 + x]);
-      const uint4 u0 = __ldcg(q), u1 = __ldcg(q + 1);
-      Fr v;
-      v.v[0] = u0.x, v.v[1] = u0.y, v.v[2] = u0.z, v.v[3] = u0.w;
-      v.v[4] = u1.x, v.v[5] = u1.y, v.v[6] = u1.z, v.v[7] = u1.w;
-      a = fe_add(a, v);
-    }
-    red[threadIdx.x] = a;
+    red[threadIdx.x] = lane == 0 ? acc[x] : fe_zero<FrConsts>();
     __syncthreads();
-    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
-      if (threadIdx.x < (unsigned)off) red[threadIdx.x] = fe_add(red[threadIdx.x], red[threadIdx.x + off]);
-      __syncthreads();
+    if (threadIdx.x == 0) {
+      Fr a = fe_zero<FrConsts>();
+      for (int w = 0; w < nwarps; ++w) a = fe_add(a, red[32 * w]);
+      st_fe(&partials[(size_t)blockIdx.x * 4 + x], a);
     }
-    if (threadIdx.x == 0) st_fe(&A.out[x], red[0]);
     __syncthreads();
   }
-  if (threadIdx.x == 0) *A.done = 0;
+  round_total(A, partials, red);
 }
 
 // Tables of length 2 -> their bound value (the last round's fold).
@@ -292,13 +364,22 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
   const int slots = 2 * n_val + n_cached;
   // Wide gate lists get narrower blocks (a power of two, for the reduction
   // tree) so that every thread's slots still fit in shared memory.
+  // (Down to 8 threads a block for the widest lists, e.g. 130-column ones.)
   int threads = kRoundThreads;
-  while (threads > 32 && (size_t)std::max(slots, 1) * 32 * threads > 200 * 1024) threads /= 2;
+  while (threads > 8 && (size_t)std::max(slots, 1) * 32 * threads > 200 * 1024) threads /= 2;
   const size_t smem = (size_t)std::max(slots, 1) * 32 * threads;
-  if (smem > 200 * 1024) throw Error(APG_ERR_BAD_CIRCUIT, "gate list too wide for one thread block");
+  // Lists of many gates go one pair per warp (k_round_warp): the pair's
+  // tables are stored once for the warp instead of once per thread.
+  const bool warp_mode = prog.n_weighted >= kWarpModeGates;
+  if (!warp_mode && smem > 200 * 1024) throw Error(APG_ERR_BAD_CIRCUIT, "gate list too wide for one thread block");
   APG_CUDA(cudaFuncSetAttribute(k_round, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  const int max_blocks = c.sm_count * 8;
-  Fr* partials = c.scratch[S_TMP6].as<Fr>((size_t)max_blocks * 4);
+  const int max_blocks = c.sm_count * 8 * (kRoundThreads / threads);  // the same thread count in smaller blocks
+  const int warp_slots = n_val + n_cached + n_val + 2;
+  const size_t warp_smem = (size_t)(kRoundThreads / 32) * warp_slots * 32;
+  if (warp_mode && warp_smem > 200 * 1024) throw Error(APG_ERR_BAD_CIRCUIT, "gate list too wide for one thread block");
+  if (warp_mode) APG_CUDA(cudaFuncSetAttribute(k_round_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  const int warp_max_blocks = c.sm_count * 16;
+  Fr* partials = c.scratch[S_TMP6].as<Fr>((size_t)std::max(max_blocks, warp_max_blocks) * 4);
   Fr* d_out = c.scratch[S_RESULT].as<Fr>(4);
   unsigned* done = c.scratch[S_ROUND].as<unsigned>(1);
   APG_CUDA(cudaMemsetAsync(done, 0, sizeof(unsigned), c.stream));
@@ -330,9 +411,13 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
     // on four threads.
     A.xsplit = A.npairs * 4 <= (size_t)threads * max_blocks ? 1 : 0;
     const size_t work = A.xsplit ? A.npairs * 4 : A.npairs;
-    const int blocks = (int)std::min<size_t>((work + threads - 1) / threads, (size_t)max_blocks);
+    const int blocks = warp_mode
+                           ? (int)std::min<size_t>((A.npairs + kRoundThreads / 32 - 1) / (kRoundThreads / 32),
+                                                   (size_t)warp_max_blocks)
+                           : (int)std::min<size_t>((work + threads - 1) / threads, (size_t)max_blocks);
     cudaEvent_t t0 = c.timer_begin();
-    launch(c, k_round, blocks, threads, smem, A, P, V, partials);
+    if (warp_mode) launch(c, k_round_warp, blocks, kRoundThreads, warp_smem, A, P, V, partials);
+    else launch(c, k_round, blocks, threads, smem, A, P, V, partials);
     c.timer_end(APG_TIMER_SUMCHECK_ROUND, t0);
     APG_CUDA(cudaMemcpyAsync(sums, d_out, 128, cudaMemcpyDeviceToHost, c.stream));
     APG_CUDA(cudaStreamSynchronize(c.stream));

@@ -8,9 +8,11 @@
 // (crates/sumcheck/src/lib.rs:109-169) is the one-gate list
 // `Quadratic { 0, linear terms, product terms }` with weight 1.
 //
-// Slots hold one Fr each, word-major across the block's threads so that a
-// warp's 32-bit accesses fall in distinct banks: word w of slot s of thread t
-// sits at smem[(s * 8 + w) * blockDim.x + t].
+// Slots hold one Fr each in shared memory (Slots below): either a thread's
+// own, word-major across the block's threads so that a warp's 32-bit accesses
+// fall in distinct banks (word w of slot s of thread t at
+// smem[(s * 8 + w) * blockDim.x + t]), or one set a whole warp shares and
+// reads at once (wide gate lists, one pair per warp).
 #pragma once
 #include "field.cuh"
 
@@ -49,18 +51,27 @@ struct DevProgram {
   uint32_t weight_ones; // bit j: weight j is 1 (lambda^0 always is)
 };
 
-__device__ __forceinline__ Fr sm_ld(const uint32_t* sm, int slot) {
+// One evaluation's slots: word w of slot s at base[(s * 8 + w) * stride].
+// A thread's own slots (thread_slots) interleave with the block's other
+// threads (stride blockDim.x); a warp's shared slots (stride 1) are read by
+// all its lanes at once.
+struct Slots {
+  uint32_t* base;
+  int stride;
+};
+
+__device__ __forceinline__ Slots thread_slots(uint32_t* sm) { return Slots{sm + threadIdx.x, (int)blockDim.x}; }
+
+__device__ __forceinline__ Fr sm_ld(const Slots& S, int slot) {
   Fr r;
-  const int nt = blockDim.x, t = threadIdx.x;
 #pragma unroll
-  for (int w = 0; w < 8; ++w) r.v[w] = sm[(slot * 8 + w) * nt + t];
+  for (int w = 0; w < 8; ++w) r.v[w] = S.base[(slot * 8 + w) * S.stride];
   return r;
 }
 
-__device__ __forceinline__ void sm_st(uint32_t* sm, int slot, const Fr& a) {
-  const int nt = blockDim.x, t = threadIdx.x;
+__device__ __forceinline__ void sm_st(const Slots& S, int slot, const Fr& a) {
 #pragma unroll
-  for (int w = 0; w < 8; ++w) sm[(slot * 8 + w) * nt + t] = a.v[w];
+  for (int w = 0; w < 8; ++w) S.base[(slot * 8 + w) * S.stride] = a.v[w];
 }
 
 __device__ __forceinline__ Fr ld_g(const Fr* p) { return ld_fe(p); }
@@ -77,14 +88,14 @@ __device__ __forceinline__ Fr cmul_coef(const Fr* c, int i, uint32_t ones, const
 
 // Affine form sum_{i<t} c[i] * x_i + c[t], operands ops[0..t); `ones` is
 // the one-mask of c[0..].
-__device__ __forceinline__ Fr affine_form(const uint32_t* sm, const uint16_t* ops, const Fr* c, int t,
+__device__ __forceinline__ Fr affine_form(const Slots& sm, const uint16_t* ops, const Fr* c, int t,
                                           uint32_t ones) {
   Fr acc = ld_g(&c[t]);
   for (int i = 0; i < t; ++i) acc = fe_add(acc, cmul_coef(c, i, ones, sm_ld(sm, ops[i])));
   return acc;
 }
 
-static __device__ __noinline__ Fr eval_gate_dev(const DevProgram& P, int g, const uint32_t* sm) {
+static __device__ __noinline__ Fr eval_gate_dev(const DevProgram& P, int g, const Slots sm) {
   const DevGate G = P.gates[g];
   const uint16_t* ops = P.ops + G.op_off;
   const Fr* c = P.coeffs + G.cf_off;
@@ -122,7 +133,7 @@ static __device__ __noinline__ Fr eval_gate_dev(const DevProgram& P, int g, cons
 }
 
 // Cached entries into their slots, then the weighted sum of the gates.
-__device__ __forceinline__ Fr eval_summand(const DevProgram& P, uint32_t* sm) {
+__device__ __forceinline__ Fr eval_summand(const DevProgram& P, const Slots& sm) {
   for (int g = 0; g < P.n_cached; ++g) sm_st(sm, P.cached_slot0 + g, eval_gate_dev(P, g, sm));
   Fr acc = fe_zero<FrConsts>();
   for (int j = 0; j < P.n_weighted; ++j) {

@@ -255,6 +255,8 @@ def run_profile_case(args):
     ctx = A.Context(local)
     if args.profile_case == "shard":
         return run_profile_shard(args, ctx, torch, dev)
+    if args.profile_case == "family":
+        return run_profile_family(args, ctx, torch, dev)
     if args.profile_case == "open":
         ctx.srs_generate((TAU_SEED * 0x9E3779B97F4A7C15) % A.P_R, 1 << n)
         ctx.srs_prepare()
@@ -336,6 +338,54 @@ def run_profile_shard(args, ctx, torch, dev):
                                                             "gkr_forward", "mercury_pass"])}
     print(json.dumps({"case": "shard", "log2n": n, "cols": args.cols, "ms_per_phase": out,
                       "ms_total": sum(out.values()), "timers_ms_launches": timers}), flush=True)
+    ctx.close()
+    return 0
+
+
+def run_profile_family(args, ctx, torch, dev):
+    """One of the reference's own family circuits (its committed artifact,
+    decoded) over 2^log2n rows of mixed columns: GKR forward + proof."""
+    import apogee_gpu as A
+    import artifact
+    import shard
+
+    path = os.path.join(ROOT, "tests", "golden", "artifacts", args.family + ".bin")
+    with open(path, "rb") as f:
+        art = artifact.decode(f.read())
+    circ = artifact.to_circuit(art, args.log2n)
+    blob = circ.to_blob()
+    rng = random.Random(SEED)
+    slots = sorted({c[1] for L in art["layers"] for grp in ("cached", "producing", "enforcing")
+                    for e in L[grp] for c in e[-1]["coeffs"] if c[0] == "ch"} | {0})
+    ch = {sl: rng.randrange(A.P_R) for sl in slots}
+    cols = shard.device_columns(torch, 1 << args.log2n, circ.n_committed, SEED, dev, ctx)
+    ptrs = [t.data_ptr() for t in cols]
+    phases = {"forward": 0.0, "gkr_prove": 0.0}
+
+    def once(acc):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        v = ctx.gkr_forward(blob, ptrs, ch, on_device=True)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        ctx.gkr_prove(blob, v, ch, A.transcript_init())
+        t2 = time.perf_counter()
+        v.free()
+        if acc:
+            phases["forward"] += t1 - t0
+            phases["gkr_prove"] += t2 - t1
+
+    for _ in range(args.warmup):
+        once(False)
+    ctx.set_timing(True)
+    for _ in range(args.steps):
+        once(True)
+    timers = {name: ctx.timer(i) for i, name in enumerate(["msm_accumulate", "msm_total", "sumcheck_round",
+                                                            "gkr_forward", "mercury_pass"])}
+    print(json.dumps({"case": "family", "circuit": args.family, "log2n": args.log2n,
+                      "committed_columns": circ.n_committed, "gate_lists": circ.depth(),
+                      "ms_per_phase": {k: v * 1e3 / args.steps for k, v in phases.items()},
+                      "timers_ms_launches": timers}), flush=True)
     ctx.close()
     return 0
 
@@ -621,8 +671,9 @@ def main():
     ap.add_argument("--window-bits", type=int, default=0, help="--only-msm: fixed window width instead of autotuning")
     ap.add_argument("--no-shards", dest="shards", action="store_false",
                     help="skip the per-config shard timings and the 207-shard mix / serving run")
-    ap.add_argument("--profile-case", choices=["zerocheck", "gkr", "open", "shard"], default=None,
-                    help="run one lean sumcheck / GKR / opening / whole-shard case for profilers")
+    ap.add_argument("--profile-case", choices=["zerocheck", "gkr", "open", "shard", "family"], default=None,
+                    help="run one lean sumcheck / GKR / opening / whole-shard / family-circuit case for profilers")
+    ap.add_argument("--family", default="add_sub", help="--profile-case family: the committed artifact's name")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

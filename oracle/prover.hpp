@@ -359,8 +359,8 @@ struct Resolved {
     }
   }
   Fr eval(size_t i, const Fr* lower, const Fr* upper, const Fr* virt, const std::vector<Fr>& cache) const {
-    Fr ops[64];
     auto& s = sources[i];
+    std::vector<Fr> ops(s.size() ? s.size() : 1);  // a Linear gate may read a hundred columns
     for (size_t j = 0; j < s.size(); ++j) {
       switch (s[j].first) {
         case LOWER: ops[j] = lower[s[j].second]; break;
@@ -369,7 +369,7 @@ struct Resolved {
         case CACHED: ops[j] = cache[s[j].second]; break;
       }
     }
-    return eval_gate(*gates[i], ops, *ch);
+    return eval_gate(*gates[i], ops.data(), *ch);
   }
   void fill_cache(const Fr* lower, const Fr* upper, const Fr* virt, std::vector<Fr>& cache) const {
     cache.resize(cached);

@@ -1,5 +1,7 @@
 """Extract the golden vectors the tests replay from the reference's committed
-known-answer files.
+known-answer files, and copy the reference's committed circuit artifacts
+(crates/constraints/tests/vectors/*.bin, the family circuits in their
+postcard wire form) byte for byte into tests/golden/artifacts/.
 
 The reference pins its hot path with text fixtures generated against
 arkworks (ark-bn254 0.6) and Plonky3's Poseidon2; this script copies the
@@ -31,8 +33,25 @@ SOURCES = {
 }
 
 
+ARTIFACTS = "crates/constraints/tests/vectors"
+
+
+def copy_artifacts(ref_root: str, out_dir: str) -> None:
+    dst = os.path.join(out_dir, "artifacts")
+    os.makedirs(dst, exist_ok=True)
+    src = os.path.join(ref_root, ARTIFACTS)
+    for name in sorted(os.listdir(src)):
+        if name.endswith(".bin"):
+            with open(os.path.join(src, name), "rb") as f:
+                data = f.read()
+            with open(os.path.join(dst, name), "wb") as f:
+                f.write(data)
+            print(f"artifacts/{name}: {len(data)} bytes")
+
+
 def main(ref_root: str) -> None:
     out_dir = os.path.dirname(os.path.abspath(__file__))
+    copy_artifacts(ref_root, out_dir)
     for name, (rel, kinds, limit) in SOURCES.items():
         src = os.path.join(ref_root, rel)
         with open(src) as f:

@@ -149,3 +149,9 @@ TAG_NAMES = {
     "GLOBAL_STATE_DIGEST": 38, "SHARD_SEED": 39, "SHARD_TS_WINDOW": 40, "GENERIC_TABLE": 41,
     "STACK_CHALLENGE": 42, "FOLD_STATE": 43, "FOLD_WEIGHT": 44, "FOLD_CHILD": 45,
 }
+
+
+def golden_artifacts():
+    """The reference's committed circuit artifacts: {file name: bytes}."""
+    d = os.path.join(GOLDEN, "artifacts")
+    return {f: open(os.path.join(d, f), "rb").read() for f in sorted(os.listdir(d)) if f.endswith(".bin")}

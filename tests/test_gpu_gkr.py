@@ -40,14 +40,14 @@ def oracle_gkr(blob, base_cols, challenges, snap, circuit):
     return p, [t[j * top_n:(j + 1) * top_n] for j in range(top_w)]
 
 
-def run_case(ctx, circuit, seed):
+def run_case(ctx, circuit, seed, slots=(0, 1, 2)):
     import apogee_gpu as A
 
     rng = random.Random(seed)
     n = 1 << circuit.trace_vars
     base = [[rng.choice([0, 1, rng.getrandbits(32), rng.randrange(O.P_R)]) for _ in range(n)]
             for _ in range(circuit.n_committed)]
-    challenges = {0: rng.randrange(O.P_R), 1: rng.randrange(O.P_R), 2: rng.randrange(O.P_R)}
+    challenges = {s: rng.randrange(O.P_R) for s in slots}
     blob = circuit.to_blob()
     snap = A.transcript_append_scalars(A.transcript_init(), 39, [seed])
     values = ctx.gkr_forward(blob, [A.to_mont_bytes(c) for c in base], challenges)
@@ -121,3 +121,18 @@ def test_bad_circuits_are_refused(ctx):
     good.add_layer([C.product(("ch", 9), C.col(0), C.col(0))])
     with pytest.raises(A.ApogeeError):  # slot 9 has no value
         ctx.gkr_forward(good.to_blob(), [A.to_mont_bytes([1] * 8)], {})
+
+
+@pytest.mark.parametrize("name", sorted(O.golden_artifacts()))
+def test_reference_family_circuits(ctx, name):
+    """The reference's own committed circuit artifacts (its family circuits
+    and toy circuits, decoded from their wire form) over 2^6 rows: every
+    gate list, cached entry, virtual table and fraction tree of a real
+    circuit, forward values and proof equal to the oracle's."""
+    import artifact
+
+    art = artifact.decode(O.golden_artifacts()[name])
+    circuit = artifact.to_circuit(art, min(6, art["trace_vars"]))
+    slots = sorted({c[1] for L in art["layers"] for grp in ("cached", "producing", "enforcing")
+                    for e in L[grp] for c in e[-1]["coeffs"] if c[0] == "ch"} | {0})
+    run_case(ctx, circuit, sum(name.encode()), slots)
