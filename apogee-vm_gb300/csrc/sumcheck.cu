@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kRoundThreads) k_round_warp(RoundArgs A, DevPr
   __shared__ Fr red[kRoundThreads];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int per_warp = A.slots_step0 + A.n_val_slots + 2;
-  const Slots S{sm_raw + (size_t)warp * per_warp * 8, 1};
+  const Slots S = warp_slots(sm_raw + (size_t)warp * per_warp * 8, per_warp);
   const int eq_slot = per_warp - 2;
   Fr acc[4];
 #pragma unroll
@@ -446,11 +446,15 @@ void upload_program(Ctx& c, const HostProgram& hp, DevProgram& P, int slot_cap) 
   (void)slot_cap;
   // Mark unit coefficients and weights so the device skips their products.
   std::vector<DevGate> gates = hp.gates;
-  const host::F one = host::fone();
+  const host::F one = host::fone(), minus_one = host::fneg(host::fone()), zero = host::fzero();
   for (auto& g : gates) {
-    g.ones = 0;
-    for (uint32_t i = 0; i < 32 && g.cf_off + i < hp.coeffs.size(); ++i)
-      if (hp.coeffs[g.cf_off + i] == one) g.ones |= 1u << i;
+    g.ones = g.negs = g.zeros = 0;
+    for (uint32_t i = 0; i < 32 && g.cf_off + i < hp.coeffs.size(); ++i) {
+      const host::F& v = hp.coeffs[g.cf_off + i];
+      if (v == one) g.ones |= 1u << i;
+      else if (v == minus_one) g.negs |= 1u << i;
+      else if (v == zero) g.zeros |= 1u << i;
+    }
   }
   P.weight_ones = 0;
   for (size_t j = 0; j < 32 && j < hp.weights.size(); ++j)

@@ -36,6 +36,8 @@ struct DevGate {
   uint32_t op_off;   // first operand slot index in ops[]
   uint32_t cf_off;   // first coefficient in coeffs[]
   uint32_t ones;     // bit i: coefficient cf_off + i is 1 (its product is skipped)
+  uint32_t negs;     // bit i: coefficient cf_off + i is -1 (a negation instead)
+  uint32_t zeros;    // bit i: coefficient cf_off + i is 0 (its term is dropped)
 };
 
 // A resolved list on the device. Gates [0, n_cached) fill the cached slots in
@@ -57,21 +59,28 @@ struct DevProgram {
 // all its lanes at once.
 struct Slots {
   uint32_t* base;
-  int stride;
+  int slot_stride;  // words between consecutive slots
+  int word_stride;  // words between a slot's consecutive words
 };
 
-__device__ __forceinline__ Slots thread_slots(uint32_t* sm) { return Slots{sm + threadIdx.x, (int)blockDim.x}; }
+__device__ __forceinline__ Slots thread_slots(uint32_t* sm) {
+  return Slots{sm + threadIdx.x, 8 * (int)blockDim.x, (int)blockDim.x};
+}
+
+// A warp's shared set of n slots, word-major (word w of slot s at w * n + s),
+// so lanes reading different slots hit different banks.
+__device__ __forceinline__ Slots warp_slots(uint32_t* base, int n) { return Slots{base, 1, n}; }
 
 __device__ __forceinline__ Fr sm_ld(const Slots& S, int slot) {
   Fr r;
 #pragma unroll
-  for (int w = 0; w < 8; ++w) r.v[w] = S.base[(slot * 8 + w) * S.stride];
+  for (int w = 0; w < 8; ++w) r.v[w] = S.base[slot * S.slot_stride + w * S.word_stride];
   return r;
 }
 
 __device__ __forceinline__ void sm_st(const Slots& S, int slot, const Fr& a) {
 #pragma unroll
-  for (int w = 0; w < 8; ++w) S.base[(slot * 8 + w) * S.stride] = a.v[w];
+  for (int w = 0; w < 8; ++w) S.base[slot * S.slot_stride + w * S.word_stride] = a.v[w];
 }
 
 __device__ __forceinline__ Fr ld_g(const Fr* p) { return ld_fe(p); }
@@ -86,12 +95,23 @@ __device__ __forceinline__ Fr cmul_coef(const Fr* c, int i, uint32_t ones, const
   return (i < 32 && ((ones >> i) & 1u)) ? x : rmul(ld_g(&c[i]), x);
 }
 
+// The same for a gate's own coefficient i, also folding -1 (a negation) and 0.
+__device__ __forceinline__ Fr gmul_coef(const DevGate& G, const Fr* c, int i, const Fr& x) {
+  if (i < 32) {
+    const uint32_t bit = 1u << i;
+    if (G.ones & bit) return x;
+    if (G.zeros & bit) return fe_zero<FrConsts>();
+    if (G.negs & bit) return fe_neg(x);
+  }
+  return rmul(ld_g(&c[i]), x);
+}
+
 // Affine form sum_{i<t} c[i] * x_i + c[t], operands ops[0..t); `ones` is
 // the one-mask of c[0..].
-__device__ __forceinline__ Fr affine_form(const Slots& sm, const uint16_t* ops, const Fr* c, int t,
-                                          uint32_t ones) {
-  Fr acc = ld_g(&c[t]);
-  for (int i = 0; i < t; ++i) acc = fe_add(acc, cmul_coef(c, i, ones, sm_ld(sm, ops[i])));
+__device__ __forceinline__ Fr affine_form(const Slots& sm, const DevGate& G, const uint16_t* ops, const Fr* c,
+                                          int c0, int t) {
+  Fr acc = ld_g(&c[c0 + t]);
+  for (int i = 0; i < t; ++i) acc = fe_add(acc, gmul_coef(G, c, c0 + i, sm_ld(sm, ops[i])));
   return acc;
 }
 
@@ -101,17 +121,17 @@ static __device__ __noinline__ Fr eval_gate_dev(const DevProgram& P, int g, cons
   const Fr* c = P.coeffs + G.cf_off;
   switch (G.kind) {
     case G_LINEAR:
-      return affine_form(sm, ops, c, G.p1, G.ones);
+      return affine_form(sm, G, ops, c, 0, G.p1);
     case G_PRODUCT:
-      return rmul(cmul_coef(c, 0, G.ones, sm_ld(sm, ops[0])), sm_ld(sm, ops[1]));
+      return rmul(gmul_coef(G, c, 0, sm_ld(sm, ops[0])), sm_ld(sm, ops[1]));
     case G_MASK: {
       Fr x = sm_ld(sm, ops[0]), m = sm_ld(sm, ops[1]);
       return fe_sub(fe_add(rmul(x, m), fe_one<FrConsts>()), m);
     }
     case G_AFFINE: {
       const int t = G.p1, u = G.p2;
-      Fr l = affine_form(sm, ops, c, t, G.ones);
-      Fr r = affine_form(sm, ops + t, c + t + 1, u, t + 1 < 32 ? G.ones >> (t + 1) : 0u);
+      Fr l = affine_form(sm, G, ops, c, 0, t);
+      Fr r = affine_form(sm, G, ops + t, c, t + 1, u);
       return rmul(l, r);
     }
     case G_TREE_PRODUCT:
@@ -121,10 +141,12 @@ static __device__ __noinline__ Fr eval_gate_dev(const DevProgram& P, int g, cons
     case G_QUADRATIC: {
       const int t = G.p1, u = G.p2;
       Fr acc = ld_g(&c[0]);
-      for (int i = 0; i < t; ++i) acc = fe_add(acc, cmul_coef(c, 1 + i, G.ones, sm_ld(sm, ops[i])));
+      for (int i = 0; i < t; ++i) acc = fe_add(acc, gmul_coef(G, c, 1 + i, sm_ld(sm, ops[i])));
       for (int j = 0; j < u; ++j) {
+        const int ci = 1 + t + j;
+        if (ci < 32 && ((G.zeros >> ci) & 1u)) continue;
         Fr yz = rmul(sm_ld(sm, ops[t + 2 * j]), sm_ld(sm, ops[t + 2 * j + 1]));
-        acc = fe_add(acc, cmul_coef(c, 1 + t + j, G.ones, yz));
+        acc = fe_add(acc, gmul_coef(G, c, ci, yz));
       }
       return acc;
     }
