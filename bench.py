@@ -448,6 +448,31 @@ def run_shard_workloads(ctx, local, contexts=6, serve_budget_gb=150):
     out["cfg2_shard_2p20_ms"] = timed(cfg2) * 1e3
     del cols2
 
+    # A real circuit: the reference's committed add_sub artifact (69 columns,
+    # 25 gate lists at 2^20 rows), GKR forward + proof over mixed columns.
+    import artifact
+
+    with open(os.path.join(ROOT, "tests", "golden", "artifacts", "add_sub.bin"), "rb") as f:
+        art = artifact.decode(f.read())
+    fam = artifact.to_circuit(art, 20)
+    fam_blob = fam.to_blob()
+    fam_slots = sorted({c[1] for L in art["layers"] for grp in ("cached", "producing", "enforcing")
+                        for e in L[grp] for c in e[-1]["coeffs"] if c[0] == "ch"} | {0})
+    frng = random.Random(SEED + 5)
+    fam_ch = {sl: frng.randrange(A.P_R) for sl in fam_slots}
+    fam_cols = shard.device_columns(torch, 1 << 20, fam.n_committed, SEED + 5, dev, ctx)
+
+    def family():
+        ptrs = [c.data_ptr() for c in fam_cols]
+        v = ctx.gkr_forward(fam_blob, ptrs, fam_ch, on_device=True)
+        ctx.gkr_prove(fam_blob, v, fam_ch, A.transcript_init())
+        v.free()
+
+    family()
+    out["family_add_sub_gkr_2p20_ms"] = timed(family, reps=2) * 1e3
+    del fam_cols
+    torch.cuda.empty_cache()
+
     # Config 3: 16 columns x 2^22: commit, then the batched opening.
     cols3 = shard.device_columns(torch, 1 << 22, 16, SEED + 3, dev, ctx)
     rng = random.Random(SEED)
