@@ -26,10 +26,10 @@ PROOF_BYTES = 704
 STATUS = {
     0: "Ok", 1: "LengthMismatch", 2: "UnsupportedNumVars", 3: "PointLengthMismatch", 4: "SrsTooSmall",
     5: "DegenerateChallenge", 6: "EmptyBatch", 7: "BatchLengthMismatch", 8: "MixedColumnSizes",
-    9: "InvalidPoint", 20: "NonCanonical", 21: "InvalidArgument", 22: "BadCircuit", 23: "NoSrs",
+    9: "InvalidPoint", 10: "MalformedAccumulator", 20: "NonCanonical", 21: "InvalidArgument", 22: "BadCircuit", 23: "NoSrs",
     24: "Internal", 100: "Cuda", 101: "OutOfMemory", 103: "NoDevice",
 }
-PCS_CODES = {2, 3, 4, 5, 6, 7, 8, 9}
+PCS_CODES = {2, 3, 4, 5, 6, 7, 8, 9, 10}
 
 
 class ApogeeError(RuntimeError):
@@ -246,6 +246,32 @@ class Context:
         self._check(lib().apg_msm_small_u32(self._h, bases, ctypes.c_size_t(len(bases) // 64), arr,
                                             ctypes.c_size_t(len(scalars)), out))
         return out.raw
+
+    # ---- deferred-pairing accumulator ---------------------------------------
+    def _acc_args(self, sides, scalars: bytes, points: bytes, checks):
+        n = len(sides)
+        assert len(scalars) == 32 * n and len(points) == 64 * n
+        cs = (ctypes.c_size_t * max(len(checks), 1))(*checks)
+        return bytes(sides), scalars, points, ctypes.c_size_t(n), cs
+
+    def discharge_msms(self, sides, scalars: bytes, points: bytes, checks):
+        """pcs::discharge up to its pairing (crates/pcs/src/accumulator.rs:146-163):
+        sides (0 G2One / 1 G2X a byte), scalars Fr in-memory bytes, points
+        64-byte canonical, checks the group counts. Returns (A, B, nu) with A, B
+        canonical points and nu as Fr in-memory bytes."""
+        sd, sc, pt, n, cs = self._acc_args(sides, scalars, points, checks)
+        a, b, nu = (ctypes.create_string_buffer(k) for k in (64, 64, 32))
+        self._check(lib().apg_discharge_msms(self._h, sd, sc, pt, n, cs, ctypes.c_size_t(len(checks)), a, b, nu))
+        return a.raw, b.raw, nu.raw
+
+    def pairing_msms(self, sides, scalars: bytes, points: bytes, checks, weights: bytes):
+        """check_pairings' two MSMs (accumulator.rs:171-214) with one weight a
+        check (Fr in-memory bytes). Returns (A, B)."""
+        sd, sc, pt, n, cs = self._acc_args(sides, scalars, points, checks)
+        assert len(weights) == 32 * len(checks)
+        a, b = ctypes.create_string_buffer(64), ctypes.create_string_buffer(64)
+        self._check(lib().apg_pairing_msms(self._h, sd, sc, pt, n, cs, weights, ctypes.c_size_t(len(checks)), a, b))
+        return a.raw, b.raw
 
     # ---- commit -------------------------------------------------------------
     def commit(self, evals: bytes, num_vars: int) -> bytes:

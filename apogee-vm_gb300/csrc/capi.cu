@@ -268,6 +268,25 @@ int apg_msm_small_u32(apg_ctx* ctx, const uint8_t* bases, size_t n_bases, const 
   return guarded(ctx, [&](Ctx& c) { return msm_common(c, bases, n_bases, scalars, n_scalars, true, out); });
 }
 
+int apg_discharge_msms(apg_ctx* ctx, const uint8_t* sides, const uint8_t* scalars, const uint8_t* points, size_t n,
+                       const size_t* checks, size_t n_checks, uint8_t a_out[64], uint8_t b_out[64],
+                       uint8_t nu_out[32]) {
+  return guarded(ctx, [&](Ctx& c) {
+    return accumulator_msms(c, sides, scalars, points, n, checks, n_checks, nullptr, a_out, b_out, nu_out);
+  });
+}
+
+int apg_pairing_msms(apg_ctx* ctx, const uint8_t* sides, const uint8_t* scalars, const uint8_t* points, size_t n,
+                     const size_t* checks, const uint8_t* weights, size_t n_checks, uint8_t a_out[64],
+                     uint8_t b_out[64]) {
+  return guarded(ctx, [&](Ctx& c) {
+    if (n_checks && !weights) return (int)APG_ERR_INVALID_ARGUMENT;
+    static const uint8_t kNone[32] = {0};
+    return accumulator_msms(c, sides, scalars, points, n, checks, n_checks, weights ? weights : kNone, a_out, b_out,
+                            nullptr);
+  });
+}
+
 int apg_commit(apg_ctx* ctx, const uint8_t* evals, size_t num_vars, uint8_t out[64]) {
   return guarded(ctx, [&](Ctx& c) { return commit_common(c, evals, false, false, num_vars, out); });
 }

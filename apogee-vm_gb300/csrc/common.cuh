@@ -194,6 +194,8 @@ __global__ void k_fr_to_mont(Fr* v, size_t n, uint32_t* flags);
 
 // Canonical 64-byte points (host) -> device affine Montgomery, validated.
 void upload_points(Ctx& c, const uint8_t* host, size_t n, Affine* dst);
+// The same without waiting: the flags are the caller's to check.
+void upload_points_async(Ctx& c, const uint8_t* host, size_t n, Affine* dst);
 // Device affine Montgomery -> canonical 64-byte points (host).
 void download_points(Ctx& c, const Affine* src, size_t n, uint8_t* host);
 // SRS [tau^i]G for i < n, generated on the device.
@@ -237,5 +239,10 @@ const SrsTable* srs_table_for(Ctx& c, size_t n, bool tuned = true);
 void msm_autotune(Ctx& c, const void* d_sample, size_t sample_len, int kmin, int kmax, const int* cands,
                   size_t ncands, int* chosen);
 double probe_fq_mul_rate(Ctx& c, double target_ms);
+// The group side of pcs::discharge (weights null) or check_pairings (one
+// weight a check): see apg_discharge_msms / apg_pairing_msms.
+int accumulator_msms(Ctx& c, const uint8_t* sides, const uint8_t* scalars, const uint8_t* points, size_t n,
+                     const size_t* checks, size_t nchecks, const uint8_t* weights, uint8_t* a_out, uint8_t* b_out,
+                     uint8_t* nu_out);
 
 }  // namespace apg

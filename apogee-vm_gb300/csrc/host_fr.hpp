@@ -229,6 +229,20 @@ enum Tag : uint64_t {
   T_GKR_CHILD = 29,
 };
 
+// The transcript's four limbs of a canonical 64-byte G1 encoding: the 128-bit
+// halves of x and y; infinity (all zero bytes) is 2^128 four times
+// (crates/transcript/src/lib.rs:493-510).
+inline void g1_limbs(const uint8_t* p, F out[4]) {
+  bool inf = true;
+  for (int i = 0; i < 64; ++i) inf &= p[i] == 0;
+  for (int h = 0; h < 4; ++h) {
+    uint64_t c[4] = {0, 0, 0, 0};
+    if (inf) c[2] = 1;
+    else memcpy(c, p + 16 * h, 16);
+    out[h] = from_canonical(c);
+  }
+}
+
 // Rate 2, capacity 1, overwrite absorption; a squeeze pops from the end of
 // the rate. Snapshot bytes: state[3], input[2], input_len, output[2],
 // output_len with Fr canonical (226 bytes).
@@ -278,21 +292,10 @@ struct Transcript {
     observe(from_u64(tag));
     return sample();
   }
-  // A G1 point list as one message of 4 limbs a point: the 128-bit halves of
-  // the canonical x and y; infinity absorbs 2^128 four times.
+  // A G1 point list as one message of 4 limbs a point (g1_limbs).
   void absorb_g1(uint64_t tag, const uint8_t* pts, size_t n) {
-    std::vector<F> limbs;
-    for (size_t k = 0; k < n; ++k) {
-      const uint8_t* p = pts + 64 * k;
-      bool inf = true;
-      for (int i = 0; i < 64; ++i) inf &= p[i] == 0;
-      for (int h = 0; h < 4; ++h) {
-        uint64_t c[4] = {0, 0, 0, 0};
-        if (inf) c[2] = 1;
-        else memcpy(c, p + 16 * h, 16);
-        limbs.push_back(from_canonical(c));
-      }
-    }
+    std::vector<F> limbs(4 * n);
+    for (size_t k = 0; k < n; ++k) g1_limbs(pts + 64 * k, &limbs[4 * k]);
     absorb(tag, limbs);
   }
 

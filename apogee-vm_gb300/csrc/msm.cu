@@ -746,12 +746,16 @@ inline unsigned blocks_for(size_t n, int threads) {
 // Host side
 // ---------------------------------------------------------------------------
 
-void upload_points(Ctx& c, const uint8_t* host, size_t n, Affine* dst) {
+void upload_points_async(Ctx& c, const uint8_t* host, size_t n, Affine* dst) {
   if (n == 0) return;
   uint4* raw = c.scratch[S_TMP7].as<uint4>(4 * n);
   APG_CUDA(cudaMemcpyAsync(raw, host, 64 * n, cudaMemcpyHostToDevice, c.stream));
   launch(c, k_points_in, blocks_for<int>(n, 256), 256, 0, (const uint4*)raw, n, dst, c.d_flags);
-  c.check_flags();
+}
+
+void upload_points(Ctx& c, const uint8_t* host, size_t n, Affine* dst) {
+  upload_points_async(c, host, n, dst);
+  if (n) c.check_flags();
 }
 
 void download_points(Ctx& c, const Affine* src, size_t n, uint8_t* host) {

@@ -257,6 +257,8 @@ def run_profile_case(args):
         return run_profile_shard(args, ctx, torch, dev)
     if args.profile_case == "family":
         return run_profile_family(args, ctx, torch, dev)
+    if args.profile_case == "discharge":
+        return run_profile_discharge(args, ctx)
     if args.profile_case == "open":
         ctx.srs_generate((TAU_SEED * 0x9E3779B97F4A7C15) % A.P_R, 1 << n)
         ctx.srs_prepare()
@@ -386,6 +388,38 @@ def run_profile_family(args, ctx, torch, dev):
                       "committed_columns": circ.n_committed, "gate_lists": circ.depth(),
                       "ms_per_phase": {k: v * 1e3 / args.steps for k, v in phases.items()},
                       "timers_ms_launches": timers}), flush=True)
+    ctx.close()
+    return 0
+
+
+def run_profile_discharge(args, ctx):
+    """Discharging an accumulator of --checks deferred Mercury checks (ten
+    G2One and two G2X entries each, as a verification emits them) through
+    apg_discharge_msms from host buffers: the points are SRS points, the
+    scalars uniform. Prints the mean wall time a call and the MSM's share."""
+    import apogee_gpu as A
+
+    rng = random.Random(SEED)
+    pool = 4096
+    ctx.srs_generate((TAU_SEED * 0x9E3779B97F4A7C15) % A.P_R, pool)
+    pts = ctx.srs_download(pool)
+    k = args.checks
+    n = 12 * k
+    sides = bytes(([0] * 10 + [1] * 2) * k)
+    idx = [rng.randrange(pool) for _ in range(n)]
+    points = b"".join(pts[64 * i:64 * i + 64] for i in idx)
+    scalars = A.to_mont_bytes(rng.randrange(A.P_R) for _ in range(n))
+    checks = [12] * k
+    for _ in range(args.warmup):
+        ctx.discharge_msms(sides, scalars, points, checks)
+    ctx.set_timing(True)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.discharge_msms(sides, scalars, points, checks)
+    dt = (time.perf_counter() - t0) / args.steps
+    msm_ms, _ = ctx.timer(1)  # APG_TIMER_MSM_TOTAL
+    print(json.dumps({"case": "discharge", "checks": k, "entries": n, "ms_per_call": dt * 1e3,
+                      "msm_ms_per_call": msm_ms / args.steps}), flush=True)
     ctx.close()
     return 0
 
@@ -696,8 +730,10 @@ def main():
     ap.add_argument("--window-bits", type=int, default=0, help="--only-msm: fixed window width instead of autotuning")
     ap.add_argument("--no-shards", dest="shards", action="store_false",
                     help="skip the per-config shard timings and the 207-shard mix / serving run")
-    ap.add_argument("--profile-case", choices=["zerocheck", "gkr", "open", "shard", "family"], default=None,
-                    help="run one lean sumcheck / GKR / opening / whole-shard / family-circuit case for profilers")
+    ap.add_argument("--profile-case", choices=["zerocheck", "gkr", "open", "shard", "family", "discharge"],
+                    default=None, help="run one lean sumcheck / GKR / opening / whole-shard / family-circuit / "
+                    "accumulator-discharge case for profilers")
+    ap.add_argument("--checks", type=int, default=207, help="--profile-case discharge: deferred checks")
     ap.add_argument("--family", default="add_sub", help="--profile-case family: the committed artifact's name")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -48,6 +48,7 @@ enum apg_status {
   APG_ERR_BATCH_LENGTH_MISMATCH = 7,  /* PcsError::BatchLengthMismatch */
   APG_ERR_MIXED_COLUMN_SIZES = 8,     /* PcsError::MixedColumnSizes */
   APG_ERR_INVALID_POINT = 9,          /* PcsError::InvalidPoint / off-curve input */
+  APG_ERR_MALFORMED_ACCUMULATOR = 10, /* PcsError::MalformedAccumulator */
   APG_ERR_NONCANONICAL = 20,          /* an input value is >= its modulus */
   APG_ERR_INVALID_ARGUMENT = 21,      /* null pointer, bad shape */
   APG_ERR_BAD_CIRCUIT = 22,           /* malformed circuit blob */
@@ -277,6 +278,32 @@ int apg_gkr_prove(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, apg_
 /* As apg_gkr_forward with the base columns already in device memory. */
 int apg_gkr_forward_device(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, const void* const* d_base,
                            const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, apg_gkr_values** out);
+
+/* ---- deferred-pairing accumulator (crates/pcs/src/accumulator.rs) ------- */
+
+/* The group side of pcs::discharge (crates/pcs/src/accumulator.rs:146-163),
+ * everything before its pairing. The accumulator is n entries (the fields of
+ * AccumulatorEntry, :37-42): sides[i] 0 = PairingSide::G2One, 1 = G2X;
+ * scalars as n Fr in memory; points as n canonical 64-byte G1 encodings
+ * (all zero = infinity); grouped into deferred checks by the counts
+ * checks[0..n_checks). Every point is validated (APG_ERR_INVALID_POINT),
+ * then the counts must partition the entries (APG_ERR_MALFORMED_ACCUMULATOR);
+ * the merge challenge nu is drawn from the digest of the accumulator's words
+ * (pcs-verify/src/lib.rs:315-319) and
+ *   A = sum_j nu^j sum_{G2One entries of check j} s_i P_i,  B likewise over G2X,
+ * are returned as canonical points; nu_out (nullable) receives nu (Fr in
+ * memory). The caller's pairing check is e(A, [1]_2) * e(-B, [x]_2) == 1.
+ * A side other than 0/1 is APG_ERR_INVALID_ARGUMENT, an unreduced scalar
+ * APG_ERR_NONCANONICAL (neither can come from the reference's types). */
+int apg_discharge_msms(apg_ctx* ctx, const uint8_t* sides, const uint8_t* scalars, const uint8_t* points, size_t n,
+                       const size_t* checks, size_t n_checks, uint8_t a_out[64], uint8_t b_out[64],
+                       uint8_t nu_out[32]);
+/* The MSMs of check_pairings (accumulator.rs:171-214) with the caller's
+ * weights, one Fr (in memory) a check: verify and batch_verify reach it with
+ * one check of weight one. The partition is checked first, then the points. */
+int apg_pairing_msms(apg_ctx* ctx, const uint8_t* sides, const uint8_t* scalars, const uint8_t* points, size_t n,
+                     const size_t* checks, const uint8_t* weights, size_t n_checks, uint8_t a_out[64],
+                     uint8_t b_out[64]);
 
 /* ---- transcript (crates/transcript/src/lib.rs:214-346) ------------------- */
 

@@ -6,6 +6,7 @@
 #include <chrono>
 #include <memory>
 
+#include "accumulator.hpp"
 #include "mercury.hpp"
 
 using namespace oracle;
@@ -341,6 +342,66 @@ int oracle_mercury_batch_open(const uint8_t* srs_pts, size_t srs_n, const uint8_
   } catch (...) {
     return 9;
   }
+}
+
+// The deferred-pairing accumulator (accumulator.hpp). Entries: n side bytes,
+// n canonical Fr scalars, n 64-byte points; checks: the group counts.
+// weights == null: pcs::discharge (points validated first, then the
+// partition; nu from the digest of the words); otherwise check_pairings with
+// the caller's weights, one per check (the partition first). Returns 0,
+// 2 (a non-canonical scalar or weight), 3 (a side tag other than 0 and 1),
+// 9 (a point off the curve), 10 (counts that do not partition the entries).
+// nu_out / digest_out are written in the discharge form only.
+static int read_entries(const uint8_t* sides, const uint8_t* scalars, const uint8_t* points, size_t n,
+                        std::vector<AccEntry>& out) {
+  out.resize(n);
+  for (size_t i = 0; i < n; ++i) {
+    if (sides[i] > 1) return 3;
+    out[i].side = sides[i];
+    if (!G1Affine::from_bytes(points + 64 * i, out[i].point)) return 9;
+  }
+  for (size_t i = 0; i < n; ++i)
+    if (!read_fr(scalars + 32 * i, out[i].scalar)) return 2;
+  return 0;
+}
+
+int oracle_accumulator_msms(const uint8_t* sides, const uint8_t* scalars, const uint8_t* points, size_t n,
+                            const uint64_t* checks, size_t n_checks, const uint8_t* weights, size_t threads,
+                            uint8_t* a_out, uint8_t* b_out, uint8_t* nu_out, uint8_t* digest_out) {
+  std::vector<size_t> cs(checks, checks + n_checks);
+  std::vector<AccEntry> entries;
+  std::vector<Fr> w(n_checks);
+  if (weights) {
+    if (!acc_partition(n, cs)) return 10;
+    if (int st = read_entries(sides, scalars, points, n, entries)) return st;
+    for (size_t j = 0; j < n_checks; ++j)
+      if (!read_fr(weights + 32 * j, w[j])) return 2;
+  } else {
+    if (int st = read_entries(sides, scalars, points, n, entries)) return st;
+    if (!acc_partition(n, cs)) return 10;
+    const Fr digest = acc_digest(acc_words(entries, cs));
+    const Fr nu = acc_merge_challenge(digest);
+    w = acc_powers(nu, n_checks);
+    if (nu_out) nu.to_bytes(nu_out);
+    if (digest_out) digest.to_bytes(digest_out);
+  }
+  G1Affine a, b;
+  acc_side_msms(entries, cs, w, threads ? threads : 1, a, b);
+  a.to_bytes(a_out);
+  b.to_bytes(b_out);
+  return 0;
+}
+
+// accumulator_words (accumulator.rs:57-83): n_checks + 6n canonical Fr.
+int oracle_accumulator_words(const uint8_t* sides, const uint8_t* scalars, const uint8_t* points, size_t n,
+                             const uint64_t* checks, size_t n_checks, uint8_t* out) {
+  std::vector<size_t> cs(checks, checks + n_checks);
+  std::vector<AccEntry> entries;
+  if (int st = read_entries(sides, scalars, points, n, entries)) return st;
+  if (!acc_partition(n, cs)) return 10;
+  const std::vector<Fr> words = acc_words(entries, cs);
+  for (size_t i = 0; i < words.size(); ++i) words[i].to_bytes(out + 32 * i);
+  return 0;
 }
 
 }  // extern "C"

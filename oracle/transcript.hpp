@@ -23,6 +23,7 @@ enum : uint64_t {
   SUMCHECK_CHALLENGE = 5, EVALUATION_CLAIM = 6, PCS_OPENING = 7, WITNESS_DIGEST = 8,
   SUMCHECK_FINAL_EVALS = 9, MERCURY_INSTANCE = 10, MERCURY_ALPHA = 11, MERCURY_GAMMA = 12,
   MERCURY_Z = 13, BDFG_BATCH = 14, BDFG_POINT = 15, PAIRING_MERGE = 16, MERCURY_BATCH = 17,
+  ACCUMULATOR_DIGEST = 18, ACCUMULATOR_MERGE = 19,
   GKR_OUTPUTS = 25, GKR_OUTPUT_POINT = 26, GKR_BATCH = 27, GKR_LAYER_CLAIMS = 28,
   GKR_CHILD = 29, SHARD_SEED = 39, SHARD_TS_WINDOW = 40,
 };

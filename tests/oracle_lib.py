@@ -155,3 +155,74 @@ def golden_artifacts():
     """The reference's committed circuit artifacts: {file name: bytes}."""
     d = os.path.join(GOLDEN, "artifacts")
     return {f: open(os.path.join(d, f), "rb").read() for f in sorted(os.listdir(d)) if f.endswith(".bin")}
+
+
+# ---- the deferred-pairing accumulator --------------------------------------
+
+INFINITY_SENTINEL = 1 << 128
+
+
+def golden_accumulator():
+    """accumulator.txt: the toy tau, the concatenated accumulator's words and
+    their digest (crates/pcs/tests/vectors/accumulator.txt)."""
+    tau, words, digest = None, {}, None
+    for line in golden_lines("accumulator.txt"):
+        t = line.split()
+        if t[0] == "tau":
+            tau = fe_int(hexb(t[1]))
+        elif t[0] == "word":
+            words[int(t[1])] = fe_int(hexb(t[2]))
+        elif t[0] == "digest":
+            digest = fe_int(hexb(t[1]))
+    return tau, [words[i] for i in range(len(words))], digest
+
+
+def entries_from_words(words):
+    """accumulator_from_words (crates/pcs/src/accumulator.rs:90-126, limbs
+    decoded as g1_from_limbs :292-318): (sides, scalars, points, checks) with
+    sides as bytes, scalars as ints, points as 64-byte encodings."""
+    sides, scalars, points, checks = [], [], [], []
+    at = 0
+    while at < len(words):
+        count = words[at]
+        at += 1
+        assert count < 1 << 64 and count <= (len(words) - at) // 6, "malformed count word"
+        for _ in range(count):
+            side, scalar, limbs = words[at], words[at + 1], words[at + 2:at + 6]
+            assert side in (0, 1), "malformed side tag"
+            if all(x == INFINITY_SENTINEL for x in limbs):
+                point = bytes(64)
+            else:
+                assert all(x < INFINITY_SENTINEL for x in limbs), "malformed limb"
+                point = b"".join(x.to_bytes(16, "little") for x in limbs)
+            sides.append(side)
+            scalars.append(scalar)
+            points.append(point)
+            at += 6
+        checks.append(count)
+    return bytes(sides), scalars, points, checks
+
+
+def accumulator_msms(sides: bytes, scalars, points, checks, weights=None, threads: int = 8):
+    """The oracle's group side of discharge (weights None) or check_pairings:
+    (status, A, B, nu, digest) with A, B as 64-byte points, nu and digest ints."""
+    import ctypes as ct
+    n = len(sides)
+    a, b, nu, dg = buf(64), buf(64), buf(32), buf(32)
+    cs = (ct.c_uint64 * max(len(checks), 1))(*checks)
+    w = b"".join(fe(x) for x in weights) if weights is not None else None
+    rc = lib().oracle_accumulator_msms(bytes(sides), b"".join(fe(s) for s in scalars), b"".join(points),
+                                       ct.c_size_t(n), cs, ct.c_size_t(len(checks)), w, ct.c_size_t(threads),
+                                       a, b, nu, dg)
+    return rc, a.raw, b.raw, fe_int(nu.raw), fe_int(dg.raw)
+
+
+def accumulator_words(sides: bytes, scalars, points, checks):
+    import ctypes as ct
+    n = len(sides)
+    out = buf(32 * (len(checks) + 6 * n))
+    cs = (ct.c_uint64 * max(len(checks), 1))(*checks)
+    rc = lib().oracle_accumulator_words(bytes(sides), b"".join(fe(s) for s in scalars), b"".join(points),
+                                        ct.c_size_t(n), cs, ct.c_size_t(len(checks)), out)
+    assert rc == 0, rc
+    return [fe_int(out.raw[32 * i:32 * i + 32]) for i in range(len(checks) + 6 * n)]

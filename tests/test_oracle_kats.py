@@ -316,3 +316,47 @@ def test_known_tau_commitment(oracle):
     assert oracle.oracle_commit(srs, ctypes.c_size_t(1 << nv), b"".join(fe(c) for c in coeffs), nv, 4, cm) == 0
     f_tau = sum(c * pow(tau, i, O.P_R) for i, c in enumerate(coeffs)) % O.P_R
     assert cm.raw == O.g1_mul(O.G1_GEN, f_tau)
+
+
+def test_accumulator_words_and_digest(oracle):
+    """The oracle rebuilds the concatenated accumulator's 146 words (two
+    deferred checks of twelve entries) and their digest from the entries
+    accumulator.txt records (crates/pcs/tests/vectors/accumulator.txt)."""
+    tau, words, digest = O.golden_accumulator()
+    sides, scalars, points, checks = O.entries_from_words(words)
+    assert checks == [12, 12]
+    assert O.accumulator_words(sides, scalars, points, checks) == words
+    rc, _, _, _, dg = O.accumulator_msms(sides, scalars, points, checks)
+    assert rc == 0 and dg == digest
+
+
+def test_accumulator_discharge_relation(oracle):
+    """With the toy SRS's known tau, e(A, [1]_2) = e(B, [x]_2) is A = tau * B:
+    the recorded deferred verifications hold, merged and one by one, and a
+    changed scalar breaks the relation."""
+    tau, words, _ = O.golden_accumulator()
+    sides, scalars, points, checks = O.entries_from_words(words)
+    rc, a, b, _, _ = O.accumulator_msms(sides, scalars, points, checks)
+    assert rc == 0 and O.g1_mul(b, tau) == a
+    for j in range(2):
+        s = slice(12 * j, 12 * j + 12)
+        rc, a1, b1, _, _ = O.accumulator_msms(sides[s], scalars[s], points[s], [12], weights=[1])
+        assert rc == 0 and O.g1_mul(b1, tau) == a1
+    bad = list(scalars)
+    bad[3] = (bad[3] + 1) % O.P_R
+    rc, a2, b2, _, _ = O.accumulator_msms(sides, bad, points, checks)
+    assert rc == 0 and O.g1_mul(b2, tau) != a2
+
+
+def test_accumulator_refusal_order(oracle):
+    """discharge validates points before the partition; check_pairings checks
+    the partition first (crates/pcs/src/accumulator.rs:151, :177-185)."""
+    _, words, _ = O.golden_accumulator()
+    sides, scalars, points, checks = O.entries_from_words(words)
+    off = bytearray(points[0])
+    off[0] ^= 1
+    pts = [bytes(off)] + points[1:]
+    assert O.accumulator_msms(sides, scalars, points, [12, 11])[0] == 10
+    assert O.accumulator_msms(sides, scalars, pts, checks)[0] == 9
+    assert O.accumulator_msms(sides, scalars, pts, [12, 13])[0] == 9
+    assert O.accumulator_msms(sides, scalars, pts, [12, 13], weights=[1, 1])[0] == 10
