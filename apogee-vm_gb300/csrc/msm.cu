@@ -591,11 +591,22 @@ __global__ void __launch_bounds__(256) k_digits(MsmCols cols, int c, int windows
 #ifndef APG_ACC_MIN_BLOCKS
 #define APG_ACC_MIN_BLOCKS 4
 #endif
+// After affine pair rounds (`mode` non-null and *mode == 0) the input is the
+// last round's explicit point list, position i holding point i, with its own
+// bucket ends and total; otherwise references into `bases`.
 __global__ void __launch_bounds__(128, APG_ACC_MIN_BLOCKS) k_bucket_acc(const uint32_t* sorted, const uint32_t* ends, uint32_t nbins,
                                                     const uint32_t* total, size_t nseg, const Affine* bases,
-                                                    Xyzz* buckets, uint32_t* okeys, Xyzz* opts, uint8_t* opres) {
+                                                    Xyzz* buckets, uint32_t* okeys, Xyzz* opts, uint8_t* opres,
+                                                    const uint32_t* mode, const uint32_t* pair_ends,
+                                                    const Affine* pair_pts) {
   const size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (s >= nseg) return;
+  const bool direct = mode && *mode == 0;
+  if (direct) {
+    ends = pair_ends;
+    total = pair_ends + nbins - 1;
+    bases = pair_pts;
+  }
   const size_t E = *total;
   const size_t seg = (E + nseg - 1) / nseg;
   const size_t lo = s * seg;
@@ -632,9 +643,9 @@ __global__ void __launch_bounds__(128, APG_ACC_MIN_BLOCKS) k_bucket_acc(const ui
       } while (run_end <= i);
       acc = xyzz_inf();
     }
-    const uint32_t e = sorted[i];
+    const uint32_t e = direct ? (uint32_t)i : sorted[i];
     Affine p = ld_affine(&bases[e & 0x7fffffffu]);
-    if (e >> 31) p.y = fe_neg(p.y);
+    if (!direct && (e >> 31)) p.y = fe_neg(p.y);
     if (!aff_is_inf(p)) acc = xyzz_add_affine(acc, p);
   }
   const bool continues = hi < run_end;
@@ -651,6 +662,166 @@ __global__ void __launch_bounds__(128, APG_ACC_MIN_BLOCKS) k_bucket_acc(const ui
     }
   }
   if (!head_written) put_item(okeys, opts, opres, 2 * s, first, nullptr);
+}
+
+// ---- affine pair rounds ------------------------------------------------------
+//
+// Before the XYZZ accumulation, a few rounds halve every bucket's run by adding
+// its points in adjacent pairs in affine coordinates. All the pairs one thread
+// owns share one field inversion (Montgomery's batch trick: the running product
+// of the denominators going forward, one inversion, then each pair's inverse at
+// two products going backward), so a pair sum costs 5M + 1S plus a share of one
+// inversion, against 8M + 2S for each mixed XYZZ addition it replaces. Equal x
+// (a doubling, or P + (-P)) and infinity are classified per pair, so no zero
+// ever enters the product.
+//
+// Round r reads a list with bucket ends `ends_in` and writes the list of
+// ceil(len/2) points per bucket at the exclusive-scan offsets `start_out`
+// (nbins + 1 entries, the total last). Round 0 reads sorted references into
+// the bases; later rounds read the previous round's points. A round 0 whose
+// output would not fit the scratch sets *mode = 1 and every later step takes
+// the references instead.
+
+#ifndef APG_PAIR_ROUNDS
+#define APG_PAIR_ROUNDS 3
+#endif
+constexpr int kPairRounds = APG_PAIR_ROUNDS;
+// Lists shorter than this per group are left to the XYZZ kernel alone (the
+// extra launches would cost more than the products saved).
+constexpr size_t kPairMinEntries = (size_t)1 << 21;
+// Round 0's output list is held to this many points (64 bytes each).
+constexpr size_t kPairMaxPoints = (size_t)48 << 20;
+
+__global__ void k_halve_counts(const uint32_t* ends_in, uint32_t nbins, uint32_t* cnt) {
+  const size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (b > nbins) return;
+  if (b == nbins) {
+    cnt[b] = 0;
+    return;
+  }
+  const uint32_t len = ends_in[b] - (b ? ends_in[b - 1] : 0u);
+  cnt[b] = (len + 1) / 2;
+}
+
+template <bool REFS>
+__device__ __forceinline__ Affine pair_point(const uint32_t* refs, const Affine* src, uint32_t i) {
+  if (REFS) {
+    const uint32_t e = refs[i];
+    Affine p = ld_affine(&src[e & 0x7fffffffu]);
+    if (e >> 31) p.y = fe_neg(p.y);
+    return p;
+  }
+  return ld_affine(&src[i]);
+}
+
+enum : int { kPairFirst = 0, kPairSecond = 1, kPairInf = 2, kPairAdd = 3, kPairDbl = 4 };
+
+// What the pair (p0, p1) sums to: p0 or p1 when the other is infinity, the
+// point at infinity for P + (-P), else an addition or a doubling.
+__device__ __forceinline__ int pair_kind(const Affine& p0, const Affine& p1) {
+  if (aff_is_inf(p1)) return kPairFirst;
+  if (aff_is_inf(p0)) return kPairSecond;
+  if (!fe_eq(p0.x, p1.x)) return kPairAdd;
+  return fe_eq(p0.y, p1.y) ? kPairDbl : kPairInf;
+}
+
+// The forward pass needs only the x coordinates (and y where x decides nothing).
+template <bool REFS>
+__device__ __forceinline__ bool pair_denominator(const uint32_t* refs, const Affine* src, uint32_t i0, Fq& d) {
+  uint32_t j0 = i0, j1 = i0 + 1;
+  bool n0 = false, n1 = false;
+  if (REFS) {
+    const uint32_t e0 = refs[i0], e1 = refs[i0 + 1];
+    j0 = e0 & 0x7fffffffu;
+    j1 = e1 & 0x7fffffffu;
+    n0 = e0 >> 31;
+    n1 = e1 >> 31;
+  }
+  const Fq x0 = ld_fe(&src[j0].x), x1 = ld_fe(&src[j1].x);
+  if (!fe_eq(x0, x1)) {
+    if (fe_is_zero(x0) && fe_is_zero(ld_fe(&src[j0].y))) return false;
+    if (fe_is_zero(x1) && fe_is_zero(ld_fe(&src[j1].y))) return false;
+    d = fe_sub(x1, x0);
+    return true;
+  }
+  Fq y0 = ld_fe(&src[j0].y), y1 = ld_fe(&src[j1].y);
+  if (n0) y0 = fe_neg(y0);
+  if (n1) y1 = fe_neg(y1);
+  if (fe_is_zero(x0) && (fe_is_zero(y0) || fe_is_zero(y1))) return false;  // an infinity
+  if (!fe_eq(y0, y1)) return false;                                        // P + (-P)
+  d = fe_add(y0, y0);
+  return true;
+}
+
+template <bool REFS>
+__global__ void __launch_bounds__(128) k_pair_round(const uint32_t* refs, const Affine* src, const uint32_t* ends_in,
+                                                    const uint32_t* start_out, uint32_t nbins, size_t cap,
+                                                    uint32_t* mode, size_t T, Fq* pp, Affine* out) {
+  const size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (s >= T || *mode) return;
+  const size_t E = start_out[nbins];
+  if (E > cap) {
+    if (s == 0) *mode = 1;
+    return;
+  }
+  const size_t m = (E + T - 1) / T;
+  const size_t lo = s * m;
+  if (lo >= E) return;
+  const size_t hi = min(lo + m, E);
+  uint32_t a = 0, bb = nbins - 1;  // the first bucket whose output reaches past lo
+  while (a < bb) {
+    const uint32_t mid = (a + bb) >> 1;
+    if (start_out[mid + 1] > lo) bb = mid;
+    else a = mid + 1;
+  }
+  uint32_t b = a;
+  Fq acc = fe_one<FqConsts>();
+  size_t k = 0;
+  for (size_t o = lo; o < hi; ++o) {
+    while (start_out[b + 1] <= o) ++b;
+    const uint32_t i0 = (b ? ends_in[b - 1] : 0u) + 2u * (uint32_t)(o - start_out[b]);
+    if (i0 + 1 >= ends_in[b]) continue;
+    Fq d;
+    if (!pair_denominator<REFS>(refs, src, i0, d)) continue;
+    st_fe(&pp[k * T + s], acc);
+    acc = cmul(acc, d);
+    ++k;
+  }
+  Fq inv = fe_inverse(acc);
+  for (size_t o = hi; o-- > lo;) {
+    while (start_out[b] > o) --b;
+    const uint32_t i0 = (b ? ends_in[b - 1] : 0u) + 2u * (uint32_t)(o - start_out[b]);
+    const Affine p0 = pair_point<REFS>(refs, src, i0);
+    Affine r = p0;
+    if (i0 + 1 < ends_in[b]) {
+      const Affine p1 = pair_point<REFS>(refs, src, i0 + 1);
+      const int kind = pair_kind(p0, p1);
+      if (kind == kPairSecond) {
+        r = p1;
+      } else if (kind == kPairInf) {
+        r.x = fe_zero<FqConsts>();
+        r.y = fe_zero<FqConsts>();
+      } else if (kind != kPairFirst) {
+        Fq d, num;
+        if (kind == kPairAdd) {
+          d = fe_sub(p1.x, p0.x);
+          num = fe_sub(p1.y, p0.y);
+        } else {
+          d = fe_add(p0.y, p0.y);
+          const Fq t = csqr(p0.x);
+          num = fe_add(t, fe_add(t, t));
+        }
+        --k;
+        const Fq2 q = cmul2(inv, ld_fe(&pp[k * T + s]), inv, d);  // 1/d, and 1/(d_1..d_{k-1})
+        inv = q.b;
+        const Fq lam = cmul(num, q.a);
+        r.x = fe_sub(fe_sub(csqr(lam), p0.x), p1.x);
+        r.y = fe_sub(cmul(lam, fe_sub(p0.x, r.x)), p0.y);
+      }
+    }
+    st_fe(&out[o].x, r.x);
+    st_fe(&out[o].y, r.y);
+  }
 }
 
 // Bucket reduction of a small bucket set (K <= kSmallK), one block per space:
@@ -909,6 +1080,18 @@ size_t acc_resident_threads(Ctx& c) {
   return (size_t)c.sm_count * (size_t)per_sm * 128;
 }
 
+size_t pair_resident_threads(Ctx& c) {
+  static std::once_flag once;
+  static int per_sm = 0;
+  std::call_once(once, [] {
+    int a = 0, b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_pair_round<true>, 128, 0) != cudaSuccess) a = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_round<false>, 128, 0) != cudaSuccess) b = 1;
+    per_sm = std::max(1, std::min(a, b));
+  });
+  return (size_t)c.sm_count * (size_t)per_sm * 128;
+}
+
 constexpr size_t kMaxBins = (size_t)(kScanBlock - 1) * kScanBlock * kScanItems;  // one pass of the 3-kernel scan
 constexpr size_t kMaxGroupEntries = (size_t)1 << 28;                           // 1 GiB of sorted references
 
@@ -972,8 +1155,47 @@ void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols
     launch(c, k_digits<false, true>, dgrid, 256, 0, cols, p.c, p.windows, (int)p.precomp, tab_n, canon, counts,
            sorted, c.d_flags);
   cudaEvent_t t_acc = c.timer_begin();
+  const uint32_t* pair_mode = nullptr;
+  const uint32_t* pair_ends = nullptr;
+  const Affine* pair_pts = nullptr;
+  if (kPairRounds > 0 && emax >= kPairMinEntries) {
+    // Round r's list fits cap[r]: a round keeps ceil(len/2) of each run, so
+    // a list never grows and at most halves plus one point per bucket.
+    size_t cap[kPairRounds > 0 ? kPairRounds : 1];
+    cap[0] = std::min((emax + nbins + 1) / 2, kPairMaxPoints);
+    for (int r = 1; r < kPairRounds; ++r) cap[r] = std::min(cap[r - 1], (cap[r - 1] + nbins + 1) / 2);
+    const size_t T = pair_resident_threads(c);
+    Affine* lst[2] = {c.scratch[S_PAIR_A].as<Affine>(cap[0]),
+                      c.scratch[S_PAIR_B].as<Affine>(kPairRounds > 1 ? cap[1] : 1)};
+    Fq* pp = c.scratch[S_PAIR_PP].as<Fq>((cap[0] + T - 1) / T * T);
+    uint32_t* cnt = c.scratch[S_PAIR_CNT].as<uint32_t>((size_t)kPairRounds * (nbins + 1) + 2);
+    uint32_t* mode = cnt + (size_t)kPairRounds * (nbins + 1);
+    APG_CUDA(cudaMemsetAsync(mode, 0, 2 * sizeof(uint32_t), c.stream));
+    const size_t scan_n = nbins + 1;
+    const unsigned sblocks = (unsigned)((scan_n + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems));
+    const uint32_t* ends_in = counts;
+    const unsigned pblocks = (unsigned)((T + 127) / 128);
+    for (int r = 0; r < kPairRounds; ++r) {
+      uint32_t* st = cnt + (size_t)r * scan_n;
+      launch(c, k_halve_counts, blocks_for<int>(scan_n, 256), 256, 0, ends_in, (uint32_t)nbins, st);
+      launch(c, k_scan_local, sblocks, kScanBlock, 0, st, scan_n, blk);
+      launch(c, k_scan_blocks, 1, kScanBlock, 0, blk, (int)sblocks);
+      launch(c, k_scan_add, blocks_for<int>(scan_n, 256), 256, 0, st, scan_n, (const uint32_t*)blk, mode + 1);
+      if (r == 0)
+        launch(c, k_pair_round<true>, pblocks, 128, 0, (const uint32_t*)sorted, src, ends_in, (const uint32_t*)st,
+               (uint32_t)nbins, cap[0], mode, T, pp, lst[0]);
+      else
+        launch(c, k_pair_round<false>, pblocks, 128, 0, (const uint32_t*)nullptr, (const Affine*)lst[(r - 1) & 1],
+               ends_in, (const uint32_t*)st, (uint32_t)nbins, cap[r], mode, T, pp, lst[r & 1]);
+      ends_in = st + 1;
+    }
+    pair_mode = mode;
+    pair_ends = ends_in;
+    pair_pts = lst[(kPairRounds - 1) & 1];
+  }
   launch(c, k_bucket_acc, blocks_for<int>(nseg, 128), 128, 0, (const uint32_t*)sorted, (const uint32_t*)counts,
-         (uint32_t)nbins, (const uint32_t*)total, nseg, src, buckets, ikeys[0], ipts[0], ipres[0]);
+         (uint32_t)nbins, (const uint32_t*)total, nseg, src, buckets, ikeys[0], ipts[0], ipres[0], pair_mode,
+         pair_ends, pair_pts);
   c.timer_end(APG_TIMER_MSM_ACCUMULATE, t_acc);
   {
     size_t len = 2 * nseg;

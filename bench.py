@@ -660,10 +660,10 @@ def run_gpu(args):
     fq_rate = ctx.probe_fq_mul_rate(300.0)
     algo = algorithmic_fqmul_accumulate(n)
     achieved = algo / (acc_ms / acc_n / 1e3)
-    own = n * own_windows(n, tuned) * 10
     traffic = ACC_TRAFFIC_BYTES.get(log2n)
     roofline = {
-        "bound": "int", "kernel": f"k_bucket_acc (bucket accumulation, 2^{log2n} uniform scalars)",
+        "bound": "int",
+        "kernel": f"bucket accumulation (k_pair_round x3 + k_bucket_acc), 2^{log2n} uniform scalars",
         "achieved": achieved / 1e9, "peak": fq_rate / 1e9, "unit": "G Fq-mul/s", "frac": achieved / fq_rate,
         "traffic": traffic,
         "peak_source": "measured on this device in this run: dependency-free Fq Montgomery products on every SM",
@@ -671,8 +671,10 @@ def run_gpu(args):
         "msm_uniform_points_per_s": n / (tot_ms / tot_n / 1e3), "algorithmic_fqmul_per_launch": algo,
         "algorithmic_basis": f"reference work: {reference_window_windows(n)[1]} windows x n mixed adds x 10 Fq-mul",
         "achieved_timad32_equiv": achieved * 264 / 1e12,
-        "own_fqmul_per_launch": own, "own_windows": own_windows(n, tuned),
-        "own_frac": own / (acc_ms / acc_n / 1e3) / fq_rate,
+        "own_windows": own_windows(n, tuned),
+        "own_work": "affine pair sums (5M + 1S and a share of one inversion a thread) for the first three "
+                    "halvings of every bucket, mixed XYZZ adds (8M + 2S) for the rest: fewer products than "
+                    "the reference basis, so frac may exceed 1",
     }
 
     shards = None

@@ -342,3 +342,37 @@ def test_commit_narrow_backings(ctx, bits):
     cm = ctx.commit_narrow(data, bits, nv)
     assert cm == O.g1_mul(O.G1_GEN, _f_tau(vals, tau))
     assert cm == ctx.commit(A.to_mont_bytes(vals), nv)
+
+
+@pytest.mark.parametrize("scalars_kind", ["uniform", "equal", "small"])
+def test_msm_large_degenerate_bases(ctx, scalars_kind):
+    """2^18 generic bases drawn from {infinity, G, -G, 2G, 3G, 7G}: inside a
+    bucket, adjacent points collide (P + P, P + (-P), infinity) in every way
+    the affine pair rounds classify. The value is (sum s_i k_i) * G."""
+    import apogee_gpu as A
+
+    rng = random.Random(77 + len(scalars_kind))
+    n = 1 << 18
+    ks = [0, 1, O.P_R - 1, 2, 3, 7]
+    pts = {k: (bytes(64) if k == 0 else O.g1_mul(O.G1_GEN, k)) for k in ks}
+    kk = [rng.choice(ks) for _ in range(n)]
+    if scalars_kind == "uniform":
+        ss = [rng.randrange(O.P_R) for _ in range(n)]
+    elif scalars_kind == "equal":
+        ss = [rng.randrange(O.P_R)] * n
+    else:
+        ss = [rng.randrange(1, 9) for _ in range(n)]
+    want = O.g1_mul(O.G1_GEN, sum(s * k for s, k in zip(ss, kk)) % O.P_R)
+    got = ctx.msm(b"".join(pts[k] for k in kk), A.to_mont_bytes(ss))
+    assert got == want
+
+
+def test_msm_large_one_point_all_doublings(ctx):
+    """Every base G and one scalar: each window's digit puts all 2^18 points in
+    one bucket, so every affine pair round is doublings only."""
+    import apogee_gpu as A
+
+    n = 1 << 18
+    s = random.Random(5).randrange(O.P_R)
+    got = ctx.msm(O.G1_GEN * n, A.to_mont_bytes([s] * n))
+    assert got == O.g1_mul(O.G1_GEN, s * n % O.P_R)
