@@ -753,74 +753,173 @@ __device__ __forceinline__ bool pair_denominator(const uint32_t* refs, const Aff
   return true;
 }
 
+// Field element shuffles across a full warp.
+__device__ __forceinline__ Fq shfl_up_fq(const Fq& a, int off) {
+  Fq r;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) r.v[w] = __shfl_up_sync(0xffffffffu, a.v[w], off);
+  return r;
+}
+__device__ __forceinline__ Fq shfl_down_fq(const Fq& a, int off) {
+  Fq r;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) r.v[w] = __shfl_down_sync(0xffffffffu, a.v[w], off);
+  return r;
+}
+__device__ __forceinline__ Fq shfl_fq(const Fq& a, int lane) {
+  Fq r;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) r.v[w] = __shfl_sync(0xffffffffu, a.v[w], lane);
+  return r;
+}
+
+// Each lane's 1/v (v != 0) from one inversion a warp: inclusive prefix and
+// suffix products across the lanes, the inverse of the warp's total product,
+// then 1/v_i = total^-1 * (product of the lanes before i) * (after i). Every
+// lane inverts the same total, so the inversion runs without divergence.
+// All 32 lanes must call it.
+__device__ __forceinline__ Fq warp_inverse(const Fq& v) {
+  const int lane = threadIdx.x & 31;
+  Fq pre = v, suf = v;
+#pragma unroll 1
+  for (int off = 1; off < 32; off <<= 1) {
+    const Fq a = shfl_up_fq(pre, off), b = shfl_down_fq(suf, off);
+    const Fq2 q = cmul2(pre, a, suf, b);
+    if (lane >= off) pre = q.a;
+    if (lane + off < 32) suf = q.b;
+  }
+  const Fq total = shfl_fq(pre, 31);
+  Fq ex = shfl_up_fq(pre, 1), sx = shfl_down_fq(suf, 1);
+  if (lane == 0) ex = fe_one<FqConsts>();
+  if (lane == 31) sx = fe_one<FqConsts>();
+  const Fq others = cmul(ex, sx);
+  return cmul(fe_inverse(total), others);
+}
+
+// The first bucket whose output reaches past slot o (o below the total).
+__device__ __forceinline__ uint32_t pair_bucket(const uint32_t* start_out, uint32_t nbins, size_t o) {
+  uint32_t a = 0, b = nbins - 1;
+  while (a < b) {
+    const uint32_t mid = (a + b) >> 1;
+    if (start_out[mid + 1] > o) b = mid;
+    else a = mid + 1;
+  }
+  return a;
+}
+
+// Slot o of bucket b reads input i0 and, when `two`, i0 + 1.
+__device__ __forceinline__ uint32_t pair_input(const uint32_t* ends_in, const uint32_t* start_out, uint32_t b,
+                                               size_t o, bool& two) {
+  const uint32_t i0 = (b ? ends_in[b - 1] : 0u) + 2u * (uint32_t)(o - start_out[b]);
+  two = i0 + 1 < ends_in[b];
+  return i0;
+}
+
+// One output slot of the backward pass: what it needs of its inputs (x0, y0,
+// x1), its kind, and the denominator and numerator of the slope when it has
+// one (1 and 0 otherwise, which leave the running inverse unchanged).
+struct PairSlot {
+  Fq x0, y0, x1, d, num;
+  uint32_t i0;
+  int kind;
+};
+
 template <bool REFS>
-__global__ void __launch_bounds__(128) k_pair_round(const uint32_t* refs, const Affine* src, const uint32_t* ends_in,
-                                                    const uint32_t* start_out, uint32_t nbins, size_t cap,
-                                                    uint32_t* mode, size_t T, Fq* pp, Affine* out) {
+__device__ __forceinline__ void pair_load(const uint32_t* refs, const Affine* src, uint32_t i0, bool two,
+                                          PairSlot& t) {
+  const Affine p0 = pair_point<REFS>(refs, src, i0);
+  Affine p1 = p0;
+  t.i0 = i0;
+  t.kind = kPairFirst;
+  if (two) {
+    p1 = pair_point<REFS>(refs, src, i0 + 1);
+    t.kind = pair_kind(p0, p1);
+  }
+  t.x0 = p0.x;
+  t.y0 = p0.y;
+  t.x1 = p1.x;
+  t.d = fe_one<FqConsts>();
+  t.num = fe_zero<FqConsts>();
+  if (t.kind == kPairAdd) {
+    t.d = fe_sub(p1.x, p0.x);
+    t.num = fe_sub(p1.y, p0.y);
+  } else if (t.kind == kPairDbl) {
+    t.d = fe_add(p0.y, p0.y);
+    const Fq q = csqr(p0.x);
+    t.num = fe_add(q, fe_add(q, q));
+  }
+}
+
+// The slot's sum, given the slope lam when it has one.
+template <bool REFS>
+__device__ __forceinline__ void pair_store(const uint32_t* refs, const Affine* src, const PairSlot& t,
+                                           const Fq& lam, const Fq& l2, Affine* dst) {
+  Fq x = t.x0, y = t.y0;
+  if (t.kind == kPairSecond) {
+    const Affine p1 = pair_point<REFS>(refs, src, t.i0 + 1);
+    x = p1.x;
+    y = p1.y;
+  } else if (t.kind == kPairInf) {
+    x = fe_zero<FqConsts>();
+    y = fe_zero<FqConsts>();
+  } else if (t.kind != kPairFirst) {
+    x = fe_sub(fe_sub(l2, t.x0), t.x1);
+    y = fe_sub(cmul(lam, fe_sub(t.x0, x)), t.y0);
+  }
+  st_fe(&dst->x, x);
+  st_fe(&dst->y, y);
+}
+
+// Five resident blocks a SM (96 registers): occupancy hides the gathers and
+// the serial product chain better than a second chain a thread (measured:
+// two interleaved chains needed 210 registers and ran slower).
+#ifndef APG_PAIR_MIN_BLOCKS
+#define APG_PAIR_MIN_BLOCKS 5
+#endif
+
+// A thread owns output slots [lo, hi): forward it multiplies up the slope
+// denominators (keeping the running products in pp[k * T + s]), the warp
+// shares one inversion, and backward each slot takes its inverse at two
+// products and writes its sum.
+template <bool REFS>
+__global__ void __launch_bounds__(128, APG_PAIR_MIN_BLOCKS)
+    k_pair_round(const uint32_t* refs, const Affine* src, const uint32_t* ends_in, const uint32_t* start_out,
+                 uint32_t nbins, size_t cap, uint32_t* mode, size_t T, Fq* pp, Affine* out) {
   const size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (s >= T || *mode) return;
+  if (*mode) return;  // uniform across the grid
   const size_t E = start_out[nbins];
-  if (E > cap) {
+  if (E > cap) {  // uniform too
     if (s == 0) *mode = 1;
     return;
   }
   const size_t m = (E + T - 1) / T;
-  const size_t lo = s * m;
-  if (lo >= E) return;
-  const size_t hi = min(lo + m, E);
-  uint32_t a = 0, bb = nbins - 1;  // the first bucket whose output reaches past lo
-  while (a < bb) {
-    const uint32_t mid = (a + bb) >> 1;
-    if (start_out[mid + 1] > lo) bb = mid;
-    else a = mid + 1;
-  }
-  uint32_t b = a;
+  const size_t lo = min(s * m, E), hi = min(lo + m, E);
+  uint32_t b = lo < hi ? pair_bucket(start_out, nbins, lo) : 0u;
   Fq acc = fe_one<FqConsts>();
   size_t k = 0;
   for (size_t o = lo; o < hi; ++o) {
     while (start_out[b + 1] <= o) ++b;
-    const uint32_t i0 = (b ? ends_in[b - 1] : 0u) + 2u * (uint32_t)(o - start_out[b]);
-    if (i0 + 1 >= ends_in[b]) continue;
+    bool two;
+    const uint32_t i0 = pair_input(ends_in, start_out, b, o, two);
     Fq d;
-    if (!pair_denominator<REFS>(refs, src, i0, d)) continue;
-    st_fe(&pp[k * T + s], acc);
+    if (!two || !pair_denominator<REFS>(refs, src, i0, d)) continue;
+    st_fe(&pp[k++ * T + s], acc);
     acc = cmul(acc, d);
-    ++k;
   }
-  Fq inv = fe_inverse(acc);
+  Fq inv = warp_inverse(acc);  // every lane of the warp reaches this
   for (size_t o = hi; o-- > lo;) {
     while (start_out[b] > o) --b;
-    const uint32_t i0 = (b ? ends_in[b - 1] : 0u) + 2u * (uint32_t)(o - start_out[b]);
-    const Affine p0 = pair_point<REFS>(refs, src, i0);
-    Affine r = p0;
-    if (i0 + 1 < ends_in[b]) {
-      const Affine p1 = pair_point<REFS>(refs, src, i0 + 1);
-      const int kind = pair_kind(p0, p1);
-      if (kind == kPairSecond) {
-        r = p1;
-      } else if (kind == kPairInf) {
-        r.x = fe_zero<FqConsts>();
-        r.y = fe_zero<FqConsts>();
-      } else if (kind != kPairFirst) {
-        Fq d, num;
-        if (kind == kPairAdd) {
-          d = fe_sub(p1.x, p0.x);
-          num = fe_sub(p1.y, p0.y);
-        } else {
-          d = fe_add(p0.y, p0.y);
-          const Fq t = csqr(p0.x);
-          num = fe_add(t, fe_add(t, t));
-        }
-        --k;
-        const Fq2 q = cmul2(inv, ld_fe(&pp[k * T + s]), inv, d);  // 1/d, and 1/(d_1..d_{k-1})
-        inv = q.b;
-        const Fq lam = cmul(num, q.a);
-        r.x = fe_sub(fe_sub(csqr(lam), p0.x), p1.x);
-        r.y = fe_sub(cmul(lam, fe_sub(p0.x, r.x)), p0.y);
-      }
+    bool two;
+    PairSlot t;
+    pair_load<REFS>(refs, src, pair_input(ends_in, start_out, b, o, two), two, t);
+    if (t.kind < kPairAdd) {
+      pair_store<REFS>(refs, src, t, t.num, t.num, &out[o]);
+      continue;
     }
-    st_fe(&out[o].x, r.x);
-    st_fe(&out[o].y, r.y);
+    const Fq2 di = cmul2(inv, ld_fe(&pp[--k * T + s]), inv, t.d);  // 1/d, and the running inverse one back
+    inv = di.b;
+    const Fq lam = cmul(t.num, di.a);
+    pair_store<REFS>(refs, src, t, lam, csqr(lam), &out[o]);
   }
 }
 
