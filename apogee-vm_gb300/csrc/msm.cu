@@ -877,10 +877,12 @@ __device__ __forceinline__ void pair_store(const uint32_t* refs, const Affine* s
 #define APG_PAIR_MIN_BLOCKS 5
 #endif
 
-// A thread owns output slots [lo, hi): forward it multiplies up the slope
-// denominators (keeping the running products in pp[k * T + s]), the warp
-// shares one inversion, and backward each slot takes its inverse at two
-// products and writes its sum.
+// A warp owns 32 * m consecutive output slots and lane l takes slots
+// base + 32 j + l, so the lanes' references, explicit input points, running
+// products and outputs are read and written in coalesced rows. Forward a lane
+// multiplies up its slope denominators (the running products in pp[k * T + s]),
+// the warp shares one inversion, and backward each slot takes its inverse at
+// two products and writes its sum.
 template <bool REFS>
 __global__ void __launch_bounds__(128, APG_PAIR_MIN_BLOCKS)
     k_pair_round(const uint32_t* refs, const Affine* src, const uint32_t* ends_in, const uint32_t* start_out,
@@ -893,11 +895,13 @@ __global__ void __launch_bounds__(128, APG_PAIR_MIN_BLOCKS)
     return;
   }
   const size_t m = (E + T - 1) / T;
-  const size_t lo = min(s * m, E), hi = min(lo + m, E);
-  uint32_t b = lo < hi ? pair_bucket(start_out, nbins, lo) : 0u;
+  const size_t o0 = (s / 32) * 32 * m + (s & 31);
+  const size_t steps = o0 < E ? min(m, (E - o0 + 31) / 32) : 0;
+  uint32_t b = steps ? pair_bucket(start_out, nbins, o0) : 0u;
   Fq acc = fe_one<FqConsts>();
   size_t k = 0;
-  for (size_t o = lo; o < hi; ++o) {
+  for (size_t j = 0; j < steps; ++j) {
+    const size_t o = o0 + 32 * j;
     while (start_out[b + 1] <= o) ++b;
     bool two;
     const uint32_t i0 = pair_input(ends_in, start_out, b, o, two);
@@ -907,7 +911,8 @@ __global__ void __launch_bounds__(128, APG_PAIR_MIN_BLOCKS)
     acc = cmul(acc, d);
   }
   Fq inv = warp_inverse(acc);  // every lane of the warp reaches this
-  for (size_t o = hi; o-- > lo;) {
+  for (size_t j = steps; j-- > 0;) {
+    const size_t o = o0 + 32 * j;
     while (start_out[b] > o) --b;
     bool two;
     PairSlot t;
