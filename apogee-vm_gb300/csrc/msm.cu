@@ -716,6 +716,16 @@ __device__ __forceinline__ Affine pair_point(const uint32_t* refs, const Affine*
 
 enum : int { kPairFirst = 0, kPairSecond = 1, kPairInf = 2, kPairAdd = 3, kPairDbl = 4 };
 
+// The pair rounds' products are inlined (unlike the XYZZ formulas, whose ten
+// inlined products a step overflowed the instruction cache): the compiler
+// interleaves the independent ones, measured 2 % faster than calls.
+__device__ __forceinline__ Fq2 pmul2(const Fq& a, const Fq& b, const Fq& c, const Fq& d) {
+  Fq2 r;
+  r.a = fe_mul(a, b);
+  r.b = fe_mul(c, d);
+  return r;
+}
+
 // What the pair (p0, p1) sums to: p0 or p1 when the other is infinity, the
 // point at infinity for P + (-P), else an addition or a doubling.
 __device__ __forceinline__ int pair_kind(const Affine& p0, const Affine& p1) {
@@ -845,7 +855,7 @@ __device__ __forceinline__ void pair_load(const uint32_t* refs, const Affine* sr
     t.num = fe_sub(p1.y, p0.y);
   } else if (t.kind == kPairDbl) {
     t.d = fe_add(p0.y, p0.y);
-    const Fq q = csqr(p0.x);
+    const Fq q = fe_sqr(p0.x);
     t.num = fe_add(q, fe_add(q, q));
   }
 }
@@ -864,7 +874,7 @@ __device__ __forceinline__ void pair_store(const uint32_t* refs, const Affine* s
     y = fe_zero<FqConsts>();
   } else if (t.kind != kPairFirst) {
     x = fe_sub(fe_sub(l2, t.x0), t.x1);
-    y = fe_sub(cmul(lam, fe_sub(t.x0, x)), t.y0);
+    y = fe_sub(fe_mul(lam, fe_sub(t.x0, x)), t.y0);
   }
   st_fe(&dst->x, x);
   st_fe(&dst->y, y);
@@ -908,7 +918,7 @@ __global__ void __launch_bounds__(128, APG_PAIR_MIN_BLOCKS)
     Fq d;
     if (!two || !pair_denominator<REFS>(refs, src, i0, d)) continue;
     st_fe(&pp[k++ * T + s], acc);
-    acc = cmul(acc, d);
+    acc = fe_mul(acc, d);
   }
   Fq inv = warp_inverse(acc);  // every lane of the warp reaches this
   for (size_t j = steps; j-- > 0;) {
@@ -921,10 +931,10 @@ __global__ void __launch_bounds__(128, APG_PAIR_MIN_BLOCKS)
       pair_store<REFS>(refs, src, t, t.num, t.num, &out[o]);
       continue;
     }
-    const Fq2 di = cmul2(inv, ld_fe(&pp[--k * T + s]), inv, t.d);  // 1/d, and the running inverse one back
+    const Fq2 di = pmul2(inv, ld_fe(&pp[--k * T + s]), inv, t.d);  // 1/d, and the running inverse one back
     inv = di.b;
-    const Fq lam = cmul(t.num, di.a);
-    pair_store<REFS>(refs, src, t, lam, csqr(lam), &out[o]);
+    const Fq lam = fe_mul(t.num, di.a);
+    pair_store<REFS>(refs, src, t, lam, fe_sqr(lam), &out[o]);
   }
 }
 
