@@ -127,10 +127,11 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-# DRAM bytes (read + write) of one bucket-accumulation launch of a 2^22-point
-# uniform-scalar commit: one ncu capture of the 2^20 case (1.767 GB read +
-# 0.076 GB written for 13 x 2^20 references) scaled x4 to 13 x 2^22.
-ACC_TRAFFIC_BYTES = {22: 7.371e9}
+# DRAM bytes (read + write) of the bucket-accumulation phase (three affine
+# pair rounds with their scans, then the XYZZ tail) of a 2^22-point
+# uniform-scalar commit at 18-bit windows: one ncu capture of the 2^20 case
+# (7.259 GB for 15 x 2^20 references) scaled x4 to 15 x 2^22.
+ACC_TRAFFIC_BYTES = {22: 2.9035e10}
 
 
 def cpu_msm_points_per_s(bases: bytes, scalars: bytes, n: int, threads: int, reps: int = 3):
