@@ -817,6 +817,50 @@ __device__ __forceinline__ uint32_t pair_bucket(const uint32_t* start_out, uint3
   return a;
 }
 
+// The bucket holding output slot o, from the bucket b of an earlier (seek_up)
+// or later (seek_down) slot of the same lane. A lane's slots are 32 apart, so
+// where most buckets are empty (a short column grouped with a long one) the
+// cursor may pass many buckets in one step: it gallops (1, 2, 4, ... buckets)
+// and then bisects, one comparison where buckets are dense.
+__device__ __forceinline__ uint32_t pair_seek_up(const uint32_t* start_out, uint32_t nbins, uint32_t b, size_t o) {
+  if (start_out[b + 1] > o) return b;
+  uint32_t lo = b + 1, hi, step = 1;  // start_out[lo] <= o: the bucket is at or past lo
+  for (;;) {
+    hi = lo + step;
+    if (hi >= nbins - 1 || start_out[hi + 1] > o) break;
+    lo = hi + 1;
+    step <<= 1;
+  }
+  hi = min(hi, nbins - 1);
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (start_out[mid + 1] > o) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ uint32_t pair_seek_down(const uint32_t* start_out, uint32_t b, size_t o) {
+  if (start_out[b] <= o) return b;
+  uint32_t hi = b - 1, lo, step = 1;  // the bucket is at or before hi
+  for (;;) {
+    if (hi < step) {
+      lo = 0;
+      break;
+    }
+    lo = hi - step;
+    if (start_out[lo] <= o) break;
+    hi = lo - 1;
+    step <<= 1;
+  }
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (start_out[mid] <= o) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 // Slot o of bucket b reads input i0 and, when `two`, i0 + 1.
 __device__ __forceinline__ uint32_t pair_input(const uint32_t* ends_in, const uint32_t* start_out, uint32_t b,
                                                size_t o, bool& two) {
@@ -912,7 +956,7 @@ __global__ void __launch_bounds__(128, APG_PAIR_MIN_BLOCKS)
   size_t k = 0;
   for (size_t j = 0; j < steps; ++j) {
     const size_t o = o0 + 32 * j;
-    while (start_out[b + 1] <= o) ++b;
+    b = pair_seek_up(start_out, nbins, b, o);
     bool two;
     const uint32_t i0 = pair_input(ends_in, start_out, b, o, two);
     Fq d;
@@ -923,7 +967,7 @@ __global__ void __launch_bounds__(128, APG_PAIR_MIN_BLOCKS)
   Fq inv = warp_inverse(acc);  // every lane of the warp reaches this
   for (size_t j = steps; j-- > 0;) {
     const size_t o = o0 + 32 * j;
-    while (start_out[b] > o) --b;
+    b = pair_seek_down(start_out, b, o);
     bool two;
     PairSlot t;
     pair_load<REFS>(refs, src, pair_input(ends_in, start_out, b, o, two), two, t);

@@ -96,8 +96,10 @@ def _oracle_open(srs, vals, nv, cm, u, snap):
     return O.fe_int(v.raw), proof.raw
 
 
-@pytest.mark.parametrize("nv", [2, 4, 6, 8, 10, 12])
+@pytest.mark.parametrize("nv", [2, 4, 6, 8, 10, 12, 18])
 def test_open_matches_oracle(ctx, nv):
+    """nv = 18 runs the quotient MSMs through the affine pair rounds: q (2^18 - 2^9
+    points) and g (2^9) share one group, so g's bucket range is almost empty."""
     import apogee_gpu as A
 
     rng = random.Random(900 + nv)
