@@ -83,6 +83,21 @@ def fe(x: int) -> bytes:
     return int(x).to_bytes(32, "little")
 
 
+def narrow_bytes(values, bits: int) -> bytes:
+    """A column's stored form (PolyBacking, crates/poly/src/lib.rs:44-57):
+    bits 1 a bitset in u64 limbs (entry i = bit i % 64 of limb i / 64),
+    8/16/32 little-endian unsigned integers, 0 Fr in memory."""
+    if bits == 0:
+        return to_mont_bytes(values)
+    if bits == 1:
+        limbs = [0] * ((len(values) + 63) // 64)
+        for i, v in enumerate(values):
+            if v:
+                limbs[i // 64] |= 1 << (i % 64)
+        return b"".join(x.to_bytes(8, "little") for x in limbs)
+    return b"".join(int(v).to_bytes(bits // 8, "little") for v in values)
+
+
 def struct_u32(blob: bytes, off: int) -> int:
     return int.from_bytes(blob[off:off + 4], "little")
 
@@ -405,7 +420,43 @@ class Context:
         rs = from_mont_bytes(rounds.raw[:128 * num_vars])
         return [rs[4 * i:4 * i + 4] for i in range(num_vars)], from_mont_bytes(finals.raw), snap.raw
 
+    def prove_zerocheck_narrow(self, terms, polys, bits, num_vars: int, transcript: bytes, on_device: bool = False):
+        """prove_zerocheck over columns in their stored widths: polys[k] the
+        column's bytes (a bitset in u64 limbs for bits 1, little-endian
+        unsigned integers for 8/16/32, Fr in memory for 0) or device pointers
+        with on_device. Returns what prove_zerocheck returns."""
+        nt = len(terms)
+        coefs = to_mont_bytes([t[0] for t in terms])
+        ta = (ctypes.c_uint32 * max(nt, 1))(*[t[1] for t in terms])
+        tb = (ctypes.c_uint32 * max(nt, 1))(*[0xFFFFFFFF if t[2] is None else t[2] for t in terms])
+        k = len(polys)
+        snap = ctypes.create_string_buffer(bytes(transcript), TRANSCRIPT_BYTES)
+        rounds = ctypes.create_string_buffer(128 * max(num_vars, 1))
+        finals = ctypes.create_string_buffer(32 * k)
+        ptrs = (ctypes.c_void_p * k)(*polys) if on_device else (ctypes.c_char_p * k)(*polys)
+        barr = (ctypes.c_uint8 * k)(*bits)
+        self._check(lib().apg_prove_zerocheck_narrow(self._h, ctypes.c_size_t(k), coefs, ta, tb, ctypes.c_size_t(nt),
+                                                     ptrs, barr, 1 if on_device else 0, ctypes.c_size_t(num_vars),
+                                                     snap, rounds, finals))
+        rs = from_mont_bytes(rounds.raw[:128 * num_vars])
+        return [rs[4 * i:4 * i + 4] for i in range(num_vars)], from_mont_bytes(finals.raw), snap.raw
+
     # ---- GKR ------------------------------------------------------------------
+    def gkr_forward_narrow(self, blob: bytes, base, bits, challenges: dict, on_device: bool = False):
+        """gkr::forward over committed columns in their stored widths (see
+        prove_zerocheck_narrow for the byte forms). Returns a GkrValues handle."""
+        k = len(base)
+        slots = sorted(challenges)
+        sarr = (ctypes.c_uint32 * max(len(slots), 1))(*slots)
+        vals = to_mont_bytes([challenges[s] for s in slots])
+        h = ctypes.c_void_p()
+        ptrs = (ctypes.c_void_p * k)(*base) if on_device else (ctypes.c_char_p * k)(*base)
+        barr = (ctypes.c_uint8 * k)(*bits)
+        self._check(lib().apg_gkr_forward_narrow(self._h, blob, ctypes.c_size_t(len(blob)), ptrs, barr,
+                                                 1 if on_device else 0, sarr, vals, ctypes.c_size_t(len(slots)),
+                                                 ctypes.byref(h)))
+        return GkrValues(self, h)
+
     def gkr_forward(self, blob: bytes, base, challenges: dict, on_device: bool = False):
         """gkr::forward. base: committed columns as Fr in-memory bytes (layout
         order), or device pointers with on_device; challenges: {slot:

@@ -517,6 +517,17 @@ int apg_prove_zerocheck_device(apg_ctx* ctx, size_t arity, const uint8_t* coefs,
   });
 }
 
+int apg_prove_zerocheck_narrow(apg_ctx* ctx, size_t arity, const uint8_t* coefs, const uint32_t* a,
+                               const uint32_t* b, size_t nterms, const void* const* polys, const uint8_t* bits,
+                               int polys_on_device, size_t num_vars, uint8_t* transcript, uint8_t* rounds_out,
+                               uint8_t* finals_out) {
+  if (!bits) return APG_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&](Ctx& c) {
+    return prove_zerocheck_impl(c, arity, coefs, a, b, nterms, (const uint8_t* const*)polys, polys_on_device != 0,
+                                num_vars, transcript, rounds_out, finals_out, bits);
+  });
+}
+
 int apg_witness_digest(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_t num_vars, uint8_t out[32]) {
   return guarded(ctx, [&](Ctx& c) { return witness_digest_impl(c, cols, k, num_vars, out); });
 }
@@ -621,7 +632,8 @@ int apg_gkr_forward(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, co
   if (!out) return APG_ERR_INVALID_ARGUMENT;
   *out = nullptr;
   return guarded(ctx, [&](Ctx& c) {
-    GkrValues* v = gkr_forward_impl(c, circuit, circuit_len, base, false, slots, slot_values, n_slots);
+    GkrValues* v = gkr_forward_impl(c, circuit, circuit_len, (const void* const*)base, nullptr, false, slots,
+                                    slot_values, n_slots);
     *out = new apg_gkr_values{v, ctx};
     return (int)APG_OK;
   });
@@ -670,7 +682,20 @@ int apg_gkr_forward_device(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_
   if (!out) return APG_ERR_INVALID_ARGUMENT;
   *out = nullptr;
   return guarded(ctx, [&](Ctx& c) {
-    GkrValues* v = gkr_forward_impl(c, circuit, circuit_len, (const uint8_t* const*)d_base, true, slots, slot_values,
+    GkrValues* v = gkr_forward_impl(c, circuit, circuit_len, d_base, nullptr, true, slots, slot_values, n_slots);
+    *out = new apg_gkr_values{v, ctx};
+    return (int)APG_OK;
+  });
+}
+
+int apg_gkr_forward_narrow(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, const void* const* base,
+                           const uint8_t* bits, int base_on_device, const uint32_t* slots,
+                           const uint8_t* slot_values, size_t n_slots, apg_gkr_values** out) {
+  if (!out) return APG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (!bits) return APG_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&](Ctx& c) {
+    GkrValues* v = gkr_forward_impl(c, circuit, circuit_len, base, bits, base_on_device != 0, slots, slot_values,
                                     n_slots);
     *out = new apg_gkr_values{v, ctx};
     return (int)APG_OK;

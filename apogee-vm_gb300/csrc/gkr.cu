@@ -219,16 +219,18 @@ namespace {
 
 constexpr int kFwdThreads = 64;
 
+// `bits` (null: all Fr) is the stored width of each column of the base.
 __global__ void __launch_bounds__(kFwdThreads) k_forward(DevProgram P, int w, int nv, VirtualKinds vk,
-                                                         const Fr* const* cols, size_t rows, int halving,
-                                                         int width, Fr* out) {
+                                                         const Fr* const* cols, const uint8_t* bits, size_t rows,
+                                                         int halving, int width, Fr* out) {
   extern __shared__ uint32_t sm_raw[];
   const Slots sm = thread_slots(sm_raw);
   size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (y >= rows) return;
   for (int x = 0; x < w; ++x) {
-    sm_st(sm, x, ld_fe(&cols[x][y]));
-    if (halving) sm_st(sm, w + x, ld_fe(&cols[x][y + rows]));
+    const int b = bits ? bits[x] : 0;
+    sm_st(sm, x, b ? narrow_entry(cols[x], b, y) : ld_fe(&cols[x][y]));
+    if (halving) sm_st(sm, w + x, b ? narrow_entry(cols[x], b, y + rows) : ld_fe(&cols[x][y + rows]));
   }
   for (int v = 0; v < nv; ++v) sm_st(sm, w + v, virtual_at_row_dev(vk.k[v], y));
   for (int g = 0; g < P.n_cached; ++g) sm_st(sm, P.cached_slot0 + g, eval_gate_dev(P, g, sm));
@@ -237,15 +239,36 @@ __global__ void __launch_bounds__(kFwdThreads) k_forward(DevProgram P, int w, in
 
 }  // namespace
 
+// Layer k >= 1: width(k) Fr columns of 2^vars(k), contiguous. Layer 0, the
+// committed base, keeps every column in its stored width (base_bits, 0 = Fr)
+// at base_off bytes: the forward pass and gate list 0's first sumcheck rounds
+// read narrow columns through the lift. What needs the base as Fr tables
+// (reading it back, a halving list over it) lifts it once, on demand.
 struct GkrValues {
   Ctx* ctx = nullptr;
   Circuit circuit;
-  std::vector<Fr*> layers;  // layer k: width(k) columns of 2^vars(k), contiguous
+  std::vector<Fr*> layers;
+  std::vector<size_t> base_off;
+  std::vector<uint8_t> base_bits;
+  bool base_narrow = false;
+  Fr* lifted = nullptr;
   ~GkrValues() {
     for (auto p : layers)
       if (p) cudaFree(p);
+    if (lifted) cudaFree(lifted);
   }
-  const Fr* col(size_t k, size_t x) const { return layers[k] + x * ((size_t)1 << circuit.vars(k)); }
+  const void* base_raw(size_t x) const { return reinterpret_cast<const uint8_t*>(layers[0]) + base_off[x]; }
+  const Fr* col(size_t k, size_t x) {
+    const size_t rows = (size_t)1 << circuit.vars(k);
+    if (k > 0) return layers[k] + x * rows;
+    if (!base_narrow) return reinterpret_cast<const Fr*>(base_raw(x));
+    if (!lifted) {
+      APG_CUDA(cudaMalloc(&lifted, 32 * rows * circuit.n_committed));
+      for (size_t j = 0; j < circuit.n_committed; ++j)
+        lift_column(*ctx, base_raw(j), base_bits[j], rows, lifted + j * rows);
+    }
+    return lifted + x * rows;
+  }
 };
 
 static Challenges read_challenges(const uint32_t* slots, const uint8_t* values, size_t n) {
@@ -259,8 +282,9 @@ static Challenges read_challenges(const uint32_t* slots, const uint8_t* values, 
   return ch;
 }
 
-GkrValues* gkr_forward_impl(Ctx& c, const uint8_t* blob, size_t blob_len, const uint8_t* const* base,
-                            bool base_on_device, const uint32_t* slots, const uint8_t* slot_values, size_t n_slots) {
+GkrValues* gkr_forward_impl(Ctx& c, const uint8_t* blob, size_t blob_len, const void* const* base,
+                            const uint8_t* bits, bool base_on_device, const uint32_t* slots,
+                            const uint8_t* slot_values, size_t n_slots) {
   std::unique_ptr<GkrValues> V(new GkrValues());
   V->ctx = &c;
   V->circuit = parse_circuit_blob(blob, blob_len);
@@ -269,10 +293,31 @@ GkrValues* gkr_forward_impl(Ctx& c, const uint8_t* blob, size_t blob_len, const 
   Challenges ch = read_challenges(slots, slot_values, n_slots);
   const size_t n0 = (size_t)1 << C.trace_vars;
   V->layers.assign(C.layers.size() + 1, nullptr);
-  APG_CUDA(cudaMalloc(&V->layers[0], 32 * n0 * C.n_committed));
+  // The base in its stored widths, each column 256-byte aligned.
+  V->base_bits.assign(C.n_committed, 0);
+  V->base_off.assign(C.n_committed, 0);
+  size_t total = 0;
+  for (size_t x = 0; x < C.n_committed; ++x) {
+    if (bits) {
+      if (!narrow_bits_ok(bits[x])) throw Error(APG_ERR_INVALID_ARGUMENT, "a column width other than 0, 1, 8, 16, 32");
+      V->base_bits[x] = bits[x];
+      V->base_narrow |= bits[x] != 0;
+    }
+    if (!base[x]) throw Error(APG_ERR_INVALID_ARGUMENT, "null column");
+    V->base_off[x] = total;
+    total += (narrow_bytes(V->base_bits[x], n0) + 255) / 256 * 256;
+  }
+  APG_CUDA(cudaMalloc(&V->layers[0], std::max<size_t>(total, 256)));
   for (size_t x = 0; x < C.n_committed; ++x)
-    APG_CUDA(cudaMemcpyAsync(V->layers[0] + x * n0, base[x], 32 * n0,
+    APG_CUDA(cudaMemcpyAsync(reinterpret_cast<uint8_t*>(V->layers[0]) + V->base_off[x], base[x],
+                             narrow_bytes(V->base_bits[x], n0),
                              base_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c.stream));
+  const uint8_t* d_bits = nullptr;
+  if (V->base_narrow) {
+    uint8_t* db = c.scratch[S_ENTRIES].as<uint8_t>(C.n_committed);
+    APG_CUDA(cudaMemcpyAsync(db, V->base_bits.data(), C.n_committed, cudaMemcpyHostToDevice, c.stream));
+    d_bits = db;
+  }
   for (size_t k = 0; k < C.layers.size(); ++k) {
     const CLayer& L = C.layers[k];
     const size_t rows = (size_t)1 << L.num_vars;
@@ -287,7 +332,8 @@ GkrValues* gkr_forward_impl(Ctx& c, const uint8_t* blob, size_t blob_len, const 
     memset(&vk, 0, sizeof(vk));
     for (int v = 0; v < nv; ++v) vk.k[v] = (uint8_t)C.virtuals[v];
     std::vector<const Fr*> cols(w);
-    for (int x = 0; x < w; ++x) cols[x] = V->col(k, x);
+    for (int x = 0; x < w; ++x)
+      cols[x] = k == 0 ? reinterpret_cast<const Fr*>(V->base_raw(x)) : V->col(k, x);
     const Fr** d_cols = c.scratch[S_TMP5].as<const Fr*>(w);
     APG_CUDA(cudaMemcpyAsync(d_cols, cols.data(), sizeof(Fr*) * w, cudaMemcpyHostToDevice, c.stream));
     const size_t slots_n = (size_t)P.cached_slot0 + L.cached.size();
@@ -299,7 +345,8 @@ GkrValues* gkr_forward_impl(Ctx& c, const uint8_t* blob, size_t blob_len, const 
     cudaEvent_t t0 = c.timer_begin();
     if (L.width)
       launch(c, k_forward, (unsigned)((rows + threads - 1) / threads), threads, smem, P, w, nv, vk,
-             (const Fr* const*)d_cols, rows, L.halving ? 1 : 0, (int)L.width, V->layers[k + 1]);
+             (const Fr* const*)d_cols, k == 0 ? d_bits : (const uint8_t*)nullptr, rows, L.halving ? 1 : 0,
+             (int)L.width, V->layers[k + 1]);
     c.timer_end(APG_TIMER_GKR_FORWARD, t0);
     // The program and column list buffers are reused by the next layer.
     APG_CUDA(cudaStreamSynchronize(c.stream));
@@ -372,18 +419,24 @@ int gkr_prove_impl(Ctx& c, const uint8_t* blob, size_t blob_len, GkrValues* V, c
     // L2: the tables, child 0 then child 1 of every column for a halving list.
     const uint32_t w = C.width(kk);
     std::vector<const Fr*> src;
-    std::vector<uint8_t> vkinds;
+    std::vector<uint8_t> vkinds, src_bits;
     if (L.halving) {
       const size_t half = (size_t)1 << (C.vars(kk) - 1);
       for (uint32_t x = 0; x < w; ++x) src.push_back(V->col(kk, x));
       for (uint32_t x = 0; x < w; ++x) src.push_back(V->col(kk, x) + half);
+    } else if (kk == 0 && V->base_narrow) {
+      // The base in its stored widths: the first bind lifts it.
+      for (uint32_t x = 0; x < w; ++x) src.push_back(reinterpret_cast<const Fr*>(V->base_raw(x)));
+      src_bits = V->base_bits;
+      for (auto k : C.virtuals) vkinds.push_back((uint8_t)k);
     } else {
       for (uint32_t x = 0; x < w; ++x) src.push_back(V->col(kk, x));
       for (auto k : C.virtuals) vkinds.push_back((uint8_t)k);
     }
     std::vector<std::array<F, 4>> rounds;
     std::vector<F> rho, finals;
-    run_sumcheck(c, P, (int)src.size(), vkinds, (int)L.cached.size(), src, point, tr, rounds, rho, finals);
+    run_sumcheck(c, P, (int)src.size(), vkinds, (int)L.cached.size(), src, point, tr, rounds, rho, finals,
+                 src_bits);
     // L3.
     std::vector<F> claims;
     if (L.halving) {

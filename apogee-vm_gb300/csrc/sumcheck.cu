@@ -35,6 +35,7 @@ struct RoundArgs {
   unsigned* done;            // blocks finished this round (zero between rounds)
   Fr* out;                   // the round's 4 sums, written by the last block
   int xsplit;                // one thread per (pair, node X) instead of per pair
+  const uint8_t* src_bits;   // stored width of each src table (null: all Fr)
 };
 
 __device__ __forceinline__ const Fr* table_in(const RoundArgs& A, int k) {
@@ -46,12 +47,24 @@ __device__ __forceinline__ const Fr* table_in(const RoundArgs& A, int k) {
 // folded pair is stored when `store` is set).
 __device__ __forceinline__ void load_line(const RoundArgs& A, int k, size_t i, Fr& lo, Fr& hi, bool store = true) {
   const Fr* t = table_in(A, k);
+  const int bits = A.in_is_src && A.src_bits ? A.src_bits[k] : 0;
   if (!A.bind) {
-    lo = ld_fe(&t[2 * i]);
-    hi = ld_fe(&t[2 * i + 1]);
+    lo = bits ? narrow_entry(t, bits, 2 * i) : ld_fe(&t[2 * i]);
+    hi = bits ? narrow_entry(t, bits, 2 * i + 1) : ld_fe(&t[2 * i + 1]);
     return;
   }
-  Fr a0 = ld_fe(&t[4 * i]), a1 = ld_fe(&t[4 * i + 1]), a2 = ld_fe(&t[4 * i + 2]), a3 = ld_fe(&t[4 * i + 3]);
+  Fr a0, a1, a2, a3;
+  if (bits) {
+    a0 = narrow_entry(t, bits, 4 * i);
+    a1 = narrow_entry(t, bits, 4 * i + 1);
+    a2 = narrow_entry(t, bits, 4 * i + 2);
+    a3 = narrow_entry(t, bits, 4 * i + 3);
+  } else {
+    a0 = ld_fe(&t[4 * i]);
+    a1 = ld_fe(&t[4 * i + 1]);
+    a2 = ld_fe(&t[4 * i + 2]);
+    a3 = ld_fe(&t[4 * i + 3]);
+  }
   lo = fe_add(a0, fe_mul(A.c, fe_sub(a1, a0)));
   hi = fe_add(a2, fe_mul(A.c, fe_sub(a3, a2)));
   if (!store) return;
@@ -246,13 +259,26 @@ __global__ void __launch_bounds__(kRoundThreads) k_round_warp(RoundArgs A, DevPr
 }
 
 // Tables of length 2 -> their bound value (the last round's fold).
-__global__ void k_final_bind(const Fr* const* src, const Fr* in_base, size_t in_len, int in_is_src, int nt, Fr c,
-                             Fr* out) {
+// With no rounds at all (a one-entry table) c is ignored and the entry itself
+// is the value.
+__global__ void k_final_bind(const Fr* const* src, const uint8_t* src_bits, const Fr* in_base, size_t in_len,
+                             int in_is_src, int nt, Fr c, int no_rounds, Fr* out) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nt) return;
   const Fr* t = in_is_src ? src[k] : in_base + (size_t)k * in_len;
-  Fr a0 = ld_fe(&t[0]), a1 = ld_fe(&t[1]);
+  const int bits = in_is_src && src_bits ? src_bits[k] : 0;
+  const Fr a0 = bits ? narrow_entry(t, bits, 0) : ld_fe(&t[0]);
+  if (no_rounds) {
+    st_fe(&out[k], a0);
+    return;
+  }
+  const Fr a1 = bits ? narrow_entry(t, bits, 1) : ld_fe(&t[1]);
   st_fe(&out[k], fe_add(a0, fe_mul(c, fe_sub(a1, a0))));
+}
+
+__global__ void k_lift(const void* p, int bits, size_t n, Fr* out) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) st_fe(&out[i], narrow_entry(p, bits, i));
 }
 
 // eq(r, y) for every y < 2^n: prod_j (y_j ? r_j : 1 - r_j).
@@ -291,6 +317,10 @@ static Fr to_dev(const F& a) {
 // eq(r, y) for every y < 2^|r|. Up to 12 variables each entry is its own
 // product of |r| factors; beyond, the two halves' tables (2^(n/2) entries
 // each) are built that way and every entry is one product of the two.
+void lift_column(Ctx& c, const void* p, int bits, size_t n, Fr* out) {
+  if (n) launch(c, k_lift, (unsigned)((n + 255) / 256), 256, 0, p, bits, n, out);
+}
+
 void build_eq_table(Ctx& c, const std::vector<F>& r, Fr* out) {
   const int n = (int)r.size();
   const size_t len = (size_t)1 << n;
@@ -337,7 +367,8 @@ static VirtualRound virtual_round(const std::vector<F>& point, int nvars) {
 
 void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint8_t>& vkinds, int n_cached,
                   const std::vector<const Fr*>& src, const std::vector<F>& eq_point, host::Transcript& tr,
-                  std::vector<std::array<F, 4>>& rounds, std::vector<F>& point, std::vector<F>& finals) {
+                  std::vector<std::array<F, 4>>& rounds, std::vector<F>& point, std::vector<F>& finals,
+                  const std::vector<uint8_t>& src_bits) {
   const int n = (int)eq_point.size();
   const int nt = nd + 1;  // with eq
   if (vkinds.size() > 8) throw Error(APG_ERR_BAD_CIRCUIT, "more than 8 virtual tables");
@@ -353,6 +384,19 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
   srcs.push_back(eq);
   const Fr** d_src = c.scratch[S_TMP5].as<const Fr*>(nt);
   APG_CUDA(cudaMemcpyAsync(d_src, srcs.data(), sizeof(Fr*) * nt, cudaMemcpyHostToDevice, c.stream));
+  // Stored widths of the data tables, when any is narrow (eq is Fr).
+  const uint8_t* d_bits = nullptr;
+  bool narrow = false;
+  for (uint8_t b : src_bits) narrow |= b != 0;
+  if (narrow) {
+    if ((int)src_bits.size() != nd) throw Error(APG_ERR_INTERNAL, "one width per data table");
+    std::vector<uint8_t> bits(src_bits);
+    bits.push_back(0);
+    uint8_t* db = c.scratch[S_ENTRIES].as<uint8_t>(nt);
+    APG_CUDA(cudaMemcpyAsync(db, bits.data(), nt, cudaMemcpyHostToDevice, c.stream));
+    APG_CUDA(cudaStreamSynchronize(c.stream));  // `bits` is a host temporary
+    d_bits = db;
+  }
 
   // Level buffers: level r (r >= 1) holds nt tables of 2^(n-r) entries.
   Fr* lvl[2] = {nullptr, nullptr};
@@ -410,6 +454,7 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
     // Rounds too small to fill the device evaluate the four nodes of a pair
     // on four threads.
     A.xsplit = A.npairs * 4 <= (size_t)threads * max_blocks ? 1 : 0;
+    A.src_bits = d_bits;
     const size_t work = A.xsplit ? A.npairs * 4 : A.npairs;
     const int blocks = warp_mode
                            ? (int)std::min<size_t>((A.npairs + kRoundThreads / 32 - 1) / (kRoundThreads / 32),
@@ -429,13 +474,10 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
   }
   // The last fold: every table bound to the full point.
   Fr* d_fin = c.scratch[S_TMP7].as<Fr>(nt);
-  if (n == 0) {
-    for (int k = 0; k < nd; ++k) APG_CUDA(cudaMemcpyAsync(&finals[k], src[k], 32, cudaMemcpyDeviceToHost, c.stream));
-  } else {
+  if (nd > 0) {
     const Fr* base = n >= 2 ? lvl[(n - 1) & 1] : nullptr;
-    launch(c, k_final_bind, (unsigned)((nd + 63) / 64), 64, 0, (const Fr* const*)d_src, base, (size_t)2,
-           n <= 1 ? 1 : 0, nd, to_dev(chal),
-           d_fin);
+    launch(c, k_final_bind, (unsigned)((nd + 63) / 64), 64, 0, (const Fr* const*)d_src, d_bits, base, (size_t)2,
+           n <= 1 ? 1 : 0, nd, to_dev(chal), n == 0 ? 1 : 0, d_fin);
     APG_CUDA(cudaMemcpyAsync(finals.data(), d_fin, 32 * (size_t)nd, cudaMemcpyDeviceToHost, c.stream));
   }
   APG_CUDA(cudaStreamSynchronize(c.stream));

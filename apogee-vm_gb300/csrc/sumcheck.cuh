@@ -20,6 +20,43 @@ struct HostProgram {
   int n_weighted = 0;
 };
 
+// Stored widths of a committed column (PolyBacking, crates/poly/src/lib.rs:44-57):
+// 0 Fr in memory, 1 a bitset (u64 limbs, entry i = bit i % 64 of limb i / 64),
+// 8 / 16 / 32 unsigned integers.
+inline bool narrow_bits_ok(int bits) { return bits == 0 || bits == 1 || bits == 8 || bits == 16 || bits == 32; }
+// Bytes a column of n entries takes at that width.
+inline size_t narrow_bytes(int bits, size_t n) {
+  return bits == 0 ? 32 * n : bits == 1 ? 8 * ((n + 63) / 64) : (size_t)(bits / 8) * n;
+}
+
+// Entry i of a column in its stored width, lifted into Montgomery Fr: the one
+// lift of PolyBacking::entry (crates/poly/src/lib.rs:72-88).
+__device__ __forceinline__ Fr narrow_entry(const void* p, int bits, size_t i) {
+  uint32_t v;
+  switch (bits) {
+    case 0:
+      return ld_fe(reinterpret_cast<const Fr*>(p) + i);
+    case 1:
+      return (reinterpret_cast<const uint64_t*>(p)[i >> 6] >> (i & 63)) & 1 ? fe_one<FrConsts>()
+                                                                             : fe_zero<FrConsts>();
+    case 8:
+      v = reinterpret_cast<const uint8_t*>(p)[i];
+      break;
+    case 16:
+      v = reinterpret_cast<const uint16_t*>(p)[i];
+      break;
+    default:
+      v = reinterpret_cast<const uint32_t*>(p)[i];
+      break;
+  }
+  Fr r = fe_zero<FrConsts>();
+  r.v[0] = v;
+  return fe_to_mont(r);
+}
+
+// The first n entries of a column, lifted into an Fr table.
+void lift_column(Ctx& c, const void* p, int bits, size_t n, Fr* out);
+
 void upload_program(Ctx& c, const HostProgram& hp, DevProgram& P, int slot_cap);
 void build_eq_table(Ctx& c, const std::vector<host::F>& r, Fr* out);
 
@@ -27,22 +64,29 @@ void build_eq_table(Ctx& c, const std::vector<host::F>& r, Fr* out);
 // 2^|eq_point| entries, device memory), drawing challenges from `tr`. Returns
 // the rounds' ascending coefficients, the bound point and each data table's
 // final value.
+// `src_bits` (empty: every table Fr) gives each data table's stored width;
+// narrow tables are read through the lift in the first two rounds and the
+// first bind writes Fr (the lazy lift of crates/poly/src/lib.rs:156-185).
 void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint8_t>& vkinds, int n_cached,
                   const std::vector<const Fr*>& src, const std::vector<host::F>& eq_point, host::Transcript& tr,
                   std::vector<std::array<host::F, 4>>& rounds, std::vector<host::F>& point,
-                  std::vector<host::F>& finals);
+                  std::vector<host::F>& finals, const std::vector<uint8_t>& src_bits = {});
 
+// `bits` (null: all Fr) is each table's stored width.
 int prove_zerocheck_impl(Ctx& c, size_t arity, const uint8_t* coefs, const uint32_t* ta, const uint32_t* tb,
                          size_t nterms, const uint8_t* const* polys, bool polys_on_device, size_t num_vars,
-                         uint8_t* transcript, uint8_t* rounds_out, uint8_t* finals_out);
+                         uint8_t* transcript, uint8_t* rounds_out, uint8_t* finals_out,
+                         const uint8_t* bits = nullptr);
 int witness_digest_impl(Ctx& c, const uint8_t* const* cols, size_t k, size_t num_vars, uint8_t out[32]);
 
 struct Circuit;
 struct GkrValues;
 Circuit parse_circuit_blob(const uint8_t* blob, size_t len);
 size_t gkr_proof_elems(const Circuit& C);
-GkrValues* gkr_forward_impl(Ctx& c, const uint8_t* blob, size_t blob_len, const uint8_t* const* base,
-                            bool base_on_device, const uint32_t* slots, const uint8_t* slot_values, size_t n_slots);
+// `bits` (null: all Fr) is each base column's stored width.
+GkrValues* gkr_forward_impl(Ctx& c, const uint8_t* blob, size_t blob_len, const void* const* base,
+                            const uint8_t* bits, bool base_on_device, const uint32_t* slots,
+                            const uint8_t* slot_values, size_t n_slots);
 int gkr_prove_impl(Ctx& c, const uint8_t* blob, size_t blob_len, GkrValues* V, const uint32_t* slots,
                    const uint8_t* slot_values, size_t n_slots, uint8_t* transcript, uint8_t* proof_out,
                    size_t proof_cap, size_t* proof_len, uint8_t* point_out);

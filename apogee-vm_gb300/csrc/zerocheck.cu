@@ -55,7 +55,7 @@ static bool read_mem_fr(const uint8_t* p, F& out) {
 
 int prove_zerocheck_impl(Ctx& c, size_t arity, const uint8_t* coefs, const uint32_t* ta, const uint32_t* tb,
                          size_t nterms, const uint8_t* const* polys, bool polys_on_device, size_t num_vars,
-                         uint8_t* transcript, uint8_t* rounds_out, uint8_t* finals_out) {
+                         uint8_t* transcript, uint8_t* rounds_out, uint8_t* finals_out, const uint8_t* bits) {
   if (arity == 0) {
     c.last_error = "a gate with no inputs";
     return APG_ERR_INVALID_ARGUMENT;
@@ -77,14 +77,34 @@ int prove_zerocheck_impl(Ctx& c, size_t arity, const uint8_t* coefs, const uint3
     return APG_ERR_INVALID_ARGUMENT;
   }
   const size_t n = (size_t)1 << num_vars;
+  // Stored widths (empty: all Fr). Narrow tables cross and stay narrow; the
+  // first bind lifts them (crates/poly/src/lib.rs:156-185).
+  std::vector<uint8_t> src_bits;
+  if (bits) {
+    for (size_t k = 0; k < arity; ++k)
+      if (!narrow_bits_ok(bits[k])) {
+        c.last_error = "a column width other than 0, 1, 8, 16, 32";
+        return APG_ERR_INVALID_ARGUMENT;
+      }
+    src_bits.assign(bits, bits + arity);
+  }
   std::vector<const Fr*> src(arity);
+  for (size_t k = 0; k < arity; ++k)
+    if (!polys[k]) return APG_ERR_INVALID_ARGUMENT;
   if (polys_on_device) {
     for (size_t k = 0; k < arity; ++k) src[k] = (const Fr*)polys[k];
   } else {
-    Fr* d = c.scratch[S_SCALARS].as<Fr>(arity * n);
+    std::vector<size_t> off(arity);
+    size_t total = 0;
     for (size_t k = 0; k < arity; ++k) {
-      APG_CUDA(cudaMemcpyAsync(d + k * n, polys[k], 32 * n, cudaMemcpyHostToDevice, c.stream));
-      src[k] = d + k * n;
+      off[k] = total;
+      total += (narrow_bytes(bits ? bits[k] : 0, n) + 255) / 256 * 256;
+    }
+    uint8_t* d = c.scratch[S_SCALARS].as<uint8_t>(total);
+    for (size_t k = 0; k < arity; ++k) {
+      APG_CUDA(cudaMemcpyAsync(d + off[k], polys[k], narrow_bytes(bits ? bits[k] : 0, n), cudaMemcpyHostToDevice,
+                               c.stream));
+      src[k] = reinterpret_cast<const Fr*>(d + off[k]);
     }
   }
   std::vector<F> r(num_vars);
@@ -94,7 +114,7 @@ int prove_zerocheck_impl(Ctx& c, size_t arity, const uint8_t* coefs, const uint3
   upload_program(c, hp, P, 0);
   std::vector<std::array<F, 4>> rounds;
   std::vector<F> point, finals;
-  run_sumcheck(c, P, (int)arity, {}, 0, src, r, tr, rounds, point, finals);
+  run_sumcheck(c, P, (int)arity, {}, 0, src, r, tr, rounds, point, finals, src_bits);
   for (auto& f : finals)
     if (!host::below_p(f.w)) throw Error(APG_ERR_INTERNAL, "non-canonical device value");
   tr.absorb(host::T_SUMCHECK_FINAL_EVALS, finals);

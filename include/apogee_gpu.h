@@ -222,6 +222,15 @@ int apg_prove_zerocheck(apg_ctx* ctx, size_t arity, const uint8_t* coefs, const 
 int apg_prove_zerocheck_device(apg_ctx* ctx, size_t arity, const uint8_t* coefs, const uint32_t* a,
                                const uint32_t* b, size_t nterms, const void* const* d_polys, size_t num_vars,
                                uint8_t* transcript, uint8_t* rounds_out, uint8_t* finals_out);
+/* As apg_prove_zerocheck with each column in its stored width (bits[k] as in
+ * apg_gkr_forward_narrow: 1 a bitset in u64 limbs, 8/16/32 unsigned integers,
+ * 0 Fr in memory), host or device (polys_on_device) pointers. Narrow columns
+ * cross and stay narrow: the first two rounds read them through the lift and
+ * the first bind writes Fr (MultilinearPoly::bind, crates/poly/src/lib.rs:156-185). */
+int apg_prove_zerocheck_narrow(apg_ctx* ctx, size_t arity, const uint8_t* coefs, const uint32_t* a,
+                               const uint32_t* b, size_t nterms, const void* const* polys, const uint8_t* bits,
+                               int polys_on_device, size_t num_vars, uint8_t* transcript, uint8_t* rounds_out,
+                               uint8_t* finals_out);
 /* sumcheck::witness_digest (lib.rs:228-256): the Poseidon2 sponge over the
  * column count, the variable count and every cell, squeezed once. Columns
  * are host Fr in memory; out is Fr in memory. Inherently sequential. */
@@ -278,6 +287,20 @@ int apg_gkr_prove(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, apg_
 /* As apg_gkr_forward with the base columns already in device memory. */
 int apg_gkr_forward_device(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, const void* const* d_base,
                            const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, apg_gkr_values** out);
+/* As apg_gkr_forward with every committed column in its stored width, the
+ * PolyBacking variants of crates/poly/src/lib.rs:44-57: bits[x] = 1 (a bitset,
+ * ceil(2^n / 64) u64 limbs, entry i = bit i % 64 of limb i / 64), 8, 16 or 32
+ * (unsigned integers, one per entry) or 0 (Fr in memory). base_on_device: the
+ * columns are device pointers. The columns stay in their widths on the device:
+ * the forward pass and the first two sumcheck rounds of gate list 0 read them
+ * through the lift (PolyBacking::entry, :72-88), and that sumcheck's first
+ * bind writes Fr, so no full-size Fr copy of a narrow column is made (the lazy
+ * lift of MultilinearPoly::bind, :156-185). apg_gkr_prove and
+ * apg_gkr_values_read take the handle as from apg_gkr_forward. A width other
+ * than 0, 1, 8, 16, 32 is APG_ERR_INVALID_ARGUMENT. */
+int apg_gkr_forward_narrow(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, const void* const* base,
+                           const uint8_t* bits, int base_on_device, const uint32_t* slots,
+                           const uint8_t* slot_values, size_t n_slots, apg_gkr_values** out);
 
 /* ---- deferred-pairing accumulator (crates/pcs/src/accumulator.rs) ------- */
 

@@ -136,3 +136,61 @@ def test_reference_family_circuits(ctx, name):
     slots = sorted({c[1] for L in art["layers"] for grp in ("cached", "producing", "enforcing")
                     for e in L[grp] for c in e[-1]["coeffs"] if c[0] == "ch"} | {0})
     run_case(ctx, circuit, sum(name.encode()), slots)
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_narrow_base_matches_oracle(ctx, seed):
+    """A random circuit over a base in every stored width (bitset, u8, u16,
+    u32, Fr): the forward values, the proof and the transcript equal the
+    oracle's over the lifted base; reading the base back lifts it."""
+    import apogee_gpu as A
+    import circuits as C
+
+    rng = random.Random(500 + seed)
+    circ = C.random_circuit(rng, 6 + seed, 5 + seed, 3, rng.sample(range(7), 2), slots=(0, 1, 2))
+    n = 1 << circ.trace_vars
+    widths = [(1, 8, 16, 32, 0)[j % 5] for j in range(circ.n_committed)]
+    base = [[rng.getrandbits(b) for _ in range(n)] if b else [rng.randrange(O.P_R) for _ in range(n)]
+            for b in widths]
+    challenges = {s: rng.randrange(O.P_R) for s in (0, 1, 2)}
+    blob = circ.to_blob()
+    snap = A.transcript_append_scalars(A.transcript_init(), 39, [seed])
+    values = ctx.gkr_forward_narrow(blob, [A.narrow_bytes(c, b) for c, b in zip(base, widths)], widths, challenges)
+    osnap = bytearray(snap)
+    want_proof, want_top = oracle_gkr(blob, base, challenges, osnap, circ)
+    top = circ.depth()
+    for j in range(circ.width(top)):
+        assert values.read(top, j) == want_top[j]
+    proof, after = ctx.gkr_prove(blob, values, challenges, snap)
+    assert proof == want_proof
+    assert after == bytes(osnap)
+    for j in range(circ.n_committed):
+        assert values.read(0, j) == base[j]
+    values.free()
+
+
+def test_narrow_base_family_circuit(ctx):
+    """The reference's add_sub artifact over a base of bitsets and u32 columns
+    (its committed columns are trace values), forward + proof against the
+    oracle."""
+    import apogee_gpu as A
+    import artifact
+
+    art = artifact.decode(O.golden_artifacts()["add_sub.bin"])
+    circ = artifact.to_circuit(art, 6)
+    rng = random.Random(8)
+    n = 1 << circ.trace_vars
+    widths = [1 if j % 3 == 0 else 32 for j in range(circ.n_committed)]
+    base = [[rng.getrandbits(b) for _ in range(n)] for b in widths]
+    slots = sorted({c[1] for L in art["layers"] for grp in ("cached", "producing", "enforcing")
+                    for e in L[grp] for c in e[-1]["coeffs"] if c[0] == "ch"} | {0})
+    challenges = {s: rng.randrange(O.P_R) for s in slots}
+    blob = circ.to_blob()
+    snap = A.transcript_init()
+    values = ctx.gkr_forward_narrow(blob, [A.narrow_bytes(c, b) for c, b in zip(base, widths)], widths, challenges)
+    osnap = bytearray(snap)
+    want_proof, _ = oracle_gkr(blob, base, challenges, osnap, circ)
+    proof, after = ctx.gkr_prove(blob, values, challenges, snap)
+    assert proof == want_proof and after == bytes(osnap)
+    values.free()
+
