@@ -361,14 +361,33 @@ def run_profile_family(args, ctx, torch, dev):
     slots = sorted({c[1] for L in art["layers"] for grp in ("cached", "producing", "enforcing")
                     for e in L[grp] for c in e[-1]["coeffs"] if c[0] == "ch"} | {0})
     ch = {sl: rng.randrange(A.P_R) for sl in slots}
-    cols = shard.device_columns(torch, 1 << args.log2n, circ.n_committed, SEED, dev, ctx)
+    if args.narrow:
+        # Trace-like base columns kept in their widths: every third a bitset,
+        # the rest 32-bit values.
+        import numpy as np
+
+        nrng = np.random.Generator(np.random.PCG64(SEED))
+        n = 1 << args.log2n
+        widths = [1 if j % 3 == 0 else 32 for j in range(circ.n_committed)]
+        cols = []
+        for b in widths:
+            if b == 1:
+                raw = nrng.integers(0, 1 << 63, size=(n + 63) // 64, dtype=np.uint64)
+            else:
+                raw = nrng.integers(0, 1 << 32, size=n, dtype=np.uint64).astype(np.uint32)
+            cols.append(torch.from_numpy(raw.view(np.uint8).copy()).to(dev))
+    else:
+        cols = shard.device_columns(torch, 1 << args.log2n, circ.n_committed, SEED, dev, ctx)
     ptrs = [t.data_ptr() for t in cols]
     phases = {"forward": 0.0, "gkr_prove": 0.0}
 
     def once(acc):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        v = ctx.gkr_forward(blob, ptrs, ch, on_device=True)
+        if args.narrow:
+            v = ctx.gkr_forward_narrow(blob, ptrs, widths, ch, on_device=True)
+        else:
+            v = ctx.gkr_forward(blob, ptrs, ch, on_device=True)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         ctx.gkr_prove(blob, v, ch, A.transcript_init())
@@ -385,7 +404,8 @@ def run_profile_family(args, ctx, torch, dev):
         once(True)
     timers = {name: ctx.timer(i) for i, name in enumerate(["msm_accumulate", "msm_total", "sumcheck_round",
                                                             "gkr_forward", "mercury_pass"])}
-    print(json.dumps({"case": "family", "circuit": args.family, "log2n": args.log2n,
+    print(json.dumps({"case": "family", "circuit": args.family, "log2n": args.log2n, "narrow_base": args.narrow,
+                      "base_bytes": sum(t.numel() * t.element_size() for t in cols),
                       "committed_columns": circ.n_committed, "gate_lists": circ.depth(),
                       "ms_per_phase": {k: v * 1e3 / args.steps for k, v in phases.items()},
                       "timers_ms_launches": timers}), flush=True)
@@ -738,6 +758,8 @@ def main():
                     "accumulator-discharge case for profilers")
     ap.add_argument("--checks", type=int, default=207, help="--profile-case discharge: deferred checks")
     ap.add_argument("--family", default="add_sub", help="--profile-case family: the committed artifact's name")
+    ap.add_argument("--narrow", action="store_true",
+                    help="--profile-case family: base columns in their stored widths (bitsets and 32-bit values)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
