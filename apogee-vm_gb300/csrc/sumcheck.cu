@@ -36,6 +36,7 @@ struct RoundArgs {
   Fr* out;                   // the round's 4 sums, written by the last block
   int xsplit;                // one thread per (pair, node X) instead of per pair
   const uint8_t* src_bits;   // stored width of each src table (null: all Fr)
+  int nodes;                 // bit X set: evaluate the summand at node X (0..2)
 };
 
 __device__ __forceinline__ const Fr* table_in(const RoundArgs& A, int k) {
@@ -128,7 +129,9 @@ __global__ void __launch_bounds__(kRoundThreads) k_round(RoundArgs A, DevProgram
     // what bounds a round with few pairs). Threads 4j..4j+3 of a block share
     // a pair; the X = 0 thread stores the folded level.
     const int x = threadIdx.x & 3;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t / 4 < A.npairs; t += stride) {
+    // The X = 0 thread also stores the folded level, so it always runs.
+    const bool on = x == 0 || ((A.nodes >> x) & 1);
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; on && t / 4 < A.npairs; t += stride) {
       const size_t i = t / 4;
       Fr lo, hi;
       for (int k = 0; k < A.nd; ++k) {
@@ -141,8 +144,7 @@ __global__ void __launch_bounds__(kRoundThreads) k_round(RoundArgs A, DevProgram
       }
       Fr e_lo, e_hi;
       load_line(A, A.nd, i, e_lo, e_hi, x == 0);
-      const Fr e = at_node(e_lo, fe_sub(e_hi, e_lo), x);
-      acc[0] = fe_add(acc[0], fe_mul(e, eval_summand(P, sm)));
+      acc[0] = fe_add(acc[0], fe_mul(fe_add(e_lo, e_hi), eval_summand(P, sm)));
     }
     // Reduce over threads of the same node: strides that are multiples of 4.
     red[threadIdx.x] = acc[0];
@@ -163,17 +165,18 @@ __global__ void __launch_bounds__(kRoundThreads) k_round(RoundArgs A, DevProgram
     }
     Fr e_lo, e_hi;
     load_line(A, A.nd, i, e_lo, e_hi);
-    Fr e_step = fe_sub(e_hi, e_lo);
+    const Fr w = fe_add(e_lo, e_hi);  // the pair's eq weight without the current variable's factor
     for (int v = 0; v < A.nv; ++v) {
       virtual_line_dev(V, A.vkinds[v], i, lo, hi);
       sm_st(sm, A.nd + v, lo);
       sm_st(sm, A.slots_step0 + A.nd + v, hi);
     }
-    for (int x = 0; x < 4; ++x) {
-      Fr s = eval_summand(P, sm);
-      acc[x] = fe_add(acc[x], fe_mul(e_lo, s));
-      if (x < 3) {
-        e_lo = fe_add(e_lo, e_step);
+    for (int x = 0; x < 3; ++x) {
+      if ((A.nodes >> x) & 1) {
+        Fr s = eval_summand(P, sm);
+        acc[x] = fe_add(acc[x], fe_mul(w, s));
+      }
+      if (x < 2) {
         for (int k = 0; k < A.n_val_slots; ++k) sm_st(sm, k, fe_add(sm_ld(sm, k), sm_ld(sm, A.slots_step0 + k)));
       }
     }
@@ -213,8 +216,12 @@ __global__ void __launch_bounds__(kRoundThreads) k_round_warp(RoundArgs A, DevPr
     Fr lo, hi;
     for (int k = lane; k <= A.nd; k += 32) {
       load_line(A, k, i, lo, hi);
-      sm_st(S, k < A.nd ? k : eq_slot, lo);
-      sm_st(S, k < A.nd ? A.slots_step0 + k : eq_slot + 1, fe_sub(hi, lo));
+      if (k < A.nd) {
+        sm_st(S, k, lo);
+        sm_st(S, A.slots_step0 + k, fe_sub(hi, lo));
+      } else {
+        sm_st(S, eq_slot, fe_add(lo, hi));  // the pair's eq weight without the current variable's factor
+      }
     }
     for (int v = lane; v < A.nv; v += 32) {
       virtual_line_dev(V, A.vkinds[v], i, lo, hi);  // hi is the step here
@@ -222,25 +229,25 @@ __global__ void __launch_bounds__(kRoundThreads) k_round_warp(RoundArgs A, DevPr
       sm_st(S, A.slots_step0 + A.nd + v, hi);
     }
     __syncwarp();
-    for (int x = 0; x < 4; ++x) {
-      if (lane == 0)
-        for (int g = 0; g < P.n_cached; ++g) sm_st(S, P.cached_slot0 + g, eval_gate_dev(P, g, S));
-      __syncwarp();
-      Fr part = fe_zero<FrConsts>();
-      for (int j = lane; j < P.n_weighted; j += 32)
-        part = fe_add(part, cmul_coef(P.weights, j, P.weight_ones, eval_gate_dev(P, P.n_cached + j, S)));
-      for (int off = 16; off > 0; off >>= 1) {
-        Fr o;
+    for (int x = 0; x < 3; ++x) {
+      if ((A.nodes >> x) & 1) {  // uniform across the warp
+        if (lane == 0)
+          for (int g = 0; g < P.n_cached; ++g) sm_st(S, P.cached_slot0 + g, eval_gate_dev(P, g, S));
+        __syncwarp();
+        Fr part = fe_zero<FrConsts>();
+        for (int j = lane; j < P.n_weighted; j += 32)
+          part = fe_add(part, cmul_coef(P.weights, j, P.weight_ones, eval_gate_dev(P, P.n_cached + j, S)));
+        for (int off = 16; off > 0; off >>= 1) {
+          Fr o;
 #pragma unroll
-        for (int w = 0; w < 8; ++w) o.v[w] = __shfl_xor_sync(0xffffffffu, part.v[w], off);
-        part = fe_add(part, o);
+          for (int w = 0; w < 8; ++w) o.v[w] = __shfl_xor_sync(0xffffffffu, part.v[w], off);
+          part = fe_add(part, o);
+        }
+        if (lane == 0) acc[x] = fe_add(acc[x], fe_mul(sm_ld(S, eq_slot), part));
       }
-      if (lane == 0) acc[x] = fe_add(acc[x], fe_mul(sm_ld(S, eq_slot), part));
       __syncwarp();
-      if (x < 3) {
+      if (x < 2)
         for (int k = lane; k < A.n_val_slots; k += 32) sm_st(S, k, fe_add(sm_ld(S, k), sm_ld(S, A.slots_step0 + k)));
-        if (lane == 0) sm_st(S, eq_slot, fe_add(sm_ld(S, eq_slot), sm_ld(S, eq_slot + 1)));
-      }
       __syncwarp();
     }
   }
@@ -431,6 +438,19 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
   DevProgram P = prog;
   P.cached_slot0 = n_val;
 
+  // 1/r_j for every nonzero eq coordinate, from one inversion (Montgomery's
+  // batch trick): the rounds divide by their coordinate.
+  std::vector<F> inv_r(n, host::fzero());
+  {
+    std::vector<F> pre(n + 1, host::fone());
+    for (int j = 0; j < n; ++j) pre[j + 1] = eq_point[j].zero() ? pre[j] : host::fmul(pre[j], eq_point[j]);
+    F inv = host::finv(pre[n]);
+    for (int j = n; j-- > 0;) {
+      if (eq_point[j].zero()) continue;
+      inv_r[j] = host::fmul(inv, pre[j]);
+      inv = host::fmul(inv, eq_point[j]);
+    }
+  }
   F chal = host::fzero();
   for (int r = 0; r < n; ++r) {
     RoundArgs A;
@@ -455,6 +475,16 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
     // on four threads.
     A.xsplit = A.npairs * 4 <= (size_t)threads * max_blocks ? 1 : 0;
     A.src_bits = d_bits;
+    // The round polynomial factors as s(X) = eq_r(X) q(X): eq's factor for
+    // this variable, eq_r(X) = (1 - r_r)(1 - X) + r_r X, is common to every
+    // pair, and the rest of a pair's eq weight is e(2i) + e(2i + 1). The
+    // device sums q at nodes 0 and 2 (q has degree 2); from the second round
+    // on q(1) follows from s(0) + s(1) = s_{r-1}(c_{r-1}), which holds for any
+    // tables because the bound tables are the lines at c. Round 0, and a round
+    // whose eq coordinate is 0, evaluate node 1 as well.
+    const F rr = eq_point[r];
+    const bool need1 = r == 0 || rr.zero();
+    A.nodes = need1 ? 7 : 5;
     const size_t work = A.xsplit ? A.npairs * 4 : A.npairs;
     const int blocks = warp_mode
                            ? (int)std::min<size_t>((A.npairs + kRoundThreads / 32 - 1) / (kRoundThreads / 32),
@@ -466,7 +496,25 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
     c.timer_end(APG_TIMER_SUMCHECK_ROUND, t0);
     APG_CUDA(cudaMemcpyAsync(sums, d_out, 128, cudaMemcpyDeviceToHost, c.stream));
     APG_CUDA(cudaStreamSynchronize(c.stream));
-    auto g = host::cubic_through(sums);
+    F q[4] = {sums[0], sums[1], sums[2], host::fzero()};
+    const F one_m_r = host::fsub(host::fone(), rr);
+    if (!need1) {
+      const auto& gp = rounds.back();  // s_{r-1}(X), ascending coefficients
+      const F claim = host::fadd(
+          gp[0], host::fmul(chal, host::fadd(gp[1], host::fmul(chal, host::fadd(gp[2], host::fmul(chal, gp[3]))))));
+      q[1] = host::fmul(host::fsub(claim, host::fmul(one_m_r, q[0])), inv_r[r]);
+    }
+    // q(3) = q(0) - 3 q(1) + 3 q(2); s(X) = eq_r(X) q(X) with eq_r(X) = 1 - r - X + 2 r X.
+    const F three = host::from_u64(3);
+    q[3] = host::fadd(q[0], host::fmul(three, host::fsub(q[2], q[1])));
+    F sv[4];
+    F eqx = one_m_r;                          // eq_r(0)
+    const F step = host::fsub(host::fadd(rr, rr), host::fone());  // eq_r(X + 1) - eq_r(X) = 2r - 1
+    for (int x = 0; x < 4; ++x) {
+      sv[x] = host::fmul(eqx, q[x]);
+      eqx = host::fadd(eqx, step);
+    }
+    auto g = host::cubic_through(sv);
     tr.absorb(host::T_SUMCHECK_ROUND, g.data(), 4);
     chal = tr.challenge(host::T_SUMCHECK_CHALLENGE);
     rounds.push_back(g);
