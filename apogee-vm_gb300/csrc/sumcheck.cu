@@ -176,7 +176,13 @@ __global__ void __launch_bounds__(kRoundThreads) k_round(RoundArgs A, DevProgram
         Fr s = eval_summand(P, sm);
         acc[x] = fe_add(acc[x], fe_mul(w, s));
       }
-      if (x < 2) {
+      if (x == 0 && !((A.nodes >> 1) & 1)) {  // straight to node 2: lo + 2 step
+        for (int k = 0; k < A.n_val_slots; ++k) {
+          const Fr st = sm_ld(sm, A.slots_step0 + k);
+          sm_st(sm, k, fe_add(sm_ld(sm, k), fe_add(st, st)));
+        }
+        ++x;
+      } else if (x < 2) {
         for (int k = 0; k < A.n_val_slots; ++k) sm_st(sm, k, fe_add(sm_ld(sm, k), sm_ld(sm, A.slots_step0 + k)));
       }
     }
@@ -246,8 +252,15 @@ __global__ void __launch_bounds__(kRoundThreads) k_round_warp(RoundArgs A, DevPr
         if (lane == 0) acc[x] = fe_add(acc[x], fe_mul(sm_ld(S, eq_slot), part));
       }
       __syncwarp();
-      if (x < 2)
+      if (x == 0 && !((A.nodes >> 1) & 1)) {  // straight to node 2: lo + 2 step
+        for (int k = lane; k < A.n_val_slots; k += 32) {
+          const Fr st = sm_ld(S, A.slots_step0 + k);
+          sm_st(S, k, fe_add(sm_ld(S, k), fe_add(st, st)));
+        }
+        ++x;
+      } else if (x < 2) {
         for (int k = lane; k < A.n_val_slots; k += 32) sm_st(S, k, fe_add(sm_ld(S, k), sm_ld(S, A.slots_step0 + k)));
+      }
       __syncwarp();
     }
   }
