@@ -376,3 +376,28 @@ def test_msm_large_one_point_all_doublings(ctx):
     s = random.Random(5).randrange(O.P_R)
     got = ctx.msm(O.G1_GEN * n, A.to_mont_bytes([s] * n))
     assert got == O.g1_mul(O.G1_GEN, s * n % O.P_R)
+
+
+def test_pair_round_fallback_agrees(ctx):
+    """16 uniform 2^22 columns commit as four groups of four: about 4 x 15 x 2^22
+    references, whose first affine pair round would exceed its scratch cap, so
+    the groups take the XYZZ path from the references (the device flag). Each
+    column committed alone runs the pair rounds. Both give the same points."""
+    import torch
+
+    nv = 22
+    n = 1 << nv
+    ctx.srs_generate(0x1234567, n)
+    ctx.srs_prepare()
+    g = torch.Generator(device="cuda").manual_seed(5)
+    cols = []
+    for _ in range(16):
+        t = torch.randint(0, 1 << 31, (n, 8), dtype=torch.int64, device="cuda", generator=g)
+        t[:, 7] &= 0x0FFFFFFF  # below 2^252 < r
+        t = t.to(torch.int32).contiguous()
+        ctx.fr_to_mont_device(t.data_ptr(), n)
+        cols.append(t)
+    ptrs = [t.data_ptr() for t in cols]
+    batch = ctx.commit_batch_device(ptrs, nv)
+    alone = [ctx.commit_device(p, nv) for p in ptrs]
+    assert batch == alone
