@@ -39,6 +39,24 @@ TAU_SEED = 0x7A75_5EED
 TUNE_WIDTHS = (8, 12, 16, 18, 20)  # window widths the autotuner tries per size class
 
 
+def max_over_ranks(x: float, dist, device: str) -> float:
+    """The largest of every rank's x (a step time): the job is as slow as its
+    slowest rank. `dist` is torch.distributed with a process group, or None."""
+    if not dist:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def weak_value(world: int, points_per_rank: int, seconds: float) -> float:
+    """Whole-job points/s when every rank commits its own columns (weak
+    scaling): all ranks' points over the slowest rank's time."""
+    return world * points_per_rank / seconds
+
+
 def env_int(name, default):
     try:
         return int(os.environ.get(name, default))
@@ -639,12 +657,8 @@ def run_gpu(args):
     torch.cuda.synchronize()
     barrier()
     launches = ctx.launch_count() - launches0
-    ms_step = ev0.elapsed_time(ev1) / args.steps
-    if dist:
-        t = torch.tensor([ms_step], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = world * k * n / (ms_step / 1e3)
+    ms_step = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, dist, f"cuda:{local}")
+    value = weak_value(world, k * n, ms_step / 1e3)
 
     # End to end through the public API with host buffers.
     for _ in range(1):
@@ -658,12 +672,9 @@ def run_gpu(args):
     torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / e2e_steps
     barrier()
-    if dist:
-        t = torch.tensor([t_e2e], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks(t_e2e, dist, f"cuda:{local}")
     assert cms_h == cms, "device-resident and host-buffer commits disagree"
-    e2e = {"value": world * k * n / t_e2e, "unit": UNIT, "h2d_bytes_per_step": k * n * 32,
+    e2e = {"value": weak_value(world, k * n, t_e2e), "unit": UNIT, "h2d_bytes_per_step": k * n * 32,
            "d2h_bytes_per_step": k * 64}
 
     # Roofline: the accumulation kernel on uniform 254-bit scalars.
