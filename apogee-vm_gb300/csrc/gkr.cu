@@ -219,6 +219,22 @@ namespace {
 
 constexpr int kFwdThreads = 64;
 
+// Row-wise lists over a contiguous Fr layer: the columns are read in place
+// (consecutive threads take consecutive rows, so each operand load is one
+// coalesced row of a column) and only the virtual and cached entries take
+// shared memory.
+__global__ void __launch_bounds__(kFwdThreads) k_forward_g(DevProgram P, int w, int nv, VirtualKinds vk,
+                                                           const Fr* layer, size_t col_stride, size_t rows, int width,
+                                                           Fr* out) {
+  extern __shared__ uint32_t sm_raw[];
+  const size_t y = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (y >= rows) return;
+  const GSlots S{layer + y, col_stride, w, thread_slots(sm_raw)};
+  for (int v = 0; v < nv; ++v) sm_st(S, w + v, virtual_at_row_dev(vk.k[v], y));
+  for (int g = 0; g < P.n_cached; ++g) sm_st(S, P.cached_slot0 + g, eval_gate_dev(P, g, S));
+  for (int j = 0; j < width; ++j) st_fe(&out[(size_t)j * rows + y], eval_gate_dev(P, P.n_cached + j, S));
+}
+
 // `bits` (null: all Fr) is the stored width of each column of the base.
 __global__ void __launch_bounds__(kFwdThreads) k_forward(DevProgram P, int w, int nv, VirtualKinds vk,
                                                          const Fr* const* cols, const uint8_t* bits, size_t rows,
@@ -336,17 +352,28 @@ GkrValues* gkr_forward_impl(Ctx& c, const uint8_t* blob, size_t blob_len, const 
       cols[x] = k == 0 ? reinterpret_cast<const Fr*>(V->base_raw(x)) : V->col(k, x);
     const Fr** d_cols = c.scratch[S_TMP5].as<const Fr*>(w);
     APG_CUDA(cudaMemcpyAsync(d_cols, cols.data(), sizeof(Fr*) * w, cudaMemcpyHostToDevice, c.stream));
-    const size_t slots_n = (size_t)P.cached_slot0 + L.cached.size();
+    // A row-wise list over an Fr layer reads the layer in place; a halving
+    // list (two rows of a column a slot pair) or a narrow base is staged.
+    const bool in_place = !L.halving && (k > 0 || !V->base_narrow) && w > 0;
+    const size_t slots_n = (size_t)P.cached_slot0 + L.cached.size() - (in_place ? (size_t)w : 0);
     int threads = kFwdThreads;
     while (threads > 8 && std::max<size_t>(slots_n, 1) * 32 * threads > 200 * 1024) threads /= 2;
     const size_t smem = std::max<size_t>(slots_n, 1) * 32 * threads;
     if (smem > 200 * 1024) throw Error(APG_ERR_BAD_CIRCUIT, "gate list too wide for one thread block");
-    APG_CUDA(cudaFuncSetAttribute(k_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     cudaEvent_t t0 = c.timer_begin();
-    if (L.width)
+    if (L.width && in_place) {
+      APG_CUDA(cudaFuncSetAttribute(k_forward_g, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      // Columns of the layer lie a fixed stride apart (the base's at its
+      // 256-byte-aligned offsets, later layers back to back).
+      const size_t stride = w > 1 ? (size_t)(cols[1] - cols[0]) : 0;
+      launch(c, k_forward_g, (unsigned)((rows + threads - 1) / threads), threads, smem, P, w, nv, vk, cols[0],
+             stride, rows, (int)L.width, V->layers[k + 1]);
+    } else if (L.width) {
+      APG_CUDA(cudaFuncSetAttribute(k_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
       launch(c, k_forward, (unsigned)((rows + threads - 1) / threads), threads, smem, P, w, nv, vk,
              (const Fr* const*)d_cols, k == 0 ? d_bits : (const uint8_t*)nullptr, rows, L.halving ? 1 : 0,
              (int)L.width, V->layers[k + 1]);
+    }
     c.timer_end(APG_TIMER_GKR_FORWARD, t0);
     // The program and column list buffers are reused by the next layer.
     APG_CUDA(cudaStreamSynchronize(c.stream));

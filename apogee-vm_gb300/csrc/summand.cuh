@@ -83,6 +83,25 @@ __device__ __forceinline__ void sm_st(const Slots& S, int slot, const Fr& a) {
   for (int w = 0; w < 8; ++w) S.base[slot * S.slot_stride + w * S.word_stride] = a.v[w];
 }
 
+// Operand slots split in two: slots below `ncols` are the columns of a
+// contiguous Fr layer read in place (column x of this row at cols + x *
+// stride), the rest per-thread shared memory. The forward pass of a row-wise
+// list reads its operands this way, so a block needs no per-thread copy of
+// the row and keeps a full complement of threads.
+struct GSlots {
+  const Fr* cols;
+  size_t stride;
+  int ncols;
+  Slots rest;
+};
+
+__device__ __forceinline__ Fr sm_ld(const GSlots& S, int slot) {
+  return slot < S.ncols ? ld_fe(S.cols + (size_t)slot * S.stride) : sm_ld(S.rest, slot - S.ncols);
+}
+
+// Only the shared-memory slots (virtual tables, cached entries) are written.
+__device__ __forceinline__ void sm_st(const GSlots& S, int slot, const Fr& a) { sm_st(S.rest, slot - S.ncols, a); }
+
 __device__ __forceinline__ Fr ld_g(const Fr* p) { return ld_fe(p); }
 
 // The interpreter calls one out-of-line Fr product: its gate kinds would
@@ -108,14 +127,16 @@ __device__ __forceinline__ Fr gmul_coef(const DevGate& G, const Fr* c, int i, co
 
 // Affine form sum_{i<t} c[i] * x_i + c[t], operands ops[0..t); `ones` is
 // the one-mask of c[0..].
-__device__ __forceinline__ Fr affine_form(const Slots& sm, const DevGate& G, const uint16_t* ops, const Fr* c,
-                                          int c0, int t) {
+template <class S>
+__device__ __forceinline__ Fr affine_form(const S& sm, const DevGate& G, const uint16_t* ops, const Fr* c, int c0,
+                                          int t) {
   Fr acc = ld_g(&c[c0 + t]);
   for (int i = 0; i < t; ++i) acc = fe_add(acc, gmul_coef(G, c, c0 + i, sm_ld(sm, ops[i])));
   return acc;
 }
 
-static __device__ __noinline__ Fr eval_gate_dev(const DevProgram& P, int g, const Slots sm) {
+template <class S>
+static __device__ __noinline__ Fr eval_gate_dev(const DevProgram& P, int g, const S sm) {
   const DevGate G = P.gates[g];
   const uint16_t* ops = P.ops + G.op_off;
   const Fr* c = P.coeffs + G.cf_off;
