@@ -208,6 +208,7 @@ static HostProgram layer_program(const Circuit& c, size_t k, const Challenges& c
   hp.n_weighted = (int)(L.producing.size() + (with_enforcing ? L.enforcing.size() : 0));
   hp.weights = weights;
   if (hp.weights.size() < (size_t)hp.n_weighted) hp.weights.resize(hp.n_weighted, host::fone());
+  hp.summed = with_enforcing;  // the prover sums the list; the forward pass writes it out gate by gate
   const size_t slots = (L.halving ? 2 * w : w + nv) + L.cached.size();
   if (slots > 60000) throw Error(APG_ERR_BAD_CIRCUIT, "gate list too wide");
   return hp;

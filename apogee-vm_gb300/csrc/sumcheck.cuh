@@ -18,6 +18,10 @@ struct HostProgram {
   std::vector<host::F> weights;
   int n_cached = 0;
   int n_weighted = 0;
+  // The weighted gates are only summed (a sumcheck's summand), never read one
+  // by one (the forward pass writes gate j to column j): they may be
+  // reordered.
+  bool summed = false;
 };
 
 // Stored widths of a committed column (PolyBacking, crates/poly/src/lib.rs:44-57):

@@ -28,9 +28,12 @@ struct VirtualKinds {
   uint8_t k[8];
 };
 
+// DevGate::flags bit: the gate's weight is 1, so its value is summed as it is.
+constexpr uint8_t kGateUnitWeight = 1;
+
 struct DevGate {
   uint8_t kind;
-  uint8_t pad;
+  uint8_t flags;
   uint16_t nops;
   uint16_t p1, p2;   // shape: Linear t; Affine t, u; Quadratic t, u
   uint32_t op_off;   // first operand slot index in ops[]
@@ -50,7 +53,6 @@ struct DevProgram {
   int n_cached;
   int n_weighted;
   int cached_slot0;     // slot of cached entry 0
-  uint32_t weight_ones; // bit j: weight j is 1 (lambda^0 always is)
 };
 
 // One evaluation's slots: word w of slot s at base[(s * 8 + w) * stride].
@@ -175,13 +177,19 @@ static __device__ __noinline__ Fr eval_gate_dev(const DevProgram& P, int g, cons
   return fe_zero<FrConsts>();
 }
 
+// Weighted gate j's contribution: its value times its weight, unless the
+// weight is 1.
+__device__ __forceinline__ Fr weigh(const DevProgram& P, int j, const Fr& v) {
+  return (P.gates[P.n_cached + j].flags & kGateUnitWeight) ? v : rmul(ld_g(&P.weights[j]), v);
+}
+
 // Cached entries into their slots, then the weighted sum of the gates.
 __device__ __forceinline__ Fr eval_summand(const DevProgram& P, const Slots& sm) {
   for (int g = 0; g < P.n_cached; ++g) sm_st(sm, P.cached_slot0 + g, eval_gate_dev(P, g, sm));
   Fr acc = fe_zero<FrConsts>();
   for (int j = 0; j < P.n_weighted; ++j) {
     Fr v = eval_gate_dev(P, P.n_cached + j, sm);
-    acc = fe_add(acc, cmul_coef(P.weights, j, P.weight_ones, v));
+    acc = fe_add(acc, weigh(P, j, v));
   }
   return acc;
 }
