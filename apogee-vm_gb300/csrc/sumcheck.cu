@@ -209,7 +209,12 @@ __global__ void __launch_bounds__(kRoundThreads) k_round(RoundArgs A, DevProgram
 // tables sit once in the warp's shared slots (values, then cached entries,
 // then steps, then eq's value and step), written lane-parallel; at each node
 // the lanes split the gates and the warp adds their weighted values.
-__global__ void __launch_bounds__(kRoundThreads) k_round_warp(RoundArgs A, DevProgram P, VirtualRound V,
+// Five resident blocks a SM (96 registers, no spills) measured about 1 %
+// faster than the unconstrained allocation (128 registers, four blocks).
+#ifndef APG_ROUND_WARP_MIN_BLOCKS
+#define APG_ROUND_WARP_MIN_BLOCKS 5
+#endif
+__global__ void __launch_bounds__(kRoundThreads, APG_ROUND_WARP_MIN_BLOCKS) k_round_warp(RoundArgs A, DevProgram P, VirtualRound V,
                                                               Fr* partials) {
   extern __shared__ uint32_t sm_raw[];
   __shared__ Fr red[kRoundThreads];
