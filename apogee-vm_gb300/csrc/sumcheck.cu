@@ -1,14 +1,18 @@
 // The sumcheck prover on the device: one fused kernel per round folds every
-// table with the previous round's challenge and evaluates the round's cubic
-// at X = 0..3, reduced over the hypercube; the host draws the next challenge.
+// table with the previous round's challenge and sums the summand over the
+// hypercube at the nodes the round needs; the host rebuilds the round's cubic
+// and draws the next challenge.
 //
 // Restates crates/sumcheck/src/lib.rs (prove_zerocheck :359-408,
 // round_evaluations :324-349) and crates/gkr/src/lib.rs (prove_sumcheck
 // :792-899): per pair (2i, 2i+1) of every table the line lo + X*(hi - lo),
-// the summand at the four nodes weighted by eq, SUMCHECK_ROUND then
+// the summand at X = 0..3 weighted by eq, SUMCHECK_ROUND then
 // SUMCHECK_CHALLENGE, and the bind f'(i) = f(2i) + r*(f(2i+1) - f(2i))
-// (crates/poly/src/lib.rs:156-185). Round r's kernel reads the level-(r-1)
-// tables once, writes the level-r tables once and never re-reads them.
+// (crates/poly/src/lib.rs:156-185). The cubic factors as eq_r(X) q(X) with q
+// quadratic, so the device sums q at X = 0 and 2 (and 1 in the first round)
+// and the host derives the rest (run_sumcheck). Round r's kernel reads the
+// level-(r-1) tables once, writes the level-r tables once and never re-reads
+// them.
 #include <algorithm>
 #include <tuple>
 
@@ -77,7 +81,7 @@ __device__ __forceinline__ void load_line(const RoundArgs& A, int k, size_t i, F
   st_fe(&o[2 * i + 1], hi);
 }
 
-// lo + x * (hi - lo) for a node x in 0..3.
+// lo + x * (hi - lo) for a node x in 0..2.
 __device__ __forceinline__ Fr at_node(const Fr& lo, const Fr& step, int x) {
   Fr v = lo;
   for (int j = 0; j < x; ++j) v = fe_add(v, step);
@@ -127,10 +131,11 @@ __global__ void __launch_bounds__(kRoundThreads) k_round(RoundArgs A, DevProgram
   for (int x = 0; x < 4; ++x) acc[x] = fe_zero<FrConsts>();
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   if (A.xsplit) {
-    // Small rounds: thread t evaluates pair t / 4 at node X = t % 4 alone, so
-    // the four evaluations of a pair run side by side (latency, not work, is
-    // what bounds a round with few pairs). Threads 4j..4j+3 of a block share
-    // a pair; the X = 0 thread stores the folded level.
+    // Small rounds: thread t evaluates pair t / 4 at node X = t % 4 alone
+    // (X = 3 and, after the first round, X = 1 stay idle), so the evaluations
+    // of a pair run side by side (latency, not work, is what bounds a round
+    // with few pairs). Threads 4j..4j+3 of a block share a pair; the X = 0
+    // thread stores the folded level.
     const int x = threadIdx.x & 3;
     // The X = 0 thread also stores the folded level, so it always runs.
     const bool on = x == 0 || ((A.nodes >> x) & 1);
@@ -492,8 +497,8 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
     A.done = done;
     A.out = d_out;
     VirtualRound V = virtual_round(point, n);
-    // Rounds too small to fill the device evaluate the four nodes of a pair
-    // on four threads.
+    // Rounds too small to fill the device evaluate the nodes of a pair on
+    // threads of their own.
     A.xsplit = A.npairs * 4 <= (size_t)threads * max_blocks ? 1 : 0;
     A.src_bits = d_bits;
     // The round polynomial factors as s(X) = eq_r(X) q(X): eq's factor for
