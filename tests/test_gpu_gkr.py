@@ -194,3 +194,40 @@ def test_narrow_base_family_circuit(ctx):
     assert proof == want_proof and after == bytes(osnap)
     values.free()
 
+
+
+def test_linearized_wide_lists_match_oracle(ctx):
+    """Wide summed lists are re-linearised into one merged quadratic form:
+    a row-wise list of every gate shape over shared operands (products,
+    masks, affine products, linear forms with a challenge, quadratics) and a
+    halving list whose tree gates repeat products; the proof equals the
+    oracle's, gate by gate."""
+    import circuits as C
+
+    rng = random.Random(77)
+
+    def r():
+        return rng.randrange(O.P_R)
+
+    circ = C.Circuit(8, 5, [C.V_ROW])
+    prod = []
+    for j in range(24):
+        a, b = C.col(j % 5), C.col((3 * j + 1) % 5)
+        kind = j % 6
+        if kind == 0:
+            prod.append(C.product(r(), a, b))
+        elif kind == 1:
+            prod.append(C.mask(a, b))
+        elif kind == 2:
+            prod.append(C.affine([(r(), a), (1, C.virt(0))], r(), [(r(), b), (O.P_R - 1, a)], r()))
+        elif kind == 3:
+            prod.append(C.linear([(r(), a), (1, b), (("ch", 1), C.virt(0))], r()))
+        elif kind == 4:
+            prod.append(C.quadratic(r(), [(r(), a)], [(1, a, b), (r(), b, b)]))
+        else:
+            prod.append(C.product(1, b, a))
+    enf = [C.quadratic(0, [(1, C.col(0))], [(O.P_R - 1, C.col(0), C.col(0))]) for _ in range(3)]
+    circ.add_layer(prod, enforcing=enf)
+    circ.add_layer([C.tree_product(C.col(j % 8)) for j in range(20)]
+                   + [C.tree_cross(C.col(0), C.col(1)), C.tree_cross(C.col(1), C.col(0))], halving=True)
+    run_case(ctx, circ, 77, slots=(0, 1, 2))
