@@ -151,6 +151,19 @@ class ClockSampler:
 # (7.259 GB for 15 x 2^20 references) scaled x4 to 15 x 2^22.
 ACC_TRAFFIC_BYTES = {22: 2.9035e10}
 
+# Copy bandwidth of the GB300s when no measured figure sits beside
+# this file (one earlier STREAM-style copy on a GB300).
+HBM_FALLBACK_GBS = 6800.0
+
+
+def hbm_peak_gbs():
+    """The measured HBM copy bandwidth written beside this file, else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError, TypeError):
+        return HBM_FALLBACK_GBS, "fallback"
+
 
 def cpu_msm_points_per_s(bases: bytes, scalars: bytes, n: int, threads: int, reps: int = 3):
     """Best-of-reps oracle MSM time on n points (the reference's best-of-3)."""
@@ -693,11 +706,17 @@ def run_gpu(args):
     algo = algorithmic_fqmul_accumulate(n)
     achieved = algo / (acc_ms / acc_n / 1e3)
     traffic = ACC_TRAFFIC_BYTES.get(log2n)
+    hbm_peak, hbm_src = hbm_peak_gbs()
+    hbm = None
+    if traffic:
+        hbm_gbs = traffic / (acc_ms / acc_n / 1e3) / 1e9
+        hbm = {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
+               "peak_source": f"{hbm_src} copy bandwidth", "basis": "the captured DRAM traffic over the phase's time"}
     roofline = {
         "bound": "int",
         "kernel": f"bucket accumulation (k_pair_round x3 + k_bucket_acc), 2^{log2n} uniform scalars",
         "achieved": achieved / 1e9, "peak": fq_rate / 1e9, "unit": "G Fq-mul/s", "frac": achieved / fq_rate,
-        "traffic": traffic,
+        "traffic": traffic, "hbm": hbm,
         "peak_source": "measured on this device in this run: dependency-free Fq Montgomery products on every SM",
         "kernel_ms": acc_ms / acc_n, "msm_ms": tot_ms / tot_n,
         "msm_uniform_points_per_s": n / (tot_ms / tot_n / 1e3), "algorithmic_fqmul_per_launch": algo,

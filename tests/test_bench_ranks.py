@@ -62,3 +62,16 @@ def test_reference_arm_prints_once_under_torchrun():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+
+
+def test_hbm_peak_is_the_measured_copy_rate():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    peak, src = bench.hbm_peak_gbs()
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            assert (peak, src) == (float(json.load(f)["hbm_gbs"]), "measured")
+    else:
+        assert (peak, src) == (bench.HBM_FALLBACK_GBS, "fallback")
