@@ -783,13 +783,20 @@ __device__ __forceinline__ Fq shfl_fq(const Fq& a, int lane) {
   return r;
 }
 
-// Each lane's 1/v (v != 0) from one inversion a warp: inclusive prefix and
-// suffix products across the lanes, the inverse of the warp's total product,
-// then 1/v_i = total^-1 * (product of the lanes before i) * (after i). Every
-// lane inverts the same total, so the inversion runs without divergence.
-// All 32 lanes must call it.
-__device__ __forceinline__ Fq warp_inverse(const Fq& v) {
-  const int lane = threadIdx.x & 31;
+// Each thread's 1/v (v != 0) from one inversion a block of kPairThreads:
+// per warp the inclusive prefix and suffix products across the lanes give
+// the warp's total and each lane's product of the others; warp 0 inverts the
+// product of the warps' totals (the binary Euclid costs as many instructions
+// as a lane's work in a late pair round, so one a block instead of one a warp
+// is a quarter of that) and hands each warp the inverse of its total; then
+// 1/v_i = (1/total_w) * (lanes before i) * (lanes after i). All threads of the
+// block must call it.
+constexpr int kPairThreads = 128;
+constexpr int kPairWarps = kPairThreads / 32;
+
+__device__ __forceinline__ Fq block_inverse(const Fq& v) {
+  __shared__ Fq tot[kPairWarps], tinv[kPairWarps];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   Fq pre = v, suf = v;
 #pragma unroll 1
   for (int off = 1; off < 32; off <<= 1) {
@@ -798,12 +805,24 @@ __device__ __forceinline__ Fq warp_inverse(const Fq& v) {
     if (lane >= off) pre = q.a;
     if (lane + off < 32) suf = q.b;
   }
-  const Fq total = shfl_fq(pre, 31);
+  if (lane == 31) tot[w] = pre;
   Fq ex = shfl_up_fq(pre, 1), sx = shfl_down_fq(suf, 1);
   if (lane == 0) ex = fe_one<FqConsts>();
   if (lane == 31) sx = fe_one<FqConsts>();
   const Fq others = cmul(ex, sx);
-  return cmul(fe_inverse(total), others);
+  __syncthreads();
+  if (w == 0) {
+    Fq all = tot[0];
+#pragma unroll 1
+    for (int i = 1; i < kPairWarps; ++i) all = cmul(all, tot[i]);
+    Fq o = fe_inverse(all);  // every lane of warp 0 inverts the same value
+#pragma unroll 1
+    for (int i = 0; i < kPairWarps; ++i)
+      if (i != lane) o = cmul(o, tot[i]);
+    if (lane < kPairWarps) tinv[lane] = o;
+  }
+  __syncthreads();
+  return cmul(tinv[w], others);
 }
 
 // The first bucket whose output reaches past slot o (o below the total).
@@ -935,10 +954,11 @@ __device__ __forceinline__ void pair_store(const uint32_t* refs, const Affine* s
 // base + 32 j + l, so the lanes' references, explicit input points, running
 // products and outputs are read and written in coalesced rows. Forward a lane
 // multiplies up its slope denominators (the running products in pp[k * T + s]),
-// the warp shares one inversion, and backward each slot takes its inverse at
-// two products and writes its sum.
+// the block shares one inversion, and backward each slot takes its inverse at
+// two products and writes its sum. The early returns are uniform across the
+// grid, so every thread of a block reaches the block's inversion.
 template <bool REFS>
-__global__ void __launch_bounds__(128, APG_PAIR_MIN_BLOCKS)
+__global__ void __launch_bounds__(kPairThreads, APG_PAIR_MIN_BLOCKS)
     k_pair_round(const uint32_t* refs, const Affine* src, const uint32_t* ends_in, const uint32_t* start_out,
                  uint32_t nbins, size_t cap, uint32_t* mode, size_t T, Fq* pp, Affine* out) {
   const size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -964,7 +984,7 @@ __global__ void __launch_bounds__(128, APG_PAIR_MIN_BLOCKS)
     st_fe(&pp[k++ * T + s], acc);
     acc = fe_mul(acc, d);
   }
-  Fq inv = warp_inverse(acc);  // every lane of the warp reaches this
+  Fq inv = block_inverse(acc);  // every thread of the block reaches this
   for (size_t j = steps; j-- > 0;) {
     const size_t o = o0 + 32 * j;
     b = pair_seek_down(start_out, b, o);
@@ -1243,11 +1263,11 @@ size_t pair_resident_threads(Ctx& c) {
   static int per_sm = 0;
   std::call_once(once, [] {
     int a = 0, b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_pair_round<true>, 128, 0) != cudaSuccess) a = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_round<false>, 128, 0) != cudaSuccess) b = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_pair_round<true>, kPairThreads, 0) != cudaSuccess) a = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_round<false>, kPairThreads, 0) != cudaSuccess) b = 1;
     per_sm = std::max(1, std::min(a, b));
   });
-  return (size_t)c.sm_count * (size_t)per_sm * 128;
+  return (size_t)c.sm_count * (size_t)per_sm * kPairThreads;
 }
 
 constexpr size_t kMaxBins = (size_t)(kScanBlock - 1) * kScanBlock * kScanItems;  // one pass of the 3-kernel scan
@@ -1332,7 +1352,7 @@ void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols
     const size_t scan_n = nbins + 1;
     const unsigned sblocks = (unsigned)((scan_n + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems));
     const uint32_t* ends_in = counts;
-    const unsigned pblocks = (unsigned)((T + 127) / 128);
+    const unsigned pblocks = (unsigned)((T + kPairThreads - 1) / kPairThreads);
     for (int r = 0; r < kPairRounds; ++r) {
       uint32_t* st = cnt + (size_t)r * scan_n;
       launch(c, k_halve_counts, blocks_for<int>(scan_n, 256), 256, 0, ends_in, (uint32_t)nbins, st);
@@ -1340,11 +1360,12 @@ void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols
       launch(c, k_scan_blocks, 1, kScanBlock, 0, blk, (int)sblocks);
       launch(c, k_scan_add, blocks_for<int>(scan_n, 256), 256, 0, st, scan_n, (const uint32_t*)blk, mode + 1);
       if (r == 0)
-        launch(c, k_pair_round<true>, pblocks, 128, 0, (const uint32_t*)sorted, src, ends_in, (const uint32_t*)st,
-               (uint32_t)nbins, cap[0], mode, T, pp, lst[0]);
+        launch(c, k_pair_round<true>, pblocks, kPairThreads, 0, (const uint32_t*)sorted, src, ends_in,
+               (const uint32_t*)st, (uint32_t)nbins, cap[0], mode, T, pp, lst[0]);
       else
-        launch(c, k_pair_round<false>, pblocks, 128, 0, (const uint32_t*)nullptr, (const Affine*)lst[(r - 1) & 1],
-               ends_in, (const uint32_t*)st, (uint32_t)nbins, cap[r], mode, T, pp, lst[r & 1]);
+        launch(c, k_pair_round<false>, pblocks, kPairThreads, 0, (const uint32_t*)nullptr,
+               (const Affine*)lst[(r - 1) & 1], ends_in, (const uint32_t*)st, (uint32_t)nbins, cap[r], mode, T, pp,
+               lst[r & 1]);
       ends_in = st + 1;
     }
     pair_mode = mode;
