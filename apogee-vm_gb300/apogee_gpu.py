@@ -394,6 +394,29 @@ class Context:
         self._check(st)
         return from_mont_bytes(vs.raw[:32 * k]), proof.raw, snap.raw
 
+    def batch_open_stacked(self, stacks, num_vars, cms, u, r, transcript: bytes, on_device: bool = False):
+        """pcs::batch_open_stacked. stacks: per stack its columns in slot
+        order (Fr in-memory bytes, or device pointers with on_device);
+        num_vars: one variable count per column, flattened (an int applies to
+        every column); cms: 64-byte commitments; u, r: canonical ints.
+        Returns (the stacks' values, 704-byte proof, transcript)."""
+        flat = [c for st in stacks for c in st]
+        nc, ns = len(flat), len(stacks)
+        nvs = [num_vars] * nc if isinstance(num_vars, int) else list(num_vars)
+        lens = (ctypes.c_size_t * max(ns, 1))(*[len(st) for st in stacks])
+        nv_arr = (ctypes.c_size_t * max(nc, 1))(*nvs)
+        snap = ctypes.create_string_buffer(bytes(transcript), TRANSCRIPT_BYTES)
+        vs = ctypes.create_string_buffer(32 * max(ns, 1))
+        proof = ctypes.create_string_buffer(PROOF_BYTES)
+        args = (nv_arr, lens, ctypes.c_size_t(ns), b"".join(cms), ctypes.c_size_t(len(cms)), to_mont_bytes(u),
+                ctypes.c_size_t(len(u)), to_mont_bytes(r), ctypes.c_size_t(len(r)), snap, vs, proof)
+        if on_device:
+            st = lib().apg_mercury_batch_open_stacked_device(self._h, (ctypes.c_void_p * max(nc, 1))(*flat), *args)
+        else:
+            st = lib().apg_mercury_batch_open_stacked(self._h, (ctypes.c_char_p * max(nc, 1))(*flat), *args)
+        self._check(st)
+        return from_mont_bytes(vs.raw[:32 * ns]), proof.raw, snap.raw
+
     # ---- zerocheck -----------------------------------------------------------
     def prove_zerocheck(self, terms, polys, num_vars: int, transcript: bytes, on_device: bool = False):
         """sumcheck::prove_zerocheck. terms: (coef, a, b-or-None) with coef a

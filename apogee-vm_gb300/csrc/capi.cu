@@ -565,44 +565,74 @@ int apg_mercury_open(apg_ctx* ctx, const uint8_t* evals, size_t num_vars, const 
   });
 }
 
-static int batch_open_common(Ctx& c, const void* const* cols, bool on_device, size_t k, size_t num_vars,
-                             const uint8_t* cms, const uint8_t* u, size_t u_len, uint8_t* transcript,
-                             uint8_t* vs_out, uint8_t* proof_out) {
-  if (k == 0) return APG_ERR_EMPTY_BATCH;
-  if (!cols || !cms || (!u && u_len) || !transcript || !vs_out || !proof_out) return APG_ERR_INVALID_ARGUMENT;
-  if (num_vars < 2 || num_vars > 54 || num_vars % 2) return APG_ERR_UNSUPPORTED_NUM_VARS;
-  if (u_len != num_vars) return APG_ERR_POINT_LENGTH_MISMATCH;
-  if (num_vars > 40) return APG_ERR_OUT_OF_MEMORY;
-  std::vector<host::F> uu;
-  if (!read_points_u(u, num_vars, uu)) return APG_ERR_NONCANONICAL;
+// batch_open_stacked's refusals (crates/pcs/src/lib.rs:713-754) in its order,
+// then the opening. cols: every stack's columns, stack after stack (host or
+// device pointers), num_vars: each column's variable count.
+static int stacked_open_common(Ctx& c, const void* const* cols, bool on_device, const size_t* num_vars,
+                               const size_t* stack_lens, size_t n_stacks, const uint8_t* cms, size_t n_cms,
+                               const uint8_t* u, size_t u_len, const uint8_t* r, size_t r_len, uint8_t* transcript,
+                               uint8_t* vs_out, uint8_t* proof_out) {
+  if (n_stacks == 0) return APG_ERR_EMPTY_BATCH;
+  if (!stack_lens) return APG_ERR_INVALID_ARGUMENT;
+  size_t ncols = 0;
+  for (size_t j = 0; j < n_stacks; ++j) {
+    if (stack_lens[j] == 0) return APG_ERR_EMPTY_BATCH;
+    ncols += stack_lens[j];
+  }
+  if (!cols || !num_vars || (!cms && n_cms) || (!u && u_len) || (!r && r_len) || !transcript || !vs_out ||
+      !proof_out)
+    return APG_ERR_INVALID_ARGUMENT;
+  if (n_cms != n_stacks) return APG_ERR_BATCH_LENGTH_MISMATCH;
+  const size_t width = num_vars[0];
+  for (size_t i = 1; i < ncols; ++i)
+    if (num_vars[i] != width) return APG_ERR_MIXED_COLUMN_SIZES;
+  const size_t nv = width + r_len;
+  if (width > 54 || r_len > 54 || nv < 2 || nv > 54 || nv % 2) return APG_ERR_UNSUPPORTED_NUM_VARS;
+  if (u_len != width) return APG_ERR_POINT_LENGTH_MISMATCH;
+  for (size_t j = 0; j < n_stacks; ++j)
+    if (stack_lens[j] > ((size_t)1 << r_len)) return APG_ERR_BATCH_LENGTH_MISMATCH;
+  if (nv > 40) return APG_ERR_OUT_OF_MEMORY;
+  std::vector<host::F> uu, rr;
+  if (!read_points_u(u, u_len, uu) || !read_points_u(r, r_len, rr)) return APG_ERR_NONCANONICAL;
   host::Transcript tr;
   if (!tr.load(transcript)) return APG_ERR_INVALID_ARGUMENT;
-  const size_t n = (size_t)1 << num_vars;
-  if (c.srs && c.srs_n < n) return APG_ERR_SRS_TOO_SMALL;
-  std::vector<const Fr*> ptrs(k);
+  if (!c.srs) return APG_ERR_NO_SRS;
+  if (c.srs_n < ((size_t)1 << nv)) return APG_ERR_SRS_TOO_SMALL;
+  const size_t column = (size_t)1 << width;
+  std::vector<const Fr*> ptrs(ncols);
   Fr* staged = nullptr;
   if (on_device) {
-    for (size_t j = 0; j < k; ++j) ptrs[j] = (const Fr*)cols[j];
+    for (size_t i = 0; i < ncols; ++i) ptrs[i] = (const Fr*)cols[i];
   } else {
-    APG_CUDA(cudaMallocAsync((void**)&staged, 32 * n * k, c.stream));
-    for (size_t j = 0; j < k; ++j) {
-      APG_CUDA(cudaMemcpyAsync(staged + j * n, cols[j], 32 * n, cudaMemcpyHostToDevice, c.stream));
-      ptrs[j] = staged + j * n;
+    APG_CUDA(cudaMallocAsync((void**)&staged, 32 * column * ncols, c.stream));
+    for (size_t i = 0; i < ncols; ++i) {
+      APG_CUDA(cudaMemcpyAsync(staged + i * column, cols[i], 32 * column, cudaMemcpyHostToDevice, c.stream));
+      ptrs[i] = staged + i * column;
     }
   }
   std::vector<host::F> vs;
   int st;
   try {
-    st = mercury_batch_open_impl(c, ptrs.data(), k, num_vars, cms, uu, tr, vs, proof_out);
+    st = mercury_batch_open_stacked_impl(c, ptrs.data(), stack_lens, n_stacks, width, cms, uu, rr, tr, vs,
+                                         proof_out);
   } catch (...) {
     if (staged) cudaFreeAsync(staged, c.stream);
     throw;
   }
   if (staged) APG_CUDA(cudaFreeAsync(staged, c.stream));
   if (st) return st;
-  memcpy(vs_out, vs.data(), 32 * k);
+  memcpy(vs_out, vs.data(), 32 * n_stacks);
   tr.save(transcript);
   return APG_OK;
+}
+
+// batch_open (crates/pcs/src/lib.rs:688-703): one column a stack, r = [].
+static int batch_open_common(Ctx& c, const void* const* cols, bool on_device, size_t k, size_t num_vars,
+                             const uint8_t* cms, const uint8_t* u, size_t u_len, uint8_t* transcript,
+                             uint8_t* vs_out, uint8_t* proof_out) {
+  const std::vector<size_t> ones(k, 1), nvs(k, num_vars);
+  return stacked_open_common(c, cols, on_device, nvs.data(), ones.data(), k, cms, k, u, u_len, nullptr, 0,
+                             transcript, vs_out, proof_out);
 }
 
 int apg_mercury_batch_open(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_t num_vars, const uint8_t* cms,
@@ -619,6 +649,27 @@ int apg_mercury_batch_open_device(apg_ctx* ctx, const void* const* d_cols, size_
                                   uint8_t* vs_out, uint8_t proof_out[704]) {
   return guarded(ctx, [&](Ctx& c) {
     return batch_open_common(c, d_cols, true, k, num_vars, cms, u, u_len, transcript, vs_out, proof_out);
+  });
+}
+
+int apg_mercury_batch_open_stacked(apg_ctx* ctx, const uint8_t* const* cols, const size_t* num_vars,
+                                   const size_t* stack_lens, size_t n_stacks, const uint8_t* cms, size_t n_cms,
+                                   const uint8_t* u, size_t u_len, const uint8_t* r, size_t r_len,
+                                   uint8_t* transcript, uint8_t* vs_out, uint8_t proof_out[704]) {
+  return guarded(ctx, [&](Ctx& c) {
+    return stacked_open_common(c, (const void* const*)cols, false, num_vars, stack_lens, n_stacks, cms, n_cms, u,
+                               u_len, r, r_len, transcript, vs_out, proof_out);
+  });
+}
+
+int apg_mercury_batch_open_stacked_device(apg_ctx* ctx, const void* const* d_cols, const size_t* num_vars,
+                                          const size_t* stack_lens, size_t n_stacks, const uint8_t* cms,
+                                          size_t n_cms, const uint8_t* u, size_t u_len, const uint8_t* r,
+                                          size_t r_len, uint8_t* transcript, uint8_t* vs_out,
+                                          uint8_t proof_out[704]) {
+  return guarded(ctx, [&](Ctx& c) {
+    return stacked_open_common(c, d_cols, true, num_vars, stack_lens, n_stacks, cms, n_cms, u, u_len, r, r_len,
+                               transcript, vs_out, proof_out);
   });
 }
 

@@ -8,6 +8,8 @@
 // all eight MSMs over the resident SRS. Host: the transcript and the O(1)
 // and O(b) scalar glue of the BDFG20 step (crates/pcs-verify/src/bdfg.rs),
 // exactly the reference's formulas.
+#include <algorithm>
+
 #include "sumcheck.cuh"
 
 namespace apg {
@@ -175,12 +177,19 @@ __global__ void k_numerator(const Fr* f, const Fr* q, size_t n, size_t nq, Fr c,
   st_fe(&out[i], v);
 }
 
-// f* = sum_c w_c col_c.
-__global__ void k_combine(const Fr* const* cols, const Fr* w, int k, size_t n, Fr* out) {
+// f* = sum_j w_j stack_j: stack j's column in slot s (cols[j * maxlen + s],
+// null past the stack's end) covers entries [s * 2^width, (s + 1) * 2^width).
+__global__ void k_combine_stacked(const Fr* const* cols, const Fr* w, int nstacks, size_t maxlen, int width,
+                                  size_t n, Fr* out) {
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const size_t slot = i >> width, row = i & (((size_t)1 << width) - 1);
   Fr acc = fe_zero<FrConsts>();
-  for (int c = 0; c < k; ++c) acc = fe_add(acc, fe_mul(ld_fe(&w[c]), ld_fe(&cols[c][i])));
+  if (slot < maxlen)
+    for (int j = 0; j < nstacks; ++j) {
+      const Fr* col = cols[(size_t)j * maxlen + slot];
+      if (col) acc = fe_add(acc, fe_mul(ld_fe(&w[j]), ld_fe(&col[row])));
+    }
   st_fe(&out[i], acc);
 }
 
@@ -507,61 +516,83 @@ int mercury_open_impl(Ctx& c, const Fr* d_f, size_t nv, const uint8_t cm[64], co
   return APG_OK;
 }
 
-int mercury_batch_open_impl(Ctx& c, const Fr* const* d_cols, size_t k, size_t nv, const uint8_t* cms,
-                            const std::vector<F>& u, host::Transcript& tr, std::vector<F>& vs,
-                            uint8_t proof_out[704]) {
+// batch_open_stacked (crates/pcs/src/lib.rs:705-789) past its refusals, which
+// the caller has checked: stack j's columns (d_cols, stack after stack, each
+// 2^width entries on the device) fill its first stack_lens[j] slots of a
+// (width + |r|)-variable table. Each column's value at u comes from one row
+// dot against eq(u_lo) and one dot against eq(u_hi); v_j = sum_s eq(r, s) *
+// col_{j,s}(u); the preamble absorbs the commitments, u || r and the values
+// and draws rho (:568-581); cm* = sum_j rho^j cm_j is a generic-base MSM and
+// f* = sum_j rho^j stack_j is opened at u || r. batch_open is r = [] with one
+// column a stack.
+int mercury_batch_open_stacked_impl(Ctx& c, const Fr* const* d_cols, const size_t* stack_lens, size_t nstacks,
+                                    size_t width, const uint8_t* cms, const std::vector<F>& u,
+                                    const std::vector<F>& r, host::Transcript& tr, std::vector<F>& vs,
+                                    uint8_t proof_out[704]) {
   using namespace host;
-  if (k == 0) return APG_ERR_EMPTY_BATCH;
-  if (nv < 2 || nv > 54 || nv % 2) return APG_ERR_UNSUPPORTED_NUM_VARS;
-  if (u.size() != nv) return APG_ERR_POINT_LENGTH_MISMATCH;
-  if (!c.srs) return APG_ERR_NO_SRS;
+  const size_t nv = width + r.size();
   const size_t n = (size_t)1 << nv;
-  if (c.srs_n < n) return APG_ERR_SRS_TOO_SMALL;
-  const size_t t = nv / 2, b = (size_t)1 << t;
-  std::vector<F> u1(u.begin(), u.begin() + t), u2(u.begin() + t, u.end());
+  size_t ncols = 0, maxlen = 0;
+  for (size_t j = 0; j < nstacks; ++j) {
+    ncols += stack_lens[j];
+    maxlen = std::max(maxlen, stack_lens[j]);
+  }
+  const size_t w1 = width / 2, b1 = (size_t)1 << w1, b2 = (size_t)1 << (width - w1);
+  std::vector<F> u1(u.begin(), u.begin() + w1), u2(u.begin() + w1, u.end());
   Fr* work;
-  const size_t words = 3 * b + k + n + 2;
+  const size_t words = b1 + 2 * b2 + ncols + nstacks + n;
   APG_CUDA(cudaMallocAsync((void**)&work, 32 * words, c.stream));
   struct Guard {
     Ctx& c;
     Fr* p;
     ~Guard() { cudaFreeAsync(p, c.stream); }
   } guard{c, work};
-  Fr *eq1 = work, *eq2 = eq1 + b, *h = eq2 + b, *w = h + b, *fstar = w + k;
-  // Each column's value at u, through the same restriction h: f(u) = <eq2, h>;
-  // the k values land in w and come back in one read.
+  Fr *eq1 = work, *eq2 = eq1 + b1, *h = eq2 + b2, *cv = h + b2, *w = cv + ncols, *fstar = w + nstacks;
   build_eq_table(c, u1, eq1);
   build_eq_table(c, u2, eq2);
-  for (size_t col = 0; col < k; ++col) {
-    launch(c, k_row_dot, nb(b * 32, 256), 256, 0, d_cols[col], (const Fr*)eq1, b, b, h);
-    launch(c, k_dot, 1, 256, 0, (const Fr*)eq2, (const Fr*)h, b, w + col);
+  for (size_t col = 0; col < ncols; ++col) {
+    launch(c, k_row_dot, nb(b2 * 32, 256), 256, 0, d_cols[col], (const Fr*)eq1, b1, b2, h);
+    launch(c, k_dot, 1, 256, 0, (const Fr*)eq2, (const Fr*)h, b2, cv + col);
   }
-  vs = read_frs(c, w, k);
-  tr.absorb_g1(T_COMMITMENT, cms, k);
-  std::vector<F> claim = u;
+  const std::vector<F> vals = read_frs(c, cv, ncols);
+  vs.assign(nstacks, fzero());
+  for (size_t j = 0, idx = 0; j < nstacks; ++j)
+    for (size_t s = 0; s < stack_lens[j]; ++s, ++idx) {
+      F e = fone();  // eq(r, s): variable i is bit i of the slot
+      for (size_t i = 0; i < r.size(); ++i) e = fmul(e, (s >> i) & 1 ? r[i] : fsub(fone(), r[i]));
+      vs[j] = fadd(vs[j], fmul(e, vals[idx]));
+    }
+  std::vector<F> point = u;
+  point.insert(point.end(), r.begin(), r.end());
+  tr.absorb_g1(T_COMMITMENT, cms, nstacks);
+  std::vector<F> claim = point;
   claim.insert(claim.end(), vs.begin(), vs.end());
   tr.absorb(T_EVALUATION_CLAIM, claim);
   F rho = tr.challenge(T_MERCURY_BATCH);
-  std::vector<F> wts(k);
+  std::vector<F> wts(nstacks);
   F acc = fone();
-  for (size_t i = 0; i < k; ++i) {
+  for (size_t i = 0; i < nstacks; ++i) {
     wts[i] = acc;
     acc = fmul(acc, rho);
   }
-  // cm* = sum rho^i cm_i through the general MSM.
-  Affine* d_cms = c.scratch[S_BASES].as<Affine>(k);
-  upload_points(c, cms, k, d_cms);
-  APG_CUDA(cudaMemcpyAsync(w, wts.data(), 32 * k, cudaMemcpyHostToDevice, c.stream));
+  // cm* = sum rho^j cm_j through the general MSM.
+  Affine* d_cms = c.scratch[S_BASES].as<Affine>(nstacks);
+  upload_points(c, cms, nstacks, d_cms);
+  APG_CUDA(cudaMemcpyAsync(w, wts.data(), 32 * nstacks, cudaMemcpyHostToDevice, c.stream));
   uint8_t cm_star[64];
-  msm_device(c, d_cms, nullptr, w, false, false, k, nullptr, cm_star);
-  const Fr** d_ptrs = c.scratch[S_TMP5].as<const Fr*>(k);
-  APG_CUDA(cudaMemcpyAsync(d_ptrs, d_cols, sizeof(Fr*) * k, cudaMemcpyHostToDevice, c.stream));
-  launch(c, k_combine, nb(n, 256), 256, 0, (const Fr* const*)d_ptrs, (const Fr*)w, (int)k, n, fstar);
+  msm_device(c, d_cms, nullptr, w, false, false, nstacks, nullptr, cm_star);
+  std::vector<const Fr*> table(nstacks * maxlen, nullptr);
+  for (size_t j = 0, idx = 0; j < nstacks; ++j)
+    for (size_t s = 0; s < stack_lens[j]; ++s) table[j * maxlen + s] = d_cols[idx++];
+  const Fr** d_table = c.scratch[S_TMP5].as<const Fr*>(table.size());
+  APG_CUDA(cudaMemcpyAsync(d_table, table.data(), sizeof(Fr*) * table.size(), cudaMemcpyHostToDevice, c.stream));
+  launch(c, k_combine_stacked, nb(n, 256), 256, 0, (const Fr* const*)d_table, (const Fr*)w, (int)nstacks, maxlen,
+         (int)width, n, fstar);
   F v;
-  int st = mercury_open_impl(c, fstar, nv, cm_star, u, tr, v, proof_out);
+  int st = mercury_open_impl(c, fstar, nv, cm_star, point, tr, v, proof_out);
   if (st) return st;
   F vstar = fzero();
-  for (size_t i = 0; i < k; ++i) vstar = fadd(vstar, fmul(wts[i], vs[i]));
+  for (size_t i = 0; i < nstacks; ++i) vstar = fadd(vstar, fmul(wts[i], vs[i]));
   if (v != vstar) throw Error(APG_ERR_INTERNAL, "the combined value is not the combination of the values");
   return APG_OK;
 }

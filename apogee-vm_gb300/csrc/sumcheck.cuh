@@ -101,8 +101,9 @@ size_t gkr_proof_len_impl(const uint8_t* blob, size_t len);
 
 int mercury_open_impl(Ctx& c, const Fr* d_f, size_t nv, const uint8_t cm[64], const std::vector<host::F>& u,
                       host::Transcript& tr, host::F& v_out, uint8_t proof_out[704]);
-int mercury_batch_open_impl(Ctx& c, const Fr* const* d_cols, size_t k, size_t nv, const uint8_t* cms,
-                            const std::vector<host::F>& u, host::Transcript& tr, std::vector<host::F>& vs,
-                            uint8_t proof_out[704]);
+int mercury_batch_open_stacked_impl(Ctx& c, const Fr* const* d_cols, const size_t* stack_lens, size_t nstacks,
+                                    size_t width, const uint8_t* cms, const std::vector<host::F>& u,
+                                    const std::vector<host::F>& r, host::Transcript& tr,
+                                    std::vector<host::F>& vs, uint8_t proof_out[704]);
 
 }  // namespace apg

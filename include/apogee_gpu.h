@@ -203,6 +203,29 @@ int apg_mercury_batch_open(apg_ctx* ctx, const uint8_t* const* cols, size_t k, s
 int apg_mercury_batch_open_device(apg_ctx* ctx, const void* const* d_cols, size_t k, size_t num_vars,
                                   const uint8_t* cms, const uint8_t* u, size_t u_len, uint8_t* transcript,
                                   uint8_t* vs_out, uint8_t proof_out[704]);
+/* pcs::batch_open_stacked (lib.rs:705-789), the prover's opening
+ * (crates/prover/src/lib.rs:1076): n_stacks stacks, stack j's columns in its
+ * first stack_lens[j] slots of a table over u || r (slot s = the r-variables'
+ * bits). cols lists every stack's columns, stack after stack (host, Fr in
+ * memory), num_vars each column's variable count; cms is n_cms x 64 bytes (the
+ * stacks' commit_stack commitments). Writes each stack's value
+ * v_j = sum_s eq(r, s) col_{j,s}(u) (vs_out, n_stacks x 32) and the proof of
+ * cm* = sum rho^j cm_j at u || r. Errors, in the reference's order:
+ * APG_ERR_EMPTY_BATCH (no stack, or an empty one), APG_ERR_BATCH_LENGTH_MISMATCH
+ * (n_cms != n_stacks), APG_ERR_MIXED_COLUMN_SIZES,
+ * APG_ERR_UNSUPPORTED_NUM_VARS (of width + r_len), APG_ERR_POINT_LENGTH_MISMATCH
+ * (u_len != the columns' width), APG_ERR_BATCH_LENGTH_MISMATCH (a stack longer
+ * than 2^r_len), APG_ERR_SRS_TOO_SMALL. */
+int apg_mercury_batch_open_stacked(apg_ctx* ctx, const uint8_t* const* cols, const size_t* num_vars,
+                                   const size_t* stack_lens, size_t n_stacks, const uint8_t* cms, size_t n_cms,
+                                   const uint8_t* u, size_t u_len, const uint8_t* r, size_t r_len,
+                                   uint8_t* transcript, uint8_t* vs_out, uint8_t proof_out[704]);
+/* As apg_mercury_batch_open_stacked with the columns in device memory. */
+int apg_mercury_batch_open_stacked_device(apg_ctx* ctx, const void* const* d_cols, const size_t* num_vars,
+                                          const size_t* stack_lens, size_t n_stacks, const uint8_t* cms,
+                                          size_t n_cms, const uint8_t* u, size_t u_len, const uint8_t* r,
+                                          size_t r_len, uint8_t* transcript, uint8_t* vs_out,
+                                          uint8_t proof_out[704]);
 
 /* ---- zerocheck (crates/sumcheck/src/lib.rs) ------------------------------ */
 

@@ -3,8 +3,8 @@
 // tests/ to check the CUDA library's proofs byte for byte.
 //
 //  * commit (crates/pcs/src/lib.rs:237-247), open (:313-492), batch_preamble
-//    (:568-581 and crates/pcs-verify/src/lib.rs:333), batch_open_stacked with
-//    r = [] (:705-789), symmetric_witness (:812-864).
+//    (:568-581 and crates/pcs-verify/src/lib.rs:333), batch_open and
+//    batch_open_stacked (:688-789), symmetric_witness (:812-864).
 //  * fft::Domain (crates/pcs/src/fft.rs:37-134); uni::{eval, div_by_linear,
 //    mul, add_scaled, vanishing, interpolate, pow_usize}
 //    (crates/pcs-verify/src/uni.rs:18-116); bdfg::{items, quotient,
@@ -340,23 +340,42 @@ inline int mercury_open(const Srs& srs, const Table& coeffs, const G1Bytes& cm, 
   return PCS_OK;
 }
 
-// batch_open = batch_open_stacked at r = [], every stack one column.
-inline int mercury_batch_open(const Srs& srs, const std::vector<Table>& cols, const std::vector<G1Bytes>& cms,
-                              const std::vector<Fr>& u, Transcript& tr, std::vector<Fr>& vs, MercuryProof& pf,
-                              size_t threads) {
-  if (cols.empty()) return PCS_EMPTY_BATCH;
-  if (cols.size() != cms.size()) return PCS_BATCH_LENGTH;
-  size_t width = (size_t)__builtin_ctzll(cols[0].size());
-  for (auto& c : cols)
-    if (c.size() != cols[0].size()) return PCS_MIXED_SIZES;
-  if (!check_num_vars(width)) return PCS_UNSUPPORTED_NUM_VARS;
+// batch_open_stacked (crates/pcs/src/lib.rs:705-789): stack j's column s sits
+// at slot s of a (width + |r|)-variable table; v_j = sum_s eq_r[s] * col_{j,s}(u)
+// (:756-764), the preamble absorbs the commitments, then u || r and the values
+// (:568-581), and f* = sum_j rho^j stack_j is opened at u || r (:766-788).
+// `stacks[j]` lists stack j's columns, each a table of 2^width entries.
+inline int mercury_batch_open_stacked(const Srs& srs, const std::vector<std::vector<const Table*>>& stacks,
+                                      const std::vector<G1Bytes>& cms, const std::vector<Fr>& u,
+                                      const std::vector<Fr>& r, Transcript& tr, std::vector<Fr>& vs,
+                                      MercuryProof& pf, size_t threads) {
+  if (stacks.empty()) return PCS_EMPTY_BATCH;
+  for (auto& st : stacks)
+    if (st.empty()) return PCS_EMPTY_BATCH;
+  if (stacks.size() != cms.size()) return PCS_BATCH_LENGTH;
+  const size_t column = stacks[0][0]->size();
+  for (auto& st : stacks)
+    for (const Table* c : st)
+      if (c->size() != column) return PCS_MIXED_SIZES;
+  const size_t width = (size_t)__builtin_ctzll(column);
+  if (!check_num_vars(width + r.size())) return PCS_UNSUPPORTED_NUM_VARS;
   if (u.size() != width) return PCS_POINT_LENGTH;
-  size_t n = cols[0].size();
+  const size_t slots = (size_t)1 << r.size();
+  for (auto& st : stacks)
+    if (st.size() > slots) return PCS_BATCH_LENGTH;
+  const size_t n = column << r.size();
   if (srs.g1.size() < n) return PCS_SRS_TOO_SMALL;
+  std::vector<Fr> point = u;
+  point.insert(point.end(), r.begin(), r.end());
+  const Table eq_r = eq_table(r);
   vs.clear();
-  for (auto& c : cols) vs.push_back(evaluate(c, u));
+  for (auto& st : stacks) {
+    Fr v = Fr::zero();
+    for (size_t s = 0; s < st.size(); ++s) v += eq_r[s] * evaluate(*st[s], u);
+    vs.push_back(v);
+  }
   append_g1(tr, tags::COMMITMENT, cms);
-  std::vector<Fr> claim = u;
+  std::vector<Fr> claim = point;
   claim.insert(claim.end(), vs.begin(), vs.end());
   tr.append_scalars(tags::EVALUATION_CLAIM, claim);
   Fr rho = tr.challenge(tags::MERCURY_BATCH);
@@ -365,13 +384,26 @@ inline int mercury_batch_open(const Srs& srs, const std::vector<Table>& cols, co
   for (size_t i = 0; i < cms.size(); ++i) G1Affine::from_bytes(cms[i].data(), cmp[i]);
   G1Bytes cm_star = g1_bytes(msm(cmp.data(), wts.data(), cmp.size(), threads));
   Table comb(n, Fr::zero());
-  for (size_t i = 0; i < n; ++i)
-    for (size_t c = 0; c < cols.size(); ++c) comb[i] += wts[c] * cols[c][i];
+  for (size_t i = 0; i < n; ++i) {
+    const size_t slot = i / column, row = i % column;
+    for (size_t j = 0; j < stacks.size(); ++j)
+      if (slot < stacks[j].size()) comb[i] += wts[j] * (*stacks[j][slot])[row];
+  }
   Fr v;
-  int st = mercury_open(srs, comb, cm_star, u, tr, v, pf, threads);
+  int st = mercury_open(srs, comb, cm_star, point, tr, v, pf, threads);
   if (st) return st;
   if (v != dot(wts, vs)) throw std::runtime_error("combined value mismatch");
   return PCS_OK;
+}
+
+// batch_open = batch_open_stacked at r = [], every stack one column
+// (crates/pcs/src/lib.rs:688-703).
+inline int mercury_batch_open(const Srs& srs, const std::vector<Table>& cols, const std::vector<G1Bytes>& cms,
+                              const std::vector<Fr>& u, Transcript& tr, std::vector<Fr>& vs, MercuryProof& pf,
+                              size_t threads) {
+  std::vector<std::vector<const Table*>> stacks;
+  for (auto& c : cols) stacks.push_back({&c});
+  return mercury_batch_open_stacked(srs, stacks, cms, u, {}, tr, vs, pf, threads);
 }
 
 }  // namespace oracle

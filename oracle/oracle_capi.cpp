@@ -318,6 +318,52 @@ int oracle_mercury_open(const uint8_t* srs_pts, size_t srs_n, const uint8_t* eva
   }
 }
 
+// batch_open_stacked: n_cols columns back to back (column c has 2^col_nv[c]
+// entries), stack j taking the next stack_lens[j] of them; n_cms commitments.
+// Returns 10 + the PcsStatus on a refusal.
+int oracle_mercury_batch_open_stacked(const uint8_t* srs_pts, size_t srs_n, const uint8_t* cols,
+                                      const size_t* col_nv, const size_t* stack_lens, size_t n_stacks,
+                                      const uint8_t* cms, size_t n_cms, const uint8_t* u, size_t u_len,
+                                      const uint8_t* r, size_t r_len, uint8_t* snap, size_t threads,
+                                      uint8_t* vs_out, uint8_t* proof_out) {
+  try {
+    Srs s = read_srs(srs_pts, srs_n);
+    size_t n_cols = 0;
+    for (size_t j = 0; j < n_stacks; ++j) n_cols += stack_lens[j];
+    std::vector<Table> tabs;
+    tabs.reserve(n_cols);
+    size_t off = 0;
+    for (size_t c = 0; c < n_cols; ++c) {
+      const size_t len = (size_t)1 << col_nv[c];
+      tabs.push_back(read_tables(cols + off, 1, len)[0]);
+      off += 32 * len;
+    }
+    std::vector<std::vector<const Table*>> stacks(n_stacks);
+    size_t c = 0;
+    for (size_t j = 0; j < n_stacks; ++j)
+      for (size_t e = 0; e < stack_lens[j]; ++e) stacks[j].push_back(&tabs[c++]);
+    std::vector<Fr> uv(u_len), rv(r_len);
+    for (size_t i = 0; i < u_len; ++i)
+      if (!read_fr(u + 32 * i, uv[i])) return 2;
+    for (size_t i = 0; i < r_len; ++i)
+      if (!read_fr(r + 32 * i, rv[i])) return 2;
+    std::vector<G1Bytes> cm(n_cms);
+    for (size_t i = 0; i < n_cms; ++i) memcpy(cm[i].data(), cms + 64 * i, 64);
+    Transcript tr;
+    if (!tr.restore(snap)) return 2;
+    std::vector<Fr> vs;
+    MercuryProof pf;
+    int st = mercury_batch_open_stacked(s, stacks, cm, uv, rv, tr, vs, pf, threads ? threads : 1);
+    if (st) return 10 + st;
+    for (size_t j = 0; j < n_stacks; ++j) vs[j].to_bytes(vs_out + 32 * j);
+    pf.to_bytes(proof_out);
+    tr.snapshot(snap);
+    return 0;
+  } catch (...) {
+    return 9;
+  }
+}
+
 int oracle_mercury_batch_open(const uint8_t* srs_pts, size_t srs_n, const uint8_t* cols, size_t k, size_t nv,
                               const uint8_t* cms, const uint8_t* u, uint8_t* snap, size_t threads, uint8_t* vs_out,
                               uint8_t* proof_out) {

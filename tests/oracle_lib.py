@@ -226,3 +226,28 @@ def accumulator_words(sides: bytes, scalars, points, checks):
                                         ct.c_size_t(n), cs, ct.c_size_t(len(checks)), out)
     assert rc == 0, rc
     return [fe_int(out.raw[32 * i:32 * i + 32]) for i in range(len(checks) + 6 * n)]
+
+
+def mle_eval(table, point):
+    """A multilinear table (variable j = bit j of the index) at `point`."""
+    t = [x % P_R for x in table]
+    for rj in point:
+        t = [(t[2 * i] + rj * (t[2 * i + 1] - t[2 * i])) % P_R for i in range(len(t) // 2)]
+    return t[0]
+
+
+def batch_open_stacked(srs: bytes, srs_n: int, stacks, col_nv, cms, u, r, snap: bytearray, threads: int = 8):
+    """The oracle's batch_open_stacked over canonical-int columns (stack after
+    stack, column c of 2^col_nv[c] entries). Returns (rc, values, proof); rc
+    is 0, or 10 + the oracle's refusal status. `snap` advances in place."""
+    flat = [c for st in stacks for c in st]
+    nc, ns = len(flat), len(stacks)
+    nvs = (ctypes.c_size_t * max(nc, 1))(*col_nv)
+    lens = (ctypes.c_size_t * max(ns, 1))(*[len(st) for st in stacks])
+    s = (ctypes.c_uint8 * SNAP).from_buffer(snap)
+    vs, proof = buf(32 * max(ns, 1)), buf(704)
+    rc = lib().oracle_mercury_batch_open_stacked(
+        srs, ctypes.c_size_t(srs_n), b"".join(fe(x) for c in flat for x in c), nvs, lens, ctypes.c_size_t(ns),
+        b"".join(cms), ctypes.c_size_t(len(cms)), b"".join(fe(x) for x in u), ctypes.c_size_t(len(u)),
+        b"".join(fe(x) for x in r), ctypes.c_size_t(len(r)), s, ctypes.c_size_t(threads), vs, proof)
+    return rc, [fe_int(vs.raw[32 * j:32 * j + 32]) for j in range(ns)], proof.raw

@@ -161,3 +161,86 @@ def test_open_shape_errors(ctx):
     with pytest.raises(A.PcsError) as e:
         ctx.batch_open([], 4, [], [1] * 4, A.transcript_init())
     assert e.value.variant == "EmptyBatch"
+
+
+@pytest.mark.parametrize("width,sigma,lens", [(4, 2, [4, 3, 1]), (3, 3, [8, 5, 1]), (5, 1, [2, 1]),
+                                              (0, 2, [4, 1]), (9, 3, [8, 2, 1, 7])])
+def test_batch_open_stacked_matches_oracle(ctx, width, sigma, lens):
+    """pcs::batch_open_stacked (crates/pcs/src/lib.rs:705-789): values, proof
+    bytes and transcript equal the oracle's; each value is its stack's
+    materialised table at u || r, whose commitment is the one opened."""
+    import apogee_gpu as A
+
+    rng = random.Random(300 + 17 * width + sigma)
+    nv = width + sigma
+    n = 1 << nv
+    srs = O.toy_srs(rng.randrange(O.P_R), n)
+    ctx.srs_upload(srs)
+    pick = lambda: rng.choice([0, 1, rng.getrandbits(32), rng.randrange(O.P_R)])  # noqa: E731
+    stacks = [[[pick() for _ in range(1 << width)] for _ in range(L)] for L in lens]
+    tables = [[x for c in st for x in c] + [0] * (((1 << sigma) - len(st)) << width) for st in stacks]
+    cms = [ctx.commit(A.to_mont_bytes(t), nv) for t in tables]
+    u = [rng.randrange(O.P_R) for _ in range(width)]
+    r = [rng.randrange(O.P_R) for _ in range(sigma)]
+    snap = A.transcript_init()
+    vs, proof, after = ctx.batch_open_stacked([[A.to_mont_bytes(c) for c in st] for st in stacks], width, cms, u,
+                                              r, snap)
+    osnap = bytearray(snap)
+    rc, ovs, oproof = O.batch_open_stacked(srs, n, stacks, [width] * sum(lens), cms, u, r, osnap)
+    assert rc == 0
+    assert vs == ovs == [O.mle_eval(t, u + r) for t in tables]
+    assert proof == oproof
+    assert after == bytes(osnap)
+
+
+def test_batch_open_stacked_from_device_columns(ctx):
+    import torch
+
+    import apogee_gpu as A
+
+    rng = random.Random(41)
+    width, sigma, lens = 6, 2, [4, 2]
+    nv = width + sigma
+    srs = O.toy_srs(rng.randrange(O.P_R), 1 << nv)
+    ctx.srs_upload(srs)
+    stacks = [[[rng.randrange(O.P_R) for _ in range(1 << width)] for _ in range(L)] for L in lens]
+    cms = [ctx.commit_stack([A.to_mont_bytes(c) for c in st], width) for st in stacks]
+    u = [rng.randrange(O.P_R) for _ in range(width)]
+    r = [rng.randrange(O.P_R) for _ in range(sigma)]
+    host = ctx.batch_open_stacked([[A.to_mont_bytes(c) for c in st] for st in stacks], width, cms, u, r,
+                                  A.transcript_init())
+    dev = [[torch.frombuffer(bytearray(A.to_mont_bytes(c)), dtype=torch.uint8).to("cuda:0") for c in st]
+           for st in stacks]
+    on_dev = ctx.batch_open_stacked([[t.data_ptr() for t in st] for st in dev], width, cms, u, r,
+                                    A.transcript_init(), on_device=True)
+    torch.cuda.synchronize()
+    assert on_dev == host
+
+
+def test_batch_open_stacked_refusal_order(ctx):
+    """EmptyBatch, BatchLengthMismatch (commitments), MixedColumnSizes,
+    UnsupportedNumVars, PointLengthMismatch, BatchLengthMismatch (slots),
+    SrsTooSmall: crates/pcs/src/lib.rs:713-754, in that order."""
+    import apogee_gpu as A
+
+    ctx.srs_generate(7, 16)
+    col = A.to_mont_bytes(list(range(4)))
+    col8 = A.to_mont_bytes(list(range(8)))
+    cms = [bytes(64)] * 2
+    u, r = [1, 2], [3, 4]
+    tr = A.transcript_init()
+
+    def refused(stacks, nvs, c, uu, rr):
+        with pytest.raises(A.PcsError) as e:
+            ctx.batch_open_stacked(stacks, nvs, c, uu, rr, tr)
+        return e.value.variant
+
+    assert refused([], 2, [], u, r) == "EmptyBatch"
+    assert refused([[col], []], 2, cms, u, r) == "EmptyBatch"
+    assert refused([[col], [col]], 2, cms[:1], u, r) == "BatchLengthMismatch"
+    assert refused([[col], [col, col8]], [2, 2, 3], cms, u, r) == "MixedColumnSizes"
+    assert refused([[col], [col]], 2, cms, u, r[:1]) == "UnsupportedNumVars"
+    assert refused([[col], [col]], 2, cms, u[:1], r) == "PointLengthMismatch"
+    assert refused([[col] * 5, [col]], 2, cms, u, r) == "BatchLengthMismatch"
+    ctx.srs_generate(7, 8)
+    assert refused([[col], [col]], 2, cms, u, r) == "SrsTooSmall"

@@ -6,6 +6,7 @@ crates/field/tests, crates/curve/tests/{fq,g1,msm}.rs, crates/poly/tests,
 crates/transcript/tests/{poseidon2,cases}.rs and crates/pcs/tests/kats.rs.
 """
 import ctypes
+import random
 
 import pytest
 
@@ -360,3 +361,85 @@ def test_accumulator_refusal_order(oracle):
     assert O.accumulator_msms(sides, scalars, pts, checks)[0] == 9
     assert O.accumulator_msms(sides, scalars, pts, [12, 13])[0] == 9
     assert O.accumulator_msms(sides, scalars, pts, [12, 13], weights=[1, 1])[0] == 10
+
+
+def _accumulator_batch():
+    rec = {"batch_value": {}, "batch_point": {}, "batch_claim": {}, "batch_cm": {}}
+    for line in O.golden_lines("accumulator.txt"):
+        f = line.split()
+        if f[0] == "batch_value":
+            rec["batch_value"][(int(f[1]), int(f[2]))] = hexb(f[3])
+        elif f[0] in ("batch_point", "batch_claim", "batch_cm"):
+            rec[f[0]][int(f[1])] = hexb(f[2])
+        elif f[0] in ("numvars", "batch_proof"):
+            rec[f[0]] = f[1]
+    return rec
+
+
+def test_stacked_opening_at_empty_r_replays_the_golden_batch(oracle):
+    """batch_open is batch_open_stacked at r = [] with one column a stack
+    (crates/pcs/src/lib.rs:688-703): the stacked entry point replays the
+    committed three-column batch proof byte for byte."""
+    rec = _accumulator_batch()
+    nv = int(rec["numvars"])
+    k = len(rec["batch_cm"])
+    stacks = [[[O.fe_int(rec["batch_value"][(c, i)]) for i in range(1 << nv)]] for c in range(k)]
+    u = [O.fe_int(rec["batch_point"][i]) for i in range(nv)]
+    srs = O.toy_srs(TOY_TAU, 1 << nv)
+    snap = O.new_snapshot()
+    rc, vs, proof = O.batch_open_stacked(srs, 1 << nv, stacks, [nv] * k, [rec["batch_cm"][c] for c in range(k)],
+                                         u, [], snap)
+    assert rc == 0
+    assert [O.fe(v) for v in vs] == [rec["batch_claim"][c] for c in range(k)]
+    assert proof.hex() == rec["batch_proof"]
+
+
+def _stacked_case(seed, width, sigma, lens):
+    rng = random.Random(seed)
+    stacks = [[[rng.randrange(O.P_R) for _ in range(1 << width)] for _ in range(L)] for L in lens]
+    tables = [[x for c in st for x in c] + [0] * (((1 << sigma) - len(st)) << width) for st in stacks]
+    u = [rng.randrange(O.P_R) for _ in range(width)]
+    r = [rng.randrange(O.P_R) for _ in range(sigma)]
+    return stacks, tables, u, r
+
+
+def test_stacked_values_are_the_stacks_at_u_r(oracle):
+    """v_j = sum_s eq(r, s) col_{j,s}(u) is stack j's table at u || r
+    (crates/pcs/tests/batch.rs:650-660), for a full, a short and a
+    one-column stack; the commitments are the materialised stacks'."""
+    width, sigma = 3, 3
+    stacks, tables, u, r = _stacked_case(5, width, sigma, [8, 5, 1])
+    nv = width + sigma
+    srs = O.toy_srs(TOY_TAU, 1 << nv)
+    cms = []
+    for t in tables:
+        cm = buf(64)
+        assert oracle.oracle_commit(srs, ctypes.c_size_t(1 << nv), b"".join(fe(x) for x in t), nv, 4, cm) == 0
+        cms.append(cm.raw)
+    rc, vs, proof = O.batch_open_stacked(srs, 1 << nv, stacks, [width] * 14, cms, u, r, O.new_snapshot())
+    assert rc == 0 and len(proof) == 704
+    assert vs == [O.mle_eval(t, u + r) for t in tables]
+
+
+def test_stacked_refusal_order(oracle):
+    """The refusals of batch_open_stacked in order (crates/pcs/src/lib.rs:713-754):
+    EmptyBatch, BatchLengthMismatch (commitments), MixedColumnSizes,
+    UnsupportedNumVars, PointLengthMismatch, BatchLengthMismatch (slots),
+    SrsTooSmall; the oracle returns 10 + its status."""
+    stacks, _, u, r = _stacked_case(6, 2, 2, [4, 2])
+    srs = O.toy_srs(TOY_TAU, 16)
+    cms = [bytes(64)] * 2
+
+    def run(st, nvs, c, uu, rr, srs_n=16):
+        return O.batch_open_stacked(srs, srs_n, st, nvs, c, uu, rr, O.new_snapshot())[0]
+
+    assert run([], [], [], u, r) == 15
+    assert run([stacks[0], []], [2] * 4, cms, u, r) == 15
+    assert run(stacks, [2] * 6, cms[:1], u, r) == 16
+    mixed = [stacks[0], [stacks[1][0], stacks[1][1] + stacks[1][1]]]
+    assert run(mixed, [2] * 5 + [3], cms, u, r) == 17
+    assert run(stacks, [2] * 6, cms, u, r[:1]) == 11
+    assert run(stacks, [2] * 6, cms, u[:1], r) == 12
+    long = [stacks[0] + [stacks[1][0]], stacks[1]]
+    assert run(long, [2] * 7, cms, u, r) == 16
+    assert run(stacks, [2] * 6, cms, u, r, srs_n=8) == 13
