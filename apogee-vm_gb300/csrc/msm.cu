@@ -1273,6 +1273,16 @@ size_t pair_resident_threads(Ctx& c) {
 constexpr size_t kMaxBins = (size_t)(kScanBlock - 1) * kScanBlock * kScanItems;  // one pass of the 3-kernel scan
 constexpr size_t kMaxGroupEntries = (size_t)1 << 28;                           // 1 GiB of sorted references
 
+// The accumulation's slices hold at least this many references: a group too
+// small to fill the resident wave gets fewer, longer slices, trading serial
+// additions a thread against levels of the edge fold. Measured on a GB300 over
+// 2^12 openings and 2^8-2^14-row shards: 4 beat 16 (4.85 -> 4.61 ms an
+// opening at 2^12) and tied 2.
+#ifndef APG_ACC_SEG_MIN
+#define APG_ACC_SEG_MIN 4
+#endif
+constexpr size_t kAccSegMin = APG_ACC_SEG_MIN;
+
 // One group: columns share the plan, the bases and one pass of every kernel.
 void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols& cols, int ncols, size_t nmax,
                const MsmPlan& p, bool small_scalars, bool scalars_canonical, uint8_t* d_out) {
@@ -1293,7 +1303,8 @@ void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols
   uint32_t* sorted = c.scratch[S_SORTED].as<uint32_t>(std::max<size_t>(emax, 1));
   Xyzz* buckets = c.scratch[S_BUCKETS].as<Xyzz>(nbins);
 
-  const size_t nseg = std::max<size_t>(1, std::min(acc_resident_threads(c), (emax + 15) / 16));
+  const size_t nseg =
+      std::max<size_t>(1, std::min(acc_resident_threads(c), (emax + kAccSegMin - 1) / kAccSegMin));
   constexpr int kFoldLen = 8;
   uint32_t* ikeys[2] = {c.scratch[S_HEAD].as<uint32_t>(2 * nseg), c.scratch[S_TAIL].as<uint32_t>(2 * nseg)};
   Xyzz* ipts[2] = {c.scratch[S_TMP0].as<Xyzz>(2 * nseg), c.scratch[S_TMP1].as<Xyzz>(2 * nseg)};
