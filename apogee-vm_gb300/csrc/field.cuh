@@ -325,32 +325,40 @@ __device__ __forceinline__ bool fe_lt_mod(const uint32_t a[8]) {
 }
 
 // 1/a by the binary extended Euclidean algorithm on the Montgomery value A =
-// aR: with u = A, v = m, x1 = 1, x2 = 0 it keeps A*x1 = u and A*x2 = v (mod m),
-// halves whichever of u, v is even (halving x mod m alongside) and otherwise
-// subtracts the smaller from the larger, until u or v is 1; then x = A^-1 =
-// a^-1 R^-1 and a^-1 R = x * R^3 (one Montgomery product with R^3 = R2 * R2
-// reduced once). Variable time (the inputs are public values). Every step
-// strictly shrinks u * v < 2^510 or makes u or v even, so at most about 1020
-// steps run; the loop is also capped. 0 maps to 0.
+// aR: with u = A, v = m, x1 = 1, x2 = 0 it keeps A*x1 = u and A*x2 = v (mod m).
+// An even u loses all its trailing zero bits at once (up to 31 a step) and x1
+// is divided by the same power of two mod m in one multiply-add; likewise v
+// and x2; otherwise the smaller of u, v is subtracted from the larger. It
+// stops when u or v is 1; then x = A^-1 = a^-1 R^-1 and a^-1 R = x * R^3 (one
+// Montgomery product with R^3 = R2 * R2 reduced once). Variable time (the
+// inputs are public values). Every subtraction leaves an even value, so the
+// steps number at most about twice the 510 bits that u * v < 2^510 can shed;
+// the loop is also capped. 0 maps to 0.
+
+// x * 2^-s mod m for x < m, 1 <= s <= 31: with k = x * (-m^-1) mod 2^s,
+// x + k*m is a multiple of 2^s below 2^s * m, so its quotient is below m.
 template <class C>
-__device__ __forceinline__ void inv_half(uint32_t x[8]) {  // x/2 mod m for x < m
+__device__ __forceinline__ void inv_div_pow2(uint32_t x[8], int s) {
   const uint32_t p[8] = {C::P0, C::P1, C::P2, C::P3, C::P4, C::P5, C::P6, C::P7};
-  uint32_t t[8];
-  if (x[0] & 1u) {  // x + m < 2^255: no carry out of 256 bits
-    uint64_t c = 0;
+  const uint32_t k = (x[0] * C::INV) & ((1u << s) - 1u);
+  uint32_t t[9];
+  uint64_t c = 0;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      c += (uint64_t)x[i] + p[i];
-      t[i] = (uint32_t)c;
-      c >>= 32;
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < 8; ++i) t[i] = x[i];
+  for (int i = 0; i < 8; ++i) {
+    c += (uint64_t)x[i] + (uint64_t)k * p[i];
+    t[i] = (uint32_t)c;
+    c >>= 32;
   }
+  t[8] = (uint32_t)c;
 #pragma unroll
-  for (int i = 0; i < 7; ++i) x[i] = __funnelshift_r(t[i], t[i + 1], 1);
-  x[7] = t[7] >> 1;
+  for (int i = 0; i < 8; ++i) x[i] = __funnelshift_r(t[i], t[i + 1], s);
+}
+
+// w >> s for 1 <= s <= 31.
+__device__ __forceinline__ void inv_shift(uint32_t w[8], int s) {
+#pragma unroll
+  for (int i = 0; i < 7; ++i) w[i] = __funnelshift_r(w[i], w[i + 1], s);
+  w[7] >>= s;
 }
 
 template <class C>
@@ -405,15 +413,13 @@ __device__ __noinline__ Fe<C> fe_inverse(const Fe<C>& a) {
   };
   for (int guard = 0; guard < 4096 && !is_one(u) && !is_one(v); ++guard) {
     if (!(u[0] & 1u)) {
-#pragma unroll
-      for (int i = 0; i < 7; ++i) u[i] = __funnelshift_r(u[i], u[i + 1], 1);
-      u[7] >>= 1;
-      inv_half<C>(x1);
+      const int sh = u[0] ? __ffs((int)u[0]) - 1 : 31;
+      inv_shift(u, sh);
+      inv_div_pow2<C>(x1, sh);
     } else if (!(v[0] & 1u)) {
-#pragma unroll
-      for (int i = 0; i < 7; ++i) v[i] = __funnelshift_r(v[i], v[i + 1], 1);
-      v[7] >>= 1;
-      inv_half<C>(x2);
+      const int sh = v[0] ? __ffs((int)v[0]) - 1 : 31;
+      inv_shift(v, sh);
+      inv_div_pow2<C>(x2, sh);
     } else {
       bool ge = true;  // u >= v
 #pragma unroll
