@@ -38,11 +38,29 @@ inline Srs toy_srs(const Fr& tau, size_t count, size_t threads) {
     sc[i] = acc;
     acc *= tau;
   }
+  // Fixed-base comb: comb[8j + ...] holds d * 2^(8j) G for every byte value d,
+  // so [s]G is 32 mixed additions (the points are the recipe's; only the
+  // arithmetic that reaches them is faster than a scalar multiplication each).
+  std::vector<G1Jac> cj(32 * 256);
+  G1Jac base = G1Jac::from(G1Affine::generator());
+  for (int j = 0; j < 32; ++j) {
+    cj[256 * j] = G1Jac::identity();
+    for (int d = 1; d < 256; ++d) cj[256 * j + d] = cj[256 * j + d - 1].add(base);
+    base = cj[256 * j + 255].add(base);  // 256 * 2^(8j) G
+  }
+  std::vector<G1Affine> comb = batch_to_affine(cj);
   std::vector<G1Jac> pj(count);
   std::vector<std::thread> pool;
   for (size_t t = 0; t < threads; ++t)
     pool.emplace_back([&, t] {
-      for (size_t i = t; i < count; i += threads) pj[i] = G1Jac::from(G1Affine::generator()).mul(sc[i]);
+      uint8_t b[32];
+      for (size_t i = t; i < count; i += threads) {
+        sc[i].to_bytes(b);
+        G1Jac acc = G1Jac::identity();
+        for (int j = 0; j < 32; ++j)
+          if (b[j]) acc = acc.add_affine(comb[256 * j + b[j]]);
+        pj[i] = acc;
+      }
     });
   for (auto& th : pool) th.join();
   return Srs{batch_to_affine(pj)};

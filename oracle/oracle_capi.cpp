@@ -3,6 +3,7 @@
 // field element crosses as 32 canonical little-endian bytes, every G1 point as
 // 64 canonical bytes (all-zero = infinity), transcripts as the 226-byte
 // snapshot tuple. Returns 0 on success, a nonzero status otherwise.
+#include <thread>
 #include <chrono>
 #include <memory>
 
@@ -276,6 +277,49 @@ static Srs read_srs(const uint8_t* pts, size_t n) {
   for (size_t i = 0; i < n; ++i)
     if (!G1Affine::from_bytes(pts + 64 * i, s.g1[i])) throw std::runtime_error("bad SRS point");
   return s;
+}
+
+// f(tau) = sum_i coeffs[i] tau^i for n canonical coefficients: the scalar of
+// the known-tau identity commit(f) = [f(tau)]G over a seeded-tau SRS
+// (crates/pcs/src/lib.rs:237-247 reads the table as coefficients). Horner per
+// chunk on `threads` host threads, chunks joined by tau^(chunk start).
+int oracle_poly_at(const uint8_t* coeffs, size_t n, const uint8_t* tau, size_t threads, uint8_t* out) {
+  Fr t;
+  if (!read_fr(tau, t)) return 2;
+  size_t nt = std::max<size_t>(1, std::min<size_t>(threads ? threads : 1, n / 4096 + 1));
+  size_t step = (n + nt - 1) / nt;
+  std::vector<Fr> part(nt, Fr::zero());
+  std::vector<int> bad(nt, 0);
+  std::vector<std::thread> pool;
+  for (size_t w = 0; w < nt; ++w) {
+    pool.emplace_back([&, w] {
+      size_t b = w * step, e = std::min(n, b + step);
+      Fr acc = Fr::zero();
+      for (size_t i = e; i-- > b;) {
+        Fr c;
+        if (!read_fr(coeffs + 32 * i, c)) {
+          bad[w] = 1;
+          return;
+        }
+        acc = acc * t + c;
+      }
+      part[w] = acc;
+    });
+  }
+  for (auto& th : pool) th.join();
+  Fr acc = Fr::zero();
+  for (size_t w = nt; w-- > 0;) {
+    if (bad[w]) return 2;
+    size_t b = w * step;
+    if (b >= n) continue;
+    // acc currently holds the value of the chunks above w, relative to their start
+    Fr tp = Fr::one(), base = t;
+    for (size_t e = std::min(n, b + step) - b; e; e >>= 1, base = base * base)
+      if (e & 1) tp = tp * base;
+    acc = acc * tp + part[w];
+  }
+  acc.to_bytes(out);
+  return 0;
 }
 
 int oracle_commit(const uint8_t* srs_pts, size_t srs_n, const uint8_t* evals, size_t nv, size_t threads, uint8_t* out) {

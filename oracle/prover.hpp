@@ -15,18 +15,53 @@
 // Circuits arrive in the library's compact resolved form (the "APGC" blob the
 // C ABI takes); parse_circuit reads it.
 #pragma once
+#include <algorithm>
 #include <array>
 #include <stdexcept>
+#include <thread>
 #include <vector>
 
 #include "transcript.hpp"
 
 namespace oracle {
 
+// Runs f(begin, end, worker) over [0, n) split into contiguous chunks, one
+// per host thread (the reference splits the same loops into rayon blocks,
+// crates/gkr/src/lib.rs:189,302-336). Sums taken per chunk and added after
+// are the same field elements in any order, so the results do not depend
+// on the thread count.
+template <class F>
+inline void parallel_chunks(size_t n, F f) {
+  size_t hw = std::max<size_t>(1, std::thread::hardware_concurrency());
+  size_t nt = std::min<size_t>(hw, std::max<size_t>(1, n / 1024));
+  if (nt <= 1) {
+    f((size_t)0, n, (size_t)0);
+    return;
+  }
+  std::vector<std::thread> pool;
+  size_t step = (n + nt - 1) / nt;
+  for (size_t w = 0; w < nt; ++w) {
+    size_t b = w * step, e = std::min(n, b + step);
+    if (b >= e) break;
+    pool.emplace_back([=, &f] { f(b, e, w); });
+  }
+  for (auto& t : pool) t.join();
+}
+
+inline size_t parallel_workers() { return std::max<size_t>(1, std::thread::hardware_concurrency()); }
+
 typedef std::vector<Fr> Table;
 
 inline void bind_table(Table& t, const Fr& r) {
   size_t half = t.size() / 2;
+  if (half >= (1u << 14)) {  // large tables: out of place, split across threads
+    Table out(half);
+    parallel_chunks(half, [&](size_t b, size_t e, size_t) {
+      for (size_t i = b; i < e; ++i) out[i] = t[2 * i] + r * (t[2 * i + 1] - t[2 * i]);
+    });
+    t.swap(out);
+    return;
+  }
   for (size_t i = 0; i < half; ++i) {
     Fr lo = t[2 * i], hi = t[2 * i + 1];
     t[i] = lo + r * (hi - lo);
@@ -360,7 +395,10 @@ struct Resolved {
   }
   Fr eval(size_t i, const Fr* lower, const Fr* upper, const Fr* virt, const std::vector<Fr>& cache) const {
     auto& s = sources[i];
-    std::vector<Fr> ops(s.size() ? s.size() : 1);  // a Linear gate may read a hundred columns
+    // One operand buffer per host thread (a Linear gate may read a hundred
+    // columns); eval_gate consumes it before the next eval on this thread.
+    thread_local std::vector<Fr> ops;
+    if (ops.size() < s.size() + 1) ops.resize(s.size() + 1);
     for (size_t j = 0; j < s.size(); ++j) {
       switch (s[j].first) {
         case LOWER: ops[j] = lower[s[j].second]; break;
@@ -379,7 +417,7 @@ struct Resolved {
     return eval(cached + j, lower, upper, virt, cache);
   }
   Fr summand(const std::vector<Fr>& w, const Fr* lower, const Fr* upper, const Fr* virt) const {
-    std::vector<Fr> cache;
+    thread_local std::vector<Fr> cache;
     fill_cache(lower, upper, virt, cache);
     Fr acc = Fr::zero();
     for (size_t j = 0; j < w.size(); ++j) acc += gate(j, lower, upper, virt, cache) * w[j];
@@ -409,20 +447,22 @@ inline std::vector<Table> produce(const Circuit& c, const LayerValues& vals, siz
   const auto& cols = vals[k];
   size_t w = cols.size();
   std::vector<Table> out(L.width, Table(rows));
-  std::vector<Fr> lower(w), upper(w), virt(c.virtuals.size()), cache;
-  for (size_t y = 0; y < rows; ++y) {
-    if (L.halving) {
-      for (size_t i = 0; i < w; ++i) {
-        lower[i] = cols[i][y];
-        upper[i] = cols[i][y + rows];
+  parallel_chunks(rows, [&](size_t y0, size_t y1, size_t) {
+    std::vector<Fr> lower(w), upper(w), virt(c.virtuals.size()), cache;
+    for (size_t y = y0; y < y1; ++y) {
+      if (L.halving) {
+        for (size_t i = 0; i < w; ++i) {
+          lower[i] = cols[i][y];
+          upper[i] = cols[i][y + rows];
+        }
+      } else {
+        for (size_t i = 0; i < w; ++i) lower[i] = cols[i][y];
+        for (size_t v = 0; v < c.virtuals.size(); ++v) virt[v] = virtual_at_row(c.virtuals[v], y);
       }
-    } else {
-      for (size_t i = 0; i < w; ++i) lower[i] = cols[i][y];
-      for (size_t v = 0; v < c.virtuals.size(); ++v) virt[v] = virtual_at_row(c.virtuals[v], y);
+      res.fill_cache(lower.data(), upper.data(), virt.data(), cache);
+      for (size_t j = 0; j < L.width; ++j) out[j][y] = res.gate(j, lower.data(), upper.data(), virt.data(), cache);
     }
-    res.fill_cache(lower.data(), upper.data(), virt.data(), cache);
-    for (size_t j = 0; j < L.width; ++j) out[j][y] = res.gate(j, lower.data(), upper.data(), virt.data(), cache);
-  }
+  });
   return out;
 }
 
@@ -444,38 +484,44 @@ inline std::pair<std::vector<std::array<Fr, 4>>, std::vector<Fr>> prove_layer_su
   std::vector<std::array<Fr, 4>> rounds;
   std::vector<Fr> point;
   size_t nl = lower_t.size(), nu = upper_t.size(), nv = kinds.size();
-  std::vector<Fr> lo(nl), los(nl), up(nu), ups(nu), vv(nv), vs(nv);
   for (size_t round = 0; round < n; ++round) {
     size_t half = eq.size() / 2;
     size_t bound = point.size();
+    std::vector<std::array<Fr, 4>> part(parallel_workers(), {Fr::zero(), Fr::zero(), Fr::zero(), Fr::zero()});
+    parallel_chunks(half, [&](size_t i0, size_t i1, size_t wk) {
+      std::vector<Fr> lo(nl), los(nl), up(nu), ups(nu), vv(nv), vs(nv);
+      std::vector<Fr> at(n, Fr::zero());
+      for (size_t i = 0; i < bound; ++i) at[i] = point[i];
+      std::array<Fr, 4>& acc = part[wk];
+      for (size_t i = i0; i < i1; ++i) {
+        for (size_t x = 0; x < nl; ++x) {
+          lo[x] = lower_t[x][2 * i];
+          los[x] = lower_t[x][2 * i + 1] - lo[x];
+        }
+        for (size_t x = 0; x < nu; ++x) {
+          up[x] = upper_t[x][2 * i];
+          ups[x] = upper_t[x][2 * i + 1] - up[x];
+        }
+        if (nv) {
+          for (size_t j = bound + 1; j < n; ++j) at[j] = Fr::from_u64((i >> (j - bound - 1)) & 1);
+          at[bound] = Fr::zero();
+          for (size_t x = 0; x < nv; ++x) vv[x] = virtual_at_point(kinds[x], at);
+          at[bound] = Fr::one();
+          for (size_t x = 0; x < nv; ++x) vs[x] = virtual_at_point(kinds[x], at) - vv[x];
+        }
+        Fr e = eq[2 * i], es = eq[2 * i + 1] - eq[2 * i];
+        for (int node = 0; node < 4; ++node) {
+          acc[node] += e * res.summand(weights, lo.data(), up.data(), vv.data());
+          e += es;
+          for (size_t x = 0; x < nl; ++x) lo[x] += los[x];
+          for (size_t x = 0; x < nu; ++x) up[x] += ups[x];
+          for (size_t x = 0; x < nv; ++x) vv[x] += vs[x];
+        }
+      }
+    });
     std::array<Fr, 4> acc = {Fr::zero(), Fr::zero(), Fr::zero(), Fr::zero()};
-    std::vector<Fr> at(n, Fr::zero());
-    for (size_t i = 0; i < bound; ++i) at[i] = point[i];
-    for (size_t i = 0; i < half; ++i) {
-      for (size_t x = 0; x < nl; ++x) {
-        lo[x] = lower_t[x][2 * i];
-        los[x] = lower_t[x][2 * i + 1] - lo[x];
-      }
-      for (size_t x = 0; x < nu; ++x) {
-        up[x] = upper_t[x][2 * i];
-        ups[x] = upper_t[x][2 * i + 1] - up[x];
-      }
-      if (nv) {
-        for (size_t j = bound + 1; j < n; ++j) at[j] = Fr::from_u64((i >> (j - bound - 1)) & 1);
-        at[bound] = Fr::zero();
-        for (size_t x = 0; x < nv; ++x) vv[x] = virtual_at_point(kinds[x], at);
-        at[bound] = Fr::one();
-        for (size_t x = 0; x < nv; ++x) vs[x] = virtual_at_point(kinds[x], at) - vv[x];
-      }
-      Fr e = eq[2 * i], es = eq[2 * i + 1] - eq[2 * i];
-      for (int node = 0; node < 4; ++node) {
-        acc[node] += e * res.summand(weights, lo.data(), up.data(), vv.data());
-        e += es;
-        for (size_t x = 0; x < nl; ++x) lo[x] += los[x];
-        for (size_t x = 0; x < nu; ++x) up[x] += ups[x];
-        for (size_t x = 0; x < nv; ++x) vv[x] += vs[x];
-      }
-    }
+    for (auto& p : part)
+      for (int node = 0; node < 4; ++node) acc[node] += p[node];
     auto g = interpolate_cubic(acc);
     t.append_scalars(tags::SUMCHECK_ROUND, g.data(), 4);
     Fr r = t.challenge(tags::SUMCHECK_CHALLENGE);

@@ -251,3 +251,12 @@ def batch_open_stacked(srs: bytes, srs_n: int, stacks, col_nv, cms, u, r, snap: 
         b"".join(cms), ctypes.c_size_t(len(cms)), b"".join(fe(x) for x in u), ctypes.c_size_t(len(u)),
         b"".join(fe(x) for x in r), ctypes.c_size_t(len(r)), s, ctypes.c_size_t(threads), vs, proof)
     return rc, [fe_int(vs.raw[32 * j:32 * j + 32]) for j in range(ns)], proof.raw
+
+
+def poly_at(coeffs: bytes, n: int, x: int, threads: int = 16) -> int:
+    """sum_i c_i x^i over n canonical 32-byte coefficients (the oracle's
+    threaded Horner): the scalar of the known-tau identity cm = [f(tau)]G."""
+    out = buf(32)
+    rc = lib().oracle_poly_at(coeffs, ctypes.c_size_t(n), fe(x), ctypes.c_size_t(threads), out)
+    assert rc == 0, rc
+    return fe_int(out.raw)

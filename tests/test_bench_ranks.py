@@ -55,7 +55,7 @@ def test_reference_arm_prints_once_under_torchrun():
     rank 1 exits 0 without work."""
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), "bench.py", "--impl", "reference",
-           "--gpus", "2", "--steps", "1", "--warmup", "0"]
+           "--gpus", "2", "--steps", "1", "--warmup", "0", "--log2n", "16"]
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
