@@ -779,6 +779,52 @@ int apg_transcript_challenge(uint8_t snapshot[226], uint64_t tag, uint8_t out[32
   return APG_OK;
 }
 
+int apg_transcript_observe(uint8_t snapshot[226], const uint8_t x[32]) {
+  host::Transcript tr;
+  if (!snapshot || !x || !tr.load(snapshot)) return APG_ERR_INVALID_ARGUMENT;
+  host::F v;
+  memcpy(v.w, x, 32);
+  if (!host::below_p(v.w)) return APG_ERR_NONCANONICAL;
+  tr.observe(v);
+  tr.save(snapshot);
+  return APG_OK;
+}
+
+int apg_transcript_sample(uint8_t snapshot[226], uint8_t out[32]) {
+  host::Transcript tr;
+  if (!snapshot || !out || !tr.load(snapshot)) return APG_ERR_INVALID_ARGUMENT;
+  host::F x = tr.sample();
+  memcpy(out, x.w, 32);
+  tr.save(snapshot);
+  return APG_OK;
+}
+
+int apg_transcript_append_bytes(uint8_t snapshot[226], uint64_t tag, const uint8_t* bytes, size_t len) {
+  host::Transcript tr;
+  if (!snapshot || (len && !bytes) || !tr.load(snapshot)) return APG_ERR_INVALID_ARGUMENT;
+  tr.absorb_bytes(tag, bytes, len);
+  tr.save(snapshot);
+  return APG_OK;
+}
+
+int apg_io_digest(const uint8_t* input, size_t input_len, const uint8_t* output, size_t output_len,
+                  uint8_t out[32]) {
+  if (!out || (input_len && !input) || (output_len && !output)) return APG_ERR_INVALID_ARGUMENT;
+  host::F d = host::io_digest(input, input_len, output, output_len);
+  memcpy(out, d.w, 32);
+  return APG_OK;
+}
+
+int apg_poseidon2_permute(uint8_t state[96]) {
+  if (!state) return APG_ERR_INVALID_ARGUMENT;
+  host::F s[3];
+  for (int i = 0; i < 3; ++i)
+    if (!host::from_bytes(state + 32 * i, s[i])) return APG_ERR_NONCANONICAL;
+  host::permute(s);
+  for (int i = 0; i < 3; ++i) host::to_bytes(s[i], state + 32 * i);
+  return APG_OK;
+}
+
 int apg_ctx_set_timing(apg_ctx* ctx, int on) {
   return guarded(ctx, [&](Ctx& c) {
     c.timers.flush();

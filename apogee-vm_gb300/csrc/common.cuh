@@ -40,6 +40,7 @@ enum DeviceFlag : uint32_t {
   DEV_TRANSCRIPT = 4u,     // a transcript invariant was broken
   DEV_DEGENERATE = 8u,     // Mercury's {z, 1/z, alpha} had a repeat
   DEV_NONZERO_REM = 16u,   // a division that must be exact left a remainder
+  DEV_INVERSE = kFlagInverse,  // a field inversion did not converge (field.cuh)
 };
 
 // A grow-only device buffer.
@@ -172,6 +173,7 @@ struct Ctx {
       if (f & DEV_OFF_CURVE) throw Error(APG_ERR_INVALID_POINT, "an input point is not on the curve");
       if (f & DEV_DEGENERATE) throw Error(APG_ERR_DEGENERATE_CHALLENGE, "degenerate Mercury challenge set");
       if (f & DEV_NONZERO_REM) throw Error(APG_ERR_INTERNAL, "an exact division left a remainder");
+      if (f & DEV_INVERSE) throw Error(APG_ERR_INTERNAL, "a field inversion did not converge");
       throw Error(APG_ERR_INTERNAL, "device invariant failed");
     }
   }

@@ -159,14 +159,14 @@ __device__ __forceinline__ Xyzz xyzz_neg(const Xyzz& p) {
 }
 
 // XYZZ -> affine (Montgomery); infinity -> (0, 0). One inversion.
-__device__ __forceinline__ Affine xyzz_to_affine(const Xyzz& p) {
+__device__ __forceinline__ Affine xyzz_to_affine(const Xyzz& p, uint32_t* flags = nullptr) {
   Affine a;
   if (xyzz_is_inf(p)) {
     a.x = fe_zero<FqConsts>();
     a.y = fe_zero<FqConsts>();
     return a;
   }
-  Fq t = fe_inverse(cmul(p.zz, p.zzz));
+  Fq t = fe_inverse(cmul(p.zz, p.zzz), flags);
   a.x = cmul(p.x, cmul(t, p.zzz));
   a.y = cmul(p.y, cmul(t, p.zz));
   return a;

@@ -392,8 +392,16 @@ __device__ __forceinline__ void inv_sub_plain(uint32_t x[8], const uint32_t y[8]
   }
 }
 
+// Bit a kernel raises in its context's device flags when an inversion did not
+// converge (the binary extended Euclid below ends in far fewer steps than its
+// guard for every nonzero input; the flag makes a broken invariant an error
+// instead of a wrong value). The host reads it as DEV_INVERSE.
+constexpr uint32_t kFlagInverse = 32u;
+
+// 1/a mod p (0 for 0). `flags` (nullable) receives kFlagInverse if the loop's
+// guard ends it.
 template <class C>
-__device__ __noinline__ Fe<C> fe_inverse(const Fe<C>& a) {
+__device__ __noinline__ Fe<C> fe_inverse(const Fe<C>& a, uint32_t* flags = nullptr) {
   if (fe_is_zero(a)) return a;
   const uint32_t p[8] = {C::P0, C::P1, C::P2, C::P3, C::P4, C::P5, C::P6, C::P7};
   uint32_t u[8], v[8], x1[8], x2[8];
@@ -438,6 +446,7 @@ __device__ __noinline__ Fe<C> fe_inverse(const Fe<C>& a) {
       }
     }
   }
+  if (!is_one(u) && !is_one(v) && flags) atomicOr(flags, kFlagInverse);
   Fe<C> x;
   const bool from_u = is_one(u);
 #pragma unroll

@@ -225,8 +225,8 @@ enum Tag : uint64_t {
   T_COMMITMENT = 3, T_SUMCHECK_ROUND = 4, T_SUMCHECK_CHALLENGE = 5, T_EVALUATION_CLAIM = 6, T_PCS_OPENING = 7,
   T_WITNESS_DIGEST = 8, T_SUMCHECK_FINAL_EVALS = 9, T_MERCURY_INSTANCE = 10, T_MERCURY_ALPHA = 11,
   T_MERCURY_GAMMA = 12, T_MERCURY_Z = 13, T_BDFG_BATCH = 14, T_BDFG_POINT = 15, T_PAIRING_MERGE = 16,
-  T_MERCURY_BATCH = 17, T_GKR_OUTPUTS = 25, T_GKR_OUTPUT_POINT = 26, T_GKR_BATCH = 27, T_GKR_LAYER_CLAIMS = 28,
-  T_GKR_CHILD = 29,
+  T_MERCURY_BATCH = 17, T_PUBLIC_INPUT_STREAM = 20, T_PUBLIC_OUTPUT_STREAM = 21, T_GKR_OUTPUTS = 25,
+  T_GKR_OUTPUT_POINT = 26, T_GKR_BATCH = 27, T_GKR_LAYER_CLAIMS = 28, T_GKR_CHILD = 29,
 };
 
 // The transcript's four limbs of a canonical 64-byte G1 encoding: the 128-bit
@@ -292,6 +292,18 @@ struct Transcript {
     observe(from_u64(tag));
     return sample();
   }
+  // Transcript::append_bytes (crates/transcript/src/lib.rs:324-338): the tag,
+  // the byte length, then the bytes 31 at a time as little-endian limbs, the
+  // last one zero-extended.
+  void absorb_bytes(uint64_t tag, const uint8_t* b, size_t len) {
+    observe(from_u64(tag));
+    observe(from_u64((uint64_t)len));
+    for (size_t off = 0; off < len; off += 31) {
+      uint64_t c[4] = {0, 0, 0, 0};
+      memcpy(c, b + off, len - off < 31 ? len - off : 31);
+      observe(from_canonical(c));
+    }
+  }
   // A G1 point list as one message of 4 limbs a point (g1_limbs).
   void absorb_g1(uint64_t tag, const uint8_t* pts, size_t n) {
     std::vector<F> limbs(4 * n);
@@ -325,6 +337,15 @@ struct Transcript {
     *p++ = (uint8_t)out_len;
   }
 };
+
+// io_digest (crates/transcript/src/lib.rs:464-475): the public input and
+// output byte streams in a sponge of their own, then one raw squeeze.
+inline F io_digest(const uint8_t* in, size_t in_len, const uint8_t* out, size_t out_len) {
+  Transcript t;
+  t.absorb_bytes(T_PUBLIC_INPUT_STREAM, in, in_len);
+  t.absorb_bytes(T_PUBLIC_OUTPUT_STREAM, out, out_len);
+  return t.sample();
+}
 
 // The cubic through (0,v0),(1,v1),(2,v2),(3,v3), ascending coefficients, by
 // Newton's forward differences (crates/sumcheck/src/lib.rs:294-305).

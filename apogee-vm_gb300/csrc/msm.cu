@@ -105,7 +105,7 @@ __global__ void k_fr_to_mont(Fr* v, size_t n, uint32_t* flags) {
 namespace {
 
 // [tau^i] G by double-and-add over the canonical bits of tau^i.
-__global__ void k_srs_powers(Fr tau, size_t n, Affine* dst) {
+__global__ void k_srs_powers(Fr tau, size_t n, Affine* dst, uint32_t* flags) {
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   Fr s = fe_one<FrConsts>(), base = tau;
@@ -120,13 +120,13 @@ __global__ void k_srs_powers(Fr tau, size_t n, Affine* dst) {
     acc = xyzz_dbl(acc);
     if ((sc.v[bit >> 5] >> (bit & 31)) & 1) acc = xyzz_add_affine(acc, g);
   }
-  Affine a = xyzz_to_affine(acc);
+  Affine a = xyzz_to_affine(acc, flags);
   st_fe(&dst[i].x, a.x);
   st_fe(&dst[i].y, a.y);
 }
 
 // tab[w*n + i] = 2^(c*w) * base[i].
-__global__ void k_window_table(const Affine* base, size_t n, int c, int windows, Affine* tab) {
+__global__ void k_window_table(const Affine* base, size_t n, int c, int windows, Affine* tab, uint32_t* flags) {
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   Affine cur = ld_affine(&base[i]);
@@ -136,7 +136,7 @@ __global__ void k_window_table(const Affine* base, size_t n, int c, int windows,
     if (!aff_is_inf(cur)) {
       Xyzz acc = xyzz_from_affine(cur);
       for (int j = 0; j < c; ++j) acc = xyzz_dbl(acc);
-      cur = xyzz_to_affine(acc);
+      cur = xyzz_to_affine(acc, flags);
     }
     st_fe(&tab[(size_t)w * n + i].x, cur.x);
     st_fe(&tab[(size_t)w * n + i].y, cur.y);
@@ -447,7 +447,8 @@ __global__ void k_sum_blocks(const Xyzz* in, int M, Xyzz* part) {
 
 // tsum[level*spaces + sp] holds level sums; combine by Horner in `fan`, then
 // combine spaces (windows) by Horner in 2^c, normalise and write 64 bytes.
-__global__ void k_finish(const Xyzz* tsum, int levels, int spaces, int fan_log, int c, uint32_t* out64) {
+__global__ void k_finish(const Xyzz* tsum, int levels, int spaces, int fan_log, int c, uint32_t* out64,
+                         uint32_t* flags) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   Xyzz total = xyzz_inf();
   for (int sp = spaces - 1; sp >= 0; --sp) {
@@ -459,7 +460,7 @@ __global__ void k_finish(const Xyzz* tsum, int levels, int spaces, int fan_log, 
     }
     total = xyzz_add(total, s);
   }
-  Affine a = xyzz_to_affine(total);
+  Affine a = xyzz_to_affine(total, flags);
   Fq x = fe_from_mont(a.x), y = fe_from_mont(a.y);
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
@@ -794,7 +795,7 @@ __device__ __forceinline__ Fq shfl_fq(const Fq& a, int lane) {
 constexpr int kPairThreads = 128;
 constexpr int kPairWarps = kPairThreads / 32;
 
-__device__ __forceinline__ Fq block_inverse(const Fq& v) {
+__device__ __forceinline__ Fq block_inverse(const Fq& v, uint32_t* flags) {
   __shared__ Fq tot[kPairWarps], tinv[kPairWarps];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   Fq pre = v, suf = v;
@@ -815,7 +816,7 @@ __device__ __forceinline__ Fq block_inverse(const Fq& v) {
     Fq all = tot[0];
 #pragma unroll 1
     for (int i = 1; i < kPairWarps; ++i) all = cmul(all, tot[i]);
-    Fq o = fe_inverse(all);  // every lane of warp 0 inverts the same value
+    Fq o = fe_inverse(all, flags);  // every lane of warp 0 inverts the same value
 #pragma unroll 1
     for (int i = 0; i < kPairWarps; ++i)
       if (i != lane) o = cmul(o, tot[i]);
@@ -943,50 +944,76 @@ __device__ __forceinline__ void pair_store(const uint32_t* refs, const Affine* s
   st_fe(&dst->y, y);
 }
 
-// Five resident blocks a SM (96 registers): occupancy hides the gathers and
-// the serial product chain better than a second chain a thread (measured:
-// two interleaved chains needed 210 registers and ran slower).
+// Resident blocks a SM for the two halves of a round (the backward half holds
+// a slot's two points, its running inverse and the slope: about 96 registers).
 #ifndef APG_PAIR_MIN_BLOCKS
 #define APG_PAIR_MIN_BLOCKS 5
 #endif
+// The slots of a pair round. A warp owns 32 * m consecutive output slots and
+// lane l takes slots base + 32 j + l, so the lanes' references, explicit input
+// points, running products and outputs move in coalesced rows. Both halves of
+// a round derive the same assignment from (E, T).
+struct PairLane {
+  size_t o0, steps;
+};
 
-// A warp owns 32 * m consecutive output slots and lane l takes slots
-// base + 32 j + l, so the lanes' references, explicit input points, running
-// products and outputs are read and written in coalesced rows. Forward a lane
-// multiplies up its slope denominators (the running products in pp[k * T + s]),
-// the block shares one inversion, and backward each slot takes its inverse at
-// two products and writes its sum. The early returns are uniform across the
-// grid, so every thread of a block reaches the block's inversion.
+__device__ __forceinline__ PairLane pair_lane(size_t s, size_t E, size_t T) {
+  PairLane l;
+  const size_t m = (E + T - 1) / T;
+  l.o0 = (s / 32) * 32 * m + (s & 31);
+  l.steps = l.o0 < E ? min(m, (E - l.o0 + 31) / 32) : 0;
+  return l;
+}
+
+// Forward half: lane s multiplies up the slope denominators of its slots,
+// leaving the running product before slot j in pp[j * T + s] and the lane's
+// total in tot[s]. No barrier: the lanes of a block finish independently.
+// A round 0 whose output would not fit the scratch (E > cap) sets *mode = 1,
+// and every later step takes the references instead.
 template <bool REFS>
-__global__ void __launch_bounds__(kPairThreads, APG_PAIR_MIN_BLOCKS)
-    k_pair_round(const uint32_t* refs, const Affine* src, const uint32_t* ends_in, const uint32_t* start_out,
-                 uint32_t nbins, size_t cap, uint32_t* mode, size_t T, Fq* pp, Affine* out) {
+__global__ void __launch_bounds__(kPairThreads)
+    k_pair_fwd(const uint32_t* refs, const Affine* src, const uint32_t* ends_in, const uint32_t* start_out,
+               uint32_t nbins, size_t cap, uint32_t* mode, size_t T, Fq* pp, Fq* tot) {
   const size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (*mode) return;  // uniform across the grid
+  if (s >= T || *mode) return;
   const size_t E = start_out[nbins];
-  if (E > cap) {  // uniform too
+  if (E > cap) {
     if (s == 0) *mode = 1;
     return;
   }
-  const size_t m = (E + T - 1) / T;
-  const size_t o0 = (s / 32) * 32 * m + (s & 31);
-  const size_t steps = o0 < E ? min(m, (E - o0 + 31) / 32) : 0;
-  uint32_t b = steps ? pair_bucket(start_out, nbins, o0) : 0u;
+  const PairLane L = pair_lane(s, E, T);
+  uint32_t b = L.steps ? pair_bucket(start_out, nbins, L.o0) : 0u;
   Fq acc = fe_one<FqConsts>();
-  size_t k = 0;
-  for (size_t j = 0; j < steps; ++j) {
-    const size_t o = o0 + 32 * j;
+  for (size_t j = 0; j < L.steps; ++j) {
+    const size_t o = L.o0 + 32 * j;
     b = pair_seek_up(start_out, nbins, b, o);
     bool two;
     const uint32_t i0 = pair_input(ends_in, start_out, b, o, two);
     Fq d;
     if (!two || !pair_denominator<REFS>(refs, src, i0, d)) continue;
-    st_fe(&pp[k++ * T + s], acc);
+    st_fe(&pp[j * T + s], acc);
     acc = fe_mul(acc, d);
   }
-  Fq inv = block_inverse(acc);  // every thread of the block reaches this
-  for (size_t j = steps; j-- > 0;) {
-    const size_t o = o0 + 32 * j;
+  st_fe(&tot[s], acc);
+}
+
+// Backward half: the block shares one inversion of its lanes' totals (every
+// lane reaches it first, before any slot), then each slot takes its inverse
+// at two products from the running inverse and writes its sum.
+template <bool REFS>
+__global__ void __launch_bounds__(kPairThreads, APG_PAIR_MIN_BLOCKS)
+    k_pair_bwd(const uint32_t* refs, const Affine* src, const uint32_t* ends_in, const uint32_t* start_out,
+               uint32_t nbins, const uint32_t* mode, size_t T, const Fq* pp, const Fq* tot, Affine* out,
+               uint32_t* flags) {
+  const size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (*mode) return;  // uniform across the grid: set before this launch
+  const size_t E = start_out[nbins];
+  const PairLane L = pair_lane(s, E, T);
+  Fq inv = block_inverse(s < T ? ld_fe(&tot[s]) : fe_one<FqConsts>(), flags);  // every thread of the block
+  if (s >= T || !L.steps) return;
+  uint32_t b = pair_bucket(start_out, nbins, L.o0 + 32 * (L.steps - 1));
+  for (size_t j = L.steps; j-- > 0;) {
+    const size_t o = L.o0 + 32 * j;
     b = pair_seek_down(start_out, b, o);
     bool two;
     PairSlot t;
@@ -995,7 +1022,7 @@ __global__ void __launch_bounds__(kPairThreads, APG_PAIR_MIN_BLOCKS)
       pair_store<REFS>(refs, src, t, t.num, t.num, &out[o]);
       continue;
     }
-    const Fq2 di = pmul2(inv, ld_fe(&pp[--k * T + s]), inv, t.d);  // 1/d, and the running inverse one back
+    const Fq2 di = pmul2(inv, ld_fe(&pp[j * T + s]), inv, t.d);  // 1/d, and the running inverse one back
     inv = di.b;
     const Fq lam = fe_mul(t.num, di.a);
     pair_store<REFS>(refs, src, t, lam, fe_sqr(lam), &out[o]);
@@ -1032,7 +1059,7 @@ __global__ void __launch_bounds__(kSmallK) k_reduce_small(const Xyzz* buckets, i
 // One thread per column: Horner over the reduction levels (in `fan`) and the
 // column's spaces (windows, in 2^c), then the canonical affine bytes.
 __global__ void k_finish_cols(const Xyzz* tsum, int levels, int spaces_total, int spaces_per_col, int ncols,
-                              int fan_log, int c, uint32_t* out64) {
+                              int fan_log, int c, uint32_t* out64, uint32_t* flags) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncols) return;
   Xyzz total = xyzz_inf();
@@ -1048,7 +1075,7 @@ __global__ void k_finish_cols(const Xyzz* tsum, int levels, int spaces_total, in
     }
     total = xyzz_add(total, s);
   }
-  const Affine a = xyzz_to_affine(total);
+  const Affine a = xyzz_to_affine(total, flags);
   const Fq x = fe_from_mont(a.x), y = fe_from_mont(a.y);
   uint32_t* o = out64 + 16 * (size_t)col;
 #pragma unroll
@@ -1060,7 +1087,7 @@ __global__ void k_finish_cols(const Xyzz* tsum, int levels, int spaces_total, in
 
 // out64 = the sum of m canonical affine points in64[0..m) (a stack whose
 // columns took more than one group).
-__global__ void k_add_points(const uint32_t* in64, int m, uint32_t* out64) {
+__global__ void k_add_points(const uint32_t* in64, int m, uint32_t* out64, uint32_t* flags) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   Xyzz acc = xyzz_inf();
   for (int j = 0; j < m; ++j) {
@@ -1075,7 +1102,7 @@ __global__ void k_add_points(const uint32_t* in64, int m, uint32_t* out64) {
     a.y = fe_to_mont(a.y);
     acc = xyzz_add(acc, xyzz_from_affine(a));
   }
-  const Affine r = xyzz_to_affine(acc);
+  const Affine r = xyzz_to_affine(acc, flags);
   const Fq x = fe_from_mont(r.x), y = fe_from_mont(r.y);
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
@@ -1123,7 +1150,7 @@ void generate_srs(Ctx& c, const uint8_t tau_canonical[32], size_t n, Affine* dst
   Fr tau_mont;
   APG_CUDA(cudaMemcpyAsync(&tau_mont, d_tau, 32, cudaMemcpyDeviceToHost, c.stream));
   APG_CUDA(cudaStreamSynchronize(c.stream));
-  launch(c, k_srs_powers, blocks_for<int>(n, 128), 128, 0, tau_mont, n, dst);
+  launch(c, k_srs_powers, blocks_for<int>(n, 128), 128, 0, tau_mont, n, dst, c.d_flags);
   APG_CUDA(cudaStreamSynchronize(c.stream));
 }
 
@@ -1164,7 +1191,8 @@ const SrsTable* srs_table(Ctx& c, int cbits, size_t need) {
   // Sorted references carry the table index in 31 bits.
   if ((size_t)t.windows * n >= ((size_t)1 << 31)) throw Error(APG_ERR_OUT_OF_MEMORY, "SRS window table too large");
   APG_CUDA(cudaMalloc(&t.tab, (size_t)t.windows * n * sizeof(Affine)));
-  launch(c, k_window_table, blocks_for<int>(n, 128), 128, 0, (const Affine*)c.srs, n, cbits, t.windows, t.tab);
+  launch(c, k_window_table, blocks_for<int>(n, 128), 128, 0, (const Affine*)c.srs, n, cbits, t.windows, t.tab,
+         c.d_flags);
   APG_CUDA(cudaStreamSynchronize(c.stream));
   c.tables.push_back(t);
   return &c.tables.back();
@@ -1263,8 +1291,8 @@ size_t pair_resident_threads(Ctx& c) {
   static int per_sm = 0;
   std::call_once(once, [] {
     int a = 0, b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_pair_round<true>, kPairThreads, 0) != cudaSuccess) a = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_round<false>, kPairThreads, 0) != cudaSuccess) b = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_pair_bwd<true>, kPairThreads, 0) != cudaSuccess) a = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_bwd<false>, kPairThreads, 0) != cudaSuccess) b = 1;
     per_sm = std::max(1, std::min(a, b));
   });
   return (size_t)c.sm_count * (size_t)per_sm * kPairThreads;
@@ -1356,7 +1384,8 @@ void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols
     const size_t T = pair_resident_threads(c);
     Affine* lst[2] = {c.scratch[S_PAIR_A].as<Affine>(cap[0]),
                       c.scratch[S_PAIR_B].as<Affine>(kPairRounds > 1 ? cap[1] : 1)};
-    Fq* pp = c.scratch[S_PAIR_PP].as<Fq>((cap[0] + T - 1) / T * T);
+    Fq* pp = c.scratch[S_PAIR_PP].as<Fq>((cap[0] + T - 1) / T * T + T);
+    Fq* tot = pp + (cap[0] + T - 1) / T * T;
     uint32_t* cnt = c.scratch[S_PAIR_CNT].as<uint32_t>((size_t)kPairRounds * (nbins + 1) + 2);
     uint32_t* mode = cnt + (size_t)kPairRounds * (nbins + 1);
     APG_CUDA(cudaMemsetAsync(mode, 0, 2 * sizeof(uint32_t), c.stream));
@@ -1370,13 +1399,19 @@ void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols
       launch(c, k_scan_local, sblocks, kScanBlock, 0, st, scan_n, blk);
       launch(c, k_scan_blocks, 1, kScanBlock, 0, blk, (int)sblocks);
       launch(c, k_scan_add, blocks_for<int>(scan_n, 256), 256, 0, st, scan_n, (const uint32_t*)blk, mode + 1);
-      if (r == 0)
-        launch(c, k_pair_round<true>, pblocks, kPairThreads, 0, (const uint32_t*)sorted, src, ends_in,
-               (const uint32_t*)st, (uint32_t)nbins, cap[0], mode, T, pp, lst[0]);
-      else
-        launch(c, k_pair_round<false>, pblocks, kPairThreads, 0, (const uint32_t*)nullptr,
-               (const Affine*)lst[(r - 1) & 1], ends_in, (const uint32_t*)st, (uint32_t)nbins, cap[r], mode, T, pp,
-               lst[r & 1]);
+      const uint32_t* rr = r == 0 ? (const uint32_t*)sorted : (const uint32_t*)nullptr;
+      const Affine* in = r == 0 ? src : lst[(r - 1) & 1];
+      if (r == 0) {
+        launch(c, k_pair_fwd<true>, pblocks, kPairThreads, 0, rr, in, ends_in, (const uint32_t*)st, (uint32_t)nbins,
+               cap[0], mode, T, pp, tot);
+        launch(c, k_pair_bwd<true>, pblocks, kPairThreads, 0, rr, in, ends_in, (const uint32_t*)st, (uint32_t)nbins,
+               (const uint32_t*)mode, T, (const Fq*)pp, (const Fq*)tot, lst[0], c.d_flags);
+      } else {
+        launch(c, k_pair_fwd<false>, pblocks, kPairThreads, 0, rr, in, ends_in, (const uint32_t*)st, (uint32_t)nbins,
+               cap[r], mode, T, pp, tot);
+        launch(c, k_pair_bwd<false>, pblocks, kPairThreads, 0, rr, in, ends_in, (const uint32_t*)st, (uint32_t)nbins,
+               (const uint32_t*)mode, T, (const Fq*)pp, (const Fq*)tot, lst[r & 1], c.d_flags);
+      }
       ends_in = st + 1;
     }
     pair_mode = mode;
@@ -1422,7 +1457,7 @@ void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols
     M = G;
   }
   launch(c, k_finish_cols, blocks_for<int>(nout, 32), 32, 0, (const Xyzz*)tsum, levels, S, spaces_per_col, nout,
-         fan_log, p.c, (uint32_t*)d_out);
+         fan_log, p.c, (uint32_t*)d_out, c.d_flags);
   c.timer_end(APG_TIMER_MSM_TOTAL, t_total);
 }
 
@@ -1472,7 +1507,7 @@ void msm_multi(Ctx& c, const Affine* bases, const SrsTable* table, const void* c
   if (o.stack) {
     if (ngroups == 0) APG_CUDA(cudaMemsetAsync(d_out, 0, 64, c.stream));
     else if (ngroups == 1) APG_CUDA(cudaMemcpyAsync(d_out, partial, 64, cudaMemcpyDeviceToDevice, c.stream));
-    else launch(c, k_add_points, 1, 32, 0, (const uint32_t*)partial, (int)ngroups, (uint32_t*)d_out);
+    else launch(c, k_add_points, 1, 32, 0, (const uint32_t*)partial, (int)ngroups, (uint32_t*)d_out, c.d_flags);
   }
 }
 
@@ -1501,9 +1536,10 @@ void msm_device(Ctx& c, const Affine* bases, const SrsTable* table, const void* 
 // afford the device-wide synchronisation cudaMalloc and cudaFree imply. For
 // them this variant of the MSM runs the same kernels with all of its scratch
 // in one fixed array that lives in the module's global memory, reserved when
-// the library is loaded and held by every GPU that loads it until the
-// process exits. It calls no cudaMalloc, no cudaFree and no allocating
-// library routine.
+// the module is loaded on a device (with CUDA's lazy loading: the first call,
+// or the first launch of any kernel of this file, on that device -- make it
+// before the device's memory is promised) and held until the process exits.
+// It calls no cudaMalloc, no cudaFree and no allocating library routine.
 //
 // Limit: at most kNoAllocMaxPoints bases. The plan is fixed: 9-bit signed
 // windows (29 of them) with one bucket set per window, 16 entries per
@@ -1559,15 +1595,19 @@ namespace {
 std::mutex g_noalloc_mu;
 void* g_noalloc_addr[256] = {nullptr};
 
-// The array's device address on the current device, looked up on the first
-// call made with that device current.
+// The array's device address, looked up once per device, on the first call
+// made with that device current (the set-up step; with CUDA's lazy module
+// loading that lookup, or the first launch of any other kernel of this file
+// on the device, loads the module, which is when the array is reserved). The
+// address belongs to the device's primary context, the one the CUDA runtime
+// uses: the entry point assumes no cudaDeviceReset while the library is
+// loaded and no other current context.
 int noalloc_scratch(int device, uint8_t** out) {
   if (device < 0 || device >= 256) return APG_ERR_NO_DEVICE;
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   if (!g_noalloc_addr[device]) {
     void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) return APG_ERR_CUDA;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return APG_ERR_CUDA;
     g_noalloc_addr[device] = p;
   }
   *out = (uint8_t*)g_noalloc_addr[device];
@@ -1596,9 +1636,6 @@ int msm_noalloc(const void* d_bases, const void* d_scalars, size_t n, void* d_ou
     APG_NA(cudaStreamSynchronize(st));
     return APG_OK;
   }
-  int sms = 0;
-  APG_NA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-  (void)sms;
   uint32_t* flags = (uint32_t*)(s + kOffFlags);
   uint32_t* total = (uint32_t*)(s + kOffTotal);
   Affine* bases = (Affine*)(s + kOffBases);
@@ -1666,7 +1703,7 @@ int msm_noalloc(const void* d_bases, const void* d_scalars, size_t n, void* d_ou
   }
   int fan_log = 0;
   while ((1 << fan_log) < kLevelFan) ++fan_log;
-  k_finish<<<1, 32, 0, st>>>((const Xyzz*)tsum, kNoAllocLevels, spaces, fan_log, kNoAllocC, (uint32_t*)d_out);
+  k_finish<<<1, 32, 0, st>>>((const Xyzz*)tsum, kNoAllocLevels, spaces, fan_log, kNoAllocC, (uint32_t*)d_out, flags);
   APG_NA_LAUNCH();
   uint32_t f = 0;
   APG_NA(cudaMemcpyAsync(&f, flags, 4, cudaMemcpyDeviceToHost, st));

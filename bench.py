@@ -306,14 +306,19 @@ def run_msm_only(args):
     for _ in range(args.warmup):
         ctx.commit_batch_device(ptrs, args.log2n)
     torch.cuda.synchronize()
+    ctx.set_timing(True)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         ctx.commit_batch_device(ptrs, args.log2n)
     torch.cuda.synchronize()
     dt = (time.perf_counter() - t0) / args.steps
+    acc_ms, acc_n = ctx.timer(A.Context.TIMER_MSM_ACCUMULATE)
+    tot_ms, tot_n = ctx.timer(A.Context.TIMER_MSM_TOTAL)
+    ctx.set_timing(False)
     print(json.dumps({"msm_only": True, "scalars": args.scalars, "log2n": args.log2n, "cols": args.cols,
                       "window_bits": tuned[args.log2n], "ms_per_step": dt * 1e3,
-                      "points_per_s": args.cols * n / dt}), flush=True)
+                      "points_per_s": args.cols * n / dt, "accumulate_ms_per_group": acc_ms / max(acc_n, 1),
+                      "msm_ms_per_group": tot_ms / max(tot_n, 1), "groups": tot_n}), flush=True)
     ctx.close()
     return 0
 

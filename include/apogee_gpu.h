@@ -127,15 +127,20 @@ int apg_msm_small_u32(apg_ctx* ctx, const uint8_t* bases, size_t n_bases, const 
  * latency-critical pipeline that cannot take the device-wide synchronisation
  * of cudaMalloc/cudaFree. It computes exactly what apg_msm does, with every
  * buffer carved from one fixed array in the library's device global memory
- * (about 8.5 MB, reserved on every GPU that loads the library, until exit).
+ * (about 8.5 MB on every GPU the library's MSM module is loaded on, until
+ * exit; under CUDA's lazy module loading the module loads at the first call
+ * on a device, or at the first launch of another MSM kernel there, so make
+ * that first call before the device's memory is promised elsewhere).
  *   d_bases:   n canonical 64-byte points in device memory (all-zero =
  *              infinity), d_scalars: n Fr in memory in device memory,
  *   d_out:     64 bytes of device memory for the canonical result,
  *   stream:    the cudaStream_t to run on (0 = legacy default stream), on the
  *              current device. The call returns when the result is written.
  * At most APG_MSM_NOALLOC_MAX_POINTS bases (APG_ERR_NOALLOC_TOO_LARGE above).
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture. All calls on a device share the one
+ * The first call on a device looks up the array's device address (and may
+ * load the module); make that first call before any stream capture. The
+ * address is the device's primary context's (the CUDA runtime's): no
+ * cudaDeviceReset while the library is loaded. All calls on a device share the one
  * array (each clears what must start at zero), so calls that overlap on the
  * GPU race: serialise them, e.g. on one stream. */
 #define APG_MSM_NOALLOC_MAX_POINTS 4096
@@ -359,6 +364,20 @@ void apg_transcript_init(uint8_t snapshot[226]);
 int apg_transcript_append_scalars(uint8_t snapshot[226], uint64_t tag, const uint8_t* xs, size_t n);
 /* Transcript::challenge_scalar(tag) -> out (Fr in memory). */
 int apg_transcript_challenge(uint8_t snapshot[226], uint64_t tag, uint8_t out[32]);
+/* Transcript::observe (lib.rs:241-251): one Fr (in memory) into the rate. */
+int apg_transcript_observe(uint8_t snapshot[226], const uint8_t x[32]);
+/* Transcript::sample (lib.rs:253-263): one raw squeeze -> out (Fr in memory). */
+int apg_transcript_sample(uint8_t snapshot[226], uint8_t out[32]);
+/* Transcript::append_bytes (lib.rs:324-338): tag, byte length, then 31-byte
+ * little-endian limbs. */
+int apg_transcript_append_bytes(uint8_t snapshot[226], uint64_t tag, const uint8_t* bytes, size_t len);
+/* transcript::io_digest (lib.rs:464-475): the public I/O digest -> out (Fr in
+ * memory). */
+int apg_io_digest(const uint8_t* input, size_t input_len, const uint8_t* output, size_t output_len,
+                  uint8_t out[32]);
+/* poseidon2_permute (lib.rs:121-146) over three canonical little-endian Fr,
+ * in place; APG_ERR_NONCANONICAL if one is >= p. */
+int apg_poseidon2_permute(uint8_t state[96]);
 
 /* ---- utilities ---------------------------------------------------------- */
 

@@ -5,9 +5,9 @@ postcard wire form) byte for byte into tests/golden/artifacts/.
 
 The reference pins its hot path with text fixtures generated against
 arkworks (ark-bn254 0.6) and Plonky3's Poseidon2; this script copies the
-lines the tests use into tests/golden/, trimming the two very large corpora
-(Fq and G1) to a deterministic prefix so the fixtures stay small. Run it from
-the repository root in a checkout that has the reference tree:
+data lines the tests use into tests/golden/ (the Fq corpus keeps only its
+base-field record kinds). Run it from the repository root, naming the root
+of a checkout of the reference tree:
 
     python tests/golden/make_golden.py /path/to/apogee-vm
 
@@ -20,12 +20,14 @@ import sys
 SOURCES = {
     # name: (path inside the reference, line filter, max data lines or None)
     "fr_kats.txt": ("crates/field/tests/vectors/fr_kats.txt", None, None),
-    "fq_kats.txt": ("crates/curve/tests/vectors/fq_kats.txt", ("fq_ops", "fq_pow", "fq_bytes", "fq_u64"), 400),
-    "g1_kats.txt": ("crates/curve/tests/vectors/g1_kats.txt", None, 120),
+    "fq_kats.txt": ("crates/curve/tests/vectors/fq_kats.txt", ("fq_ops", "fq_pow", "fq_bytes", "fq_u64"), None),
+    "g1_kats.txt": ("crates/curve/tests/vectors/g1_kats.txt", None, None),
     "msm_kats.txt": ("crates/curve/tests/vectors/msm_kats.txt", None, None),
     "poly_kats.txt": ("crates/poly/tests/vectors/poly_kats.txt", None, None),
     "poseidon2_perm.txt": ("crates/transcript/tests/vectors/poseidon2_perm.txt", None, None),
     "transcript_cases.txt": ("crates/transcript/tests/vectors/transcript_cases.txt", None, None),
+    "io_digest.txt": ("crates/transcript/tests/vectors/io_digest.txt", None, None),
+    "evaluate_diff.txt": ("crates/poly/tests/vectors/evaluate_diff.txt", None, None),
     "g1_absorb_kats.txt": ("crates/pcs/tests/vectors/g1_absorb_kats.txt", None, None),
     "mercury_proof.txt": ("crates/pcs/tests/vectors/mercury_proof.txt", None, None),
     "mercury_batch.txt": ("crates/pcs/tests/vectors/mercury_batch.txt", None, None),
@@ -79,4 +81,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <root of the reference checkout>")
+    main(sys.argv[1])

@@ -4,7 +4,7 @@
   one commit_batch_device call (the library splits them into four groups of
   four over its two lanes, the call the benchmark times), with the window
   tables the autotuner picks at 2^22 (18 bits) and the opening width (20
-  bits); and 2^17-2^20 columns at 12- and 16-bit tables. Every commitment is
+  bits); and 2^18- and 2^20-point columns at 12- and 16-bit tables. Every commitment is
   held to the known-tau identity cm = [f(tau)]G, f(tau) by the oracle's Horner.
 * Config 1 at its full size: a 2^16 commit, the witness digest and the
   16-round Product zerocheck against the oracle.
@@ -87,7 +87,7 @@ def test_mid_sizes_commit_known_tau(ctx, cbits):
     host, dev = device_mixed(ctx, 1 << 20, [77 + cbits])
     chosen = ctx.msm_autotune(dev[0].data_ptr(), 1 << 20, 17, 20, cands=(cbits,))
     assert chosen == {k: cbits for k in range(17, 21)}
-    for log2n in (17, 18, 19, 20):
+    for log2n in (18, 20):  # commits take even variable counts (Mercury)
         n = 1 << log2n
         cols, devs = device_mixed(ctx, n, [1000 * log2n + cbits + j for j in range(5)])
         cms = ctx.commit_batch_device([t.data_ptr() for t in devs], log2n)

@@ -443,3 +443,51 @@ def test_stacked_refusal_order(oracle):
     long = [stacks[0] + [stacks[1][0]], stacks[1]]
     assert run(long, [2] * 7, cms, u, r) == 16
     assert run(stacks, [2] * 6, cms, u, r, srs_n=8) == 13
+
+
+def test_evaluate_diff(oracle):
+    """crates/poly/tests/vectors/evaluate_diff.txt: 100 evaluate cases against
+    ark-poly. Case i has i % 13 variables and backing BACKINGS[i % 5]; its
+    table is drawn from splitmix64 seeded 20260908 + i (u1/u8/u16/u32 take
+    the low bits of one draw, fr four draws read mod p) and pinned by a
+    SHA-256 over the lifted entries before the oracle evaluates it."""
+    import hashlib
+
+    cases, points, results = {}, {}, {}
+    for line in O.golden_lines("evaluate_diff.txt"):
+        f = line.split()
+        if f[0] == "case":
+            cases[int(f[1])] = (f[2], int(f[3]), f[4])
+        elif f[0] == "point":
+            points.setdefault(int(f[1]), {})[int(f[2])] = O.fe_int(hexb(f[3]))
+        elif f[0] == "result":
+            results[int(f[1])] = f[2]
+    assert len(cases) == 100
+    masks = {"u1": 1, "u8": 0xFF, "u16": 0xFFFF, "u32": 0xFFFFFFFF}
+    for i, (backing, nv, digest) in cases.items():
+        rng = O.Rng(20260908 + i)
+        if backing == "fr":
+            table = [O.fe_int(rng.next_le32()) % O.P_R for _ in range(1 << nv)]
+        else:
+            table = [rng.next_u64() & masks[backing] for _ in range(1 << nv)]
+        raw = b"".join(O.fe(x) for x in table)
+        assert hashlib.sha256(raw).hexdigest() == digest, f"case {i}: table"
+        pt = [points[i][j] for j in range(nv)] if nv else []
+        out = buf(32)
+        assert oracle.oracle_evaluate(raw, ctypes.c_size_t(nv), b"".join(O.fe(x) for x in pt), out) == 0
+        assert out.raw.hex() == results[i], f"case {i}"
+
+
+def test_io_digest(oracle):
+    """crates/transcript/tests/vectors/io_digest.txt through the oracle's
+    duplex: append_bytes of each stream under its tag, then one squeeze."""
+    n = 0
+    for line in O.golden_lines("io_digest.txt"):
+        f = line.split()
+        snap = O.new_snapshot()
+        for tag, stream in ((O.TAG_NAMES["PUBLIC_INPUT_STREAM"], f[2]), (O.TAG_NAMES["PUBLIC_OUTPUT_STREAM"], f[3])):
+            data = b"" if stream == "-" else hexb(stream)
+            O.transcript_op(snap, 3, tag, data, len(data))
+        assert O.transcript_op(snap, 1).hex() == f[4], f[1]
+        n += 1
+    assert n >= 10
