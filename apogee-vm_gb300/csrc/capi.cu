@@ -1,6 +1,8 @@
 // The C ABI boundary (include/apogee_gpu.h): argument checks in the
 // reference's refusal order, context locking, and the mapping of every
 // failure to an apg_status. No exception crosses this file's functions.
+#include <chrono>
+
 #include "common.cuh"
 #include "sumcheck.cuh"
 
@@ -101,6 +103,13 @@ int apg_ctx_create(int device, apg_ctx** out) {
     APG_CUDA(cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking));
     APG_CUDA(cudaMalloc(&ctx->c.d_flags, 4));
     APG_CUDA(cudaMemset(ctx->c.d_flags, 0, 4));
+    // Memory freed to the device's stream-ordered pool (GKR layer values,
+    // staged columns) stays in the pool for the next request instead of
+    // going back to the driver at every synchronisation.
+    cudaMemPool_t pool;
+    APG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t keep = UINT64_MAX;
+    APG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
   } catch (const Error& e) {
     delete ctx;
     return e.status;
@@ -408,6 +417,8 @@ static Ctx& lane_of(Ctx& c) {
   L.srs_n = c.srs_n;
   L.srs_owned = false;
   memcpy(L.tuned_c, c.tuned_c, sizeof(c.tuned_c));
+  L.timers.on = c.timers.on;
+  L.timers.kernels = c.timers.kernels;
   return L;
 }
 
@@ -483,6 +494,15 @@ static int commit_batch_lanes(Ctx& c, const void* const* cols, bool host, size_t
   c.check_flags();
   c.launches += L.launches;
   L.launches = 0;
+  if (L.timers.on) {  // the lane's timers count as the context's
+    L.timers.flush();
+    for (int i = 0; i < Timers::N; ++i) {
+      c.timers.ms[i] += L.timers.ms[i];
+      c.timers.count[i] += L.timers.count[i];
+      L.timers.ms[i] = 0;
+      L.timers.count[i] = 0;
+    }
+  }
   return APG_OK;
 }
 
@@ -673,6 +693,18 @@ int apg_mercury_batch_open_stacked_device(apg_ctx* ctx, const void* const* d_col
   });
 }
 
+// The device bytes a context holds: its and its lane's scratch, the window
+// tables and SRS it owns.
+static size_t ctx_bytes(const Ctx& c) {
+  size_t b = 0;
+  for (const auto& d : c.scratch) b += d.cap;
+  for (const auto& t : c.tables)
+    if (t.owned) b += (size_t)t.windows * t.n * sizeof(Affine);
+  if (c.srs && c.srs_owned) b += c.srs_n * sizeof(Affine);
+  if (c.lane) b += ctx_bytes(*c.lane);
+  return b;
+}
+
 struct apg_gkr_values {
   GkrValues* v;
   apg_ctx* ctx;
@@ -829,6 +861,7 @@ int apg_ctx_set_timing(apg_ctx* ctx, int on) {
   return guarded(ctx, [&](Ctx& c) {
     c.timers.flush();
     c.timers.on = on != 0;
+    c.timers.kernels = on == 2;
     for (int i = 0; i < Timers::N; ++i) {
       c.timers.ms[i] = 0;
       c.timers.count[i] = 0;
@@ -865,4 +898,118 @@ int apg_commit_batch(apg_ctx* ctx, const uint8_t* const* cols, size_t k, size_t 
   return guarded(ctx, [&](Ctx& c) { return commit_batch_lanes(c, (const void* const*)cols, true, k, num_vars, out); });
 }
 
+
+// One shard: commit, shard transcript, GKR forward and proof, batched opening
+// at the base point (crates/prover/src/lib.rs:798-1102, the hot-path slice).
+// Host columns are copied once into a stream-ordered device buffer that every
+// phase reads; the transcript stays on the host between phases.
+static int prove_shard_common(Ctx& c, const apg_shard* sh, apg_shard_proof* out) {
+  using Clock = std::chrono::steady_clock;
+  if (!sh || !out || !sh->circuit || !sh->cols || !sh->statement_digest || !out->cms || !out->gkr_proof ||
+      !out->point || !out->values)
+    return APG_ERR_INVALID_ARGUMENT;
+  const size_t k = sh->n_cols, nv = sh->num_vars;
+  if (k == 0) return APG_ERR_EMPTY_BATCH;
+  if (!mercury_num_vars_ok(nv) || nv > 30) return APG_ERR_UNSUPPORTED_NUM_VARS;
+  const size_t n = (size_t)1 << nv;
+  host::F digest;
+  memcpy(digest.w, sh->statement_digest, 32);
+  if (!host::below_p(digest.w)) return APG_ERR_NONCANONICAL;
+  for (size_t j = 0; j < k; ++j)
+    if (!sh->cols[j]) return APG_ERR_INVALID_ARGUMENT;
+  std::vector<const void*> d_cols(sh->cols, sh->cols + k);
+  Fr* staged = nullptr;
+  auto t0 = Clock::now();
+  if (!sh->cols_on_device) {
+    APG_CUDA(cudaMallocAsync((void**)&staged, 32 * n * k, c.stream));
+    for (size_t j = 0; j < k; ++j) {
+      APG_CUDA(cudaMemcpyAsync(staged + j * n, sh->cols[j], 32 * n, cudaMemcpyHostToDevice, c.stream));
+      d_cols[j] = staged + j * n;
+    }
+  }
+  struct Staged {
+    Ctx& c;
+    Fr* p;
+    ~Staged() {
+      if (p) cudaFreeAsync(p, c.stream);
+    }
+  } guard{c, staged};
+  auto ms_since = [](Clock::time_point a) {
+    return std::chrono::duration<double, std::milli>(Clock::now() - a).count();
+  };
+  int st = commit_batch_lanes(c, d_cols.data(), false, k, nv, out->cms);
+  if (st) return st;
+  out->phase_ms[0] = ms_since(t0);
+
+  // verifier_core::shard_transcript (statement.rs:548-572).
+  host::Transcript tr;
+  const host::F seed[3] = {digest, host::from_u64(sh->family), host::from_u64(sh->index)};
+  tr.absorb(39, seed, 3);  // SHARD_SEED
+  const host::F window[2] = {host::from_u64(sh->ts_lo), host::from_u64(sh->ts_hi)};
+  tr.absorb(40, window, 2);  // SHARD_TS_WINDOW
+  tr.absorb_g1(host::T_COMMITMENT, out->cms, k);
+  const host::F g = tr.challenge(33), beta = tr.challenge(33);  // LOOKUP_CHALLENGE
+  const uint32_t slots[2] = {0, 1};
+  uint8_t slot_values[64];
+  memcpy(slot_values, g.w, 32);
+  memcpy(slot_values + 32, beta.w, 32);
+  uint8_t snap[226];
+  tr.save(snap);
+
+  auto t1 = Clock::now();
+  std::unique_ptr<GkrValues, void (*)(GkrValues*)> V(
+      gkr_forward_impl(c, sh->circuit, sh->circuit_len, d_cols.data(), nullptr, true, slots, slot_values, 2),
+      gkr_values_free);
+  APG_CUDA(cudaStreamSynchronize(c.stream));
+  out->phase_ms[1] = ms_since(t1);
+  auto t2 = Clock::now();
+  st = gkr_prove_impl(c, sh->circuit, sh->circuit_len, V.get(), slots, slot_values, 2, snap, out->gkr_proof,
+                      out->gkr_cap, &out->gkr_len, out->point);
+  if (st) return st;
+  V.reset();
+  out->phase_ms[2] = ms_since(t2);
+
+  auto t3 = Clock::now();
+  st = batch_open_common(c, d_cols.data(), true, k, nv, out->cms, out->point, nv, snap, out->values, out->opening);
+  if (st) return st;
+  out->phase_ms[3] = ms_since(t3);
+  memcpy(out->transcript, snap, 226);
+  return APG_OK;
+}
+
+size_t apg_shard_device_bytes(const apg_shard* sh) {
+  if (!sh || !sh->circuit || sh->num_vars > 40) return 0;
+  try {
+    const size_t n = (size_t)1 << sh->num_vars, k = sh->n_cols;
+    size_t b = sh->cols_on_device ? 0 : 32 * n * k;  // the staged columns
+    b += gkr_device_bytes_impl(sh->circuit, sh->circuit_len);
+    // The commits' two lanes: a group of ceil(k / 4) columns sorts up to 15
+    // windows a point (4-byte references), and the affine pair rounds hold
+    // two point lists and the running products at about half and a quarter
+    // of that (capped as msm.cu caps them), plus buckets and levels.
+    const size_t g = (k + 3) / 4;
+    const size_t E = std::min<size_t>((size_t)15 * n * g, (size_t)1 << 28);
+    const size_t cap = (size_t)48 << 20;
+    size_t lane = 4 * E + ((size_t)96 << 20);
+    if (E >= ((size_t)1 << 21))
+      lane += 64 * std::min(E / 2, cap) + 64 * std::min(E / 4, cap) + 32 * std::min(E / 2, cap);
+    b += 2 * lane;
+    b += 12 * 32 * n;  // the opening's O(n) tables
+    return b;
+  } catch (...) {
+    return 0;
+  }
+}
+
+int apg_ctx_device(apg_ctx* ctx) { return ctx ? ctx->c.device : -1; }
+
+size_t apg_ctx_device_bytes(apg_ctx* ctx) {
+  if (!ctx) return 0;
+  std::lock_guard<std::mutex> lock(ctx->c.mu);
+  return ctx_bytes(ctx->c);
+}
+
+int apg_prove_shard(apg_ctx* ctx, const apg_shard* shard, apg_shard_proof* out) {
+  return guarded(ctx, [&](Ctx& c) { return prove_shard_common(c, shard, out); });
+}
 }  // extern "C"

@@ -88,6 +88,7 @@ enum ScratchSlot {
 struct Timers {
   static constexpr int N = 8;
   bool on = false;
+  bool kernels = false;  // also bracket every launch (APG_TIMER_KERNELS)
   std::vector<cudaEvent_t> pool;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
   double ms[N] = {0};
@@ -180,11 +181,25 @@ struct Ctx {
 };
 
 // Launch a kernel on the context's stream, check the launch and count it.
+// With kernel timing on, every launch is bracketed by a pair of events, so
+// the sum of kernel durations (the device's busy time on this stream) can be
+// set against the wall clock.
 template <class... KArgs, class... Args>
 inline void launch(Ctx& c, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, Args... args) {
+  cudaEvent_t e0 = nullptr;
+  if (c.timers.on && c.timers.kernels) {
+    if (c.timers.pending.size() > 4096) c.timers.flush();
+    e0 = c.timers.get();
+    APG_CUDA(cudaEventRecord(e0, c.stream));
+  }
   kernel<<<grid, block, smem, c.stream>>>(args...);
   APG_CUDA(cudaGetLastError());
   ++c.launches;
+  if (e0) {
+    cudaEvent_t e1 = c.timers.get();
+    APG_CUDA(cudaEventRecord(e1, c.stream));
+    c.timers.pending.push_back({APG_TIMER_KERNELS, {e0, e1}});
+  }
 }
 
 // ---------------------------------------------------------------------------

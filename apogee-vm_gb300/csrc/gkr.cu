@@ -261,6 +261,10 @@ __global__ void __launch_bounds__(kFwdThreads) k_forward(DevProgram P, int w, in
 // at base_off bytes: the forward pass and gate list 0's first sumcheck rounds
 // read narrow columns through the lift. What needs the base as Fr tables
 // (reading it back, a halving list over it) lifts it once, on demand.
+// The layers come from the stream-ordered pool on the context's stream
+// (cudaMallocAsync / cudaFreeAsync): unlike cudaMalloc and cudaFree, they do
+// not synchronise the device, so contexts proving shards side by side do not
+// stall each other at every forward pass.
 struct GkrValues {
   Ctx* ctx = nullptr;
   Circuit circuit;
@@ -270,9 +274,10 @@ struct GkrValues {
   bool base_narrow = false;
   Fr* lifted = nullptr;
   ~GkrValues() {
+    cudaStream_t st = ctx ? ctx->stream : nullptr;
     for (auto p : layers)
-      if (p) cudaFree(p);
-    if (lifted) cudaFree(lifted);
+      if (p) cudaFreeAsync(p, st);
+    if (lifted) cudaFreeAsync(lifted, st);
   }
   const void* base_raw(size_t x) const { return reinterpret_cast<const uint8_t*>(layers[0]) + base_off[x]; }
   const Fr* col(size_t k, size_t x) {
@@ -280,7 +285,7 @@ struct GkrValues {
     if (k > 0) return layers[k] + x * rows;
     if (!base_narrow) return reinterpret_cast<const Fr*>(base_raw(x));
     if (!lifted) {
-      APG_CUDA(cudaMalloc(&lifted, 32 * rows * circuit.n_committed));
+      APG_CUDA(cudaMallocAsync((void**)&lifted, 32 * rows * circuit.n_committed, ctx->stream));
       for (size_t j = 0; j < circuit.n_committed; ++j)
         lift_column(*ctx, base_raw(j), base_bits[j], rows, lifted + j * rows);
     }
@@ -324,7 +329,7 @@ GkrValues* gkr_forward_impl(Ctx& c, const uint8_t* blob, size_t blob_len, const 
     V->base_off[x] = total;
     total += (narrow_bytes(V->base_bits[x], n0) + 255) / 256 * 256;
   }
-  APG_CUDA(cudaMalloc(&V->layers[0], std::max<size_t>(total, 256)));
+  APG_CUDA(cudaMallocAsync((void**)&V->layers[0], std::max<size_t>(total, 256), c.stream));
   for (size_t x = 0; x < C.n_committed; ++x)
     APG_CUDA(cudaMemcpyAsync(reinterpret_cast<uint8_t*>(V->layers[0]) + V->base_off[x], base[x],
                              narrow_bytes(V->base_bits[x], n0),
@@ -338,7 +343,7 @@ GkrValues* gkr_forward_impl(Ctx& c, const uint8_t* blob, size_t blob_len, const 
   for (size_t k = 0; k < C.layers.size(); ++k) {
     const CLayer& L = C.layers[k];
     const size_t rows = (size_t)1 << L.num_vars;
-    APG_CUDA(cudaMalloc(&V->layers[k + 1], 32 * rows * std::max<uint32_t>(L.width, 1)));
+    APG_CUDA(cudaMallocAsync((void**)&V->layers[k + 1], 32 * rows * std::max<uint32_t>(L.width, 1), c.stream));
     HostProgram hp = layer_program(C, k, ch, false, {});
     DevProgram P;
     upload_program(c, hp, P, 0);
@@ -498,6 +503,23 @@ int gkr_prove_impl(Ctx& c, const uint8_t* blob, size_t blob_len, GkrValues* V, c
 void gkr_values_free(GkrValues* v) { delete v; }
 
 size_t gkr_proof_len_impl(const uint8_t* blob, size_t len) { return 32 * gkr_proof_elems(parse_circuit_blob(blob, len)); }
+
+// Device bytes a forward pass and proof of this circuit hold at once: the
+// base as Fr, every layer, and the largest layer sumcheck's two level
+// buffers (its tables, eq and the virtual tables at half and a quarter of
+// the bound variables' rows).
+size_t gkr_device_bytes_impl(const uint8_t* blob, size_t len) {
+  const Circuit C = parse_circuit_blob(blob, len);
+  size_t b = 32 * ((size_t)1 << C.trace_vars) * C.n_committed;
+  size_t worst = 0;
+  for (size_t k = 0; k < C.layers.size(); ++k) {
+    const CLayer& L = C.layers[k];
+    b += 32 * ((size_t)1 << L.num_vars) * std::max<uint32_t>(L.width, 1);
+    const size_t tables = (L.halving ? 2 : 1) * (size_t)C.width(k) + (L.halving ? 0 : C.virtuals.size()) + 1;
+    worst = std::max(worst, tables * 24 * ((size_t)1 << L.num_vars));
+  }
+  return b + worst;
+}
 
 int gkr_values_read_impl(GkrValues* v, size_t layer, size_t col, uint8_t* out) {
   if (!v || !out || layer > v->circuit.layers.size() || col >= v->circuit.width(layer)) return APG_ERR_INVALID_ARGUMENT;

@@ -14,6 +14,7 @@
 // level-(r-1) tables once, writes the level-r tables once and never re-reads
 // them.
 #include <algorithm>
+#include <chrono>
 #include <map>
 #include <tuple>
 
@@ -523,6 +524,7 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
     c.timer_end(APG_TIMER_SUMCHECK_ROUND, t0);
     APG_CUDA(cudaMemcpyAsync(sums, d_out, 128, cudaMemcpyDeviceToHost, c.stream));
     APG_CUDA(cudaStreamSynchronize(c.stream));
+    const auto host0 = std::chrono::steady_clock::now();
     F q[4] = {sums[0], sums[1], sums[2], host::fzero()};
     const F one_m_r = host::fsub(host::fone(), rr);
     if (!need1) {
@@ -546,6 +548,11 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
     chal = tr.challenge(host::T_SUMCHECK_CHALLENGE);
     rounds.push_back(g);
     point.push_back(chal);
+    if (c.timers.on) {  // the host's share of a round: interpolation and the transcript step
+      c.timers.ms[APG_TIMER_HOST_ROUND] +=
+          std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host0).count();
+      c.timers.count[APG_TIMER_HOST_ROUND] += 1;
+    }
   }
   // The last fold: every table bound to the full point.
   Fr* d_fin = c.scratch[S_TMP7].as<Fr>(nt);

@@ -98,6 +98,7 @@ void gkr_values_free(GkrValues* v);
 int gkr_values_read_impl(GkrValues* v, size_t layer, size_t col, uint8_t* out);
 size_t gkr_values_len(GkrValues* v, size_t layer);
 size_t gkr_proof_len_impl(const uint8_t* blob, size_t len);
+size_t gkr_device_bytes_impl(const uint8_t* blob, size_t len);
 
 int mercury_open_impl(Ctx& c, const Fr* d_f, size_t nv, const uint8_t cm[64], const std::vector<host::F>& u,
                       host::Transcript& tr, host::F& v_out, uint8_t proof_out[704]);

@@ -55,6 +55,8 @@ enum apg_status {
   APG_ERR_NO_SRS = 23,                /* no SRS resident on the context */
   APG_ERR_INTERNAL = 24,              /* a device invariant failed */
   APG_ERR_NOALLOC_TOO_LARGE = 25,     /* apg_msm_noalloc: more bases than its fixed scratch holds */
+  APG_PENDING = 26,                   /* apg_poll: the request is queued or running */
+  APG_ERR_UNKNOWN_TICKET = 27,        /* apg_poll / apg_wait: no such request */
   APG_ERR_CUDA = 100,                 /* a CUDA call failed */
   APG_ERR_OUT_OF_MEMORY = 101,        /* device allocation refused */
   APG_ERR_NO_DEVICE = 103             /* no usable CUDA device */
@@ -73,6 +75,8 @@ const char* apg_last_error(apg_ctx* ctx);
 /* The context's CUDA stream (a cudaStream_t), for callers that time or
  * order work against it. */
 void* apg_ctx_stream(apg_ctx* ctx);
+/* The CUDA device ordinal of the context (-1 for null). */
+int apg_ctx_device(apg_ctx* ctx);
 /* Block until all work queued on the context has finished. */
 int apg_ctx_synchronize(apg_ctx* ctx);
 
@@ -330,6 +334,111 @@ int apg_gkr_forward_narrow(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_
                            const uint8_t* bits, int base_on_device, const uint32_t* slots,
                            const uint8_t* slot_values, size_t n_slots, apg_gkr_values** out);
 
+/* ---- shard proofs (crates/prover/src/lib.rs:798-1102) -------------------- */
+
+/* One shard's hot path, the slice of prove_shard_columns that this library
+ * replaces: commit every column (commit_all, lib.rs:444-471), seed the shard
+ * transcript (verifier_core::shard_transcript, crates/verifier-core/src/
+ * statement.rs:548-572: SHARD_SEED [statement digest, family, index],
+ * SHARD_TS_WINDOW [ts_lo, ts_hi], the commitments as one G1 list under
+ * COMMITMENT, then the lookup challenges g and beta under LOOKUP_CHALLENGE,
+ * which the circuit reads as external challenge slots 0 and 1), run
+ * gkr::forward and gkr::prove (gkr_part, lib.rs:850,943) and open every column
+ * at the base point the proof leaves (opening_part -> batch_open_stacked at
+ * r = [], lib.rs:1076). */
+typedef struct apg_shard {
+  const uint8_t* circuit;           /* APGC blob of the shard's circuit */
+  size_t circuit_len;
+  const void* const* cols;          /* n_cols columns, Fr in memory, 2^num_vars each */
+  size_t n_cols;
+  int cols_on_device;               /* 1: device pointers on the context's device */
+  size_t num_vars;                  /* even, 2..30 */
+  const uint8_t* statement_digest;  /* 32 bytes, Fr in memory */
+  uint32_t family, index;           /* the shard's family and index (u32 in the reference) */
+  uint64_t ts_lo, ts_hi;            /* its timestamp window */
+} apg_shard;
+
+/* Where a shard proof lands (caller-owned buffers, filled when it is done). */
+typedef struct apg_shard_proof {
+  uint8_t* cms;         /* n_cols x 64: the commitments */
+  uint8_t* gkr_proof;   /* apg_gkr_proof_len(circuit) bytes: the GKR proof (Fr in memory) */
+  size_t gkr_cap;
+  size_t gkr_len;       /* out */
+  uint8_t* point;       /* num_vars x 32: the base point (Fr in memory) */
+  uint8_t* values;      /* n_cols x 32: the columns at the point (Fr in memory) */
+  uint8_t opening[704]; /* the batched Mercury opening */
+  uint8_t transcript[226];
+  double phase_ms[4];   /* out: commit, forward, GKR proof, opening (host wall clock) */
+} apg_shard_proof;
+
+/* Prove one shard on the context (columns on its device or host). */
+int apg_prove_shard(apg_ctx* ctx, const apg_shard* shard, apg_shard_proof* out);
+/* No reference counterpart: an estimate of the device bytes proving `shard`
+ * holds at its peak on a context that holds nothing yet (staged columns, GKR
+ * layers, the largest sumcheck's levels, both commit lanes' MSM scratch, the
+ * opening's tables); 0 for a malformed circuit. The server admits by it. */
+size_t apg_shard_device_bytes(const apg_shard* shard);
+/* No reference counterpart: the device bytes the context (and its second
+ * lane) holds in scratch, window tables it owns and its SRS if owned. */
+size_t apg_ctx_device_bytes(apg_ctx* ctx);
+
+/* ---- the shard-proof server (no reference counterpart) ------------------
+ *
+ * Continuous batching of shard proofs on one GPU: requests are queued as they
+ * are submitted and admitted in arrival order as soon as a worker (a context
+ * with its own stream and scratch, sharing the owner's SRS, window tables and
+ * tuned widths) is idle or can be added, and the request's device bytes fit
+ * the measured free HBM (cudaMemGetInfo plus what the stream-ordered pool
+ * holds unused, minus the growth reserved for requests already admitted and
+ * `hbm_reserve`) and the budget (`hbm_budget`, 0 = none: the workers' held
+ * bytes plus reservations stay below it). Admitted requests run concurrently,
+ * each on its own worker's stream, so their kernels overlap on the device; a
+ * request keeps its columns, layer values, buckets and transcript state on
+ * its worker until it completes. Workers are added as memory admits, up to
+ * `max_workers` (0 = no cap beyond memory). Results are byte for byte those
+ * of apg_prove_shard on the same request. Build the owner's window tables
+ * (apg_srs_prepare, apg_msm_autotune) before creating the server: workers
+ * borrow the tables the owner holds then. */
+typedef struct apg_server apg_server;
+typedef struct apg_server_config {
+  size_t hbm_budget;  /* bytes; 0 = no budget beyond free HBM */
+  size_t hbm_reserve; /* free bytes never handed to a request */
+  int max_workers;    /* 0 = no cap */
+  int timing;         /* 1: time every worker's kernels and host round steps (apg_server_query) */
+} apg_server_config;
+/* Per-request timestamps, nanoseconds since the server started, and what the
+ * request reserved. */
+typedef struct apg_request_times {
+  uint64_t submit_ns, admit_ns, start_ns, done_ns;
+  uint64_t reserved_bytes;
+  int worker;
+  double phase_ms[4];
+} apg_request_times;
+typedef struct apg_server_stats {
+  uint64_t submitted, completed, failed, queued, in_flight;
+  uint64_t workers, peak_workers, peak_in_flight;
+  uint64_t held_bytes, reserved_bytes;
+  double kernel_ms;     /* with timing: the sum of every worker kernel's duration */
+  double host_round_ms; /* with timing: host time between sumcheck rounds, all workers */
+} apg_server_stats;
+
+/* A server whose workers share `owner`'s SRS and tables (`owner` must outlive
+ * it and not replace its SRS meanwhile). */
+int apg_server_create(apg_ctx* owner, const apg_server_config* cfg, apg_server** out);
+/* Finish every admitted and queued request, then release the workers. */
+void apg_server_destroy(apg_server* server);
+/* Queue a request; `shard`'s arrays and `out`'s buffers must stay valid until
+ * the request completes (host columns are copied to the device when the
+ * request runs). Writes a ticket. */
+int apg_submit(apg_server* server, const apg_shard* shard, apg_shard_proof* out, uint64_t* ticket);
+/* APG_PENDING while the request is queued or running; APG_OK once its proof
+ * is in `out`; else the request's failure status. times (nullable). */
+int apg_poll(apg_server* server, uint64_t ticket, apg_request_times* times);
+/* As apg_poll, blocking until the request is done. */
+int apg_wait(apg_server* server, uint64_t ticket, apg_request_times* times);
+/* Counters and held bytes of the server now. */
+int apg_server_query(apg_server* server, apg_server_stats* out);
+
 /* ---- deferred-pairing accumulator (crates/pcs/src/accumulator.rs) ------- */
 
 /* The group side of pcs::discharge (crates/pcs/src/accumulator.rs:146-163),
@@ -393,9 +502,13 @@ enum apg_timer {
   APG_TIMER_MSM_TOTAL = 1,      /* one whole MSM, recode to normalisation */
   APG_TIMER_SUMCHECK_ROUND = 2, /* sumcheck evaluate+fold kernel */
   APG_TIMER_GKR_FORWARD = 3,    /* GKR forward layer kernel */
-  APG_TIMER_MERCURY_PASS = 4    /* Mercury O(n) field passes */
+  APG_TIMER_MERCURY_PASS = 4,   /* Mercury O(n) field passes */
+  APG_TIMER_KERNELS = 5,        /* every kernel launch (timing mode 2 only) */
+  APG_TIMER_HOST_ROUND = 6      /* host time between a sumcheck round's sums and the next round's launch */
 };
-/* Enable (1) or disable (0) timers; enabling clears accumulated totals. */
+/* Enable (1) or disable (0) timers; enabling clears accumulated totals. Mode
+ * 2 also brackets every kernel launch with events (APG_TIMER_KERNELS: the
+ * device's busy time on the context's streams), at a small cost a launch. */
 int apg_ctx_set_timing(apg_ctx* ctx, int on);
 /* Total milliseconds and launch count recorded under `timer` so far. */
 int apg_ctx_timer(apg_ctx* ctx, int timer, double* ms, uint64_t* launches);
