@@ -27,8 +27,10 @@ STATUS = {
     0: "Ok", 1: "LengthMismatch", 2: "UnsupportedNumVars", 3: "PointLengthMismatch", 4: "SrsTooSmall",
     5: "DegenerateChallenge", 6: "EmptyBatch", 7: "BatchLengthMismatch", 8: "MixedColumnSizes",
     9: "InvalidPoint", 10: "MalformedAccumulator", 20: "NonCanonical", 21: "InvalidArgument", 22: "BadCircuit", 23: "NoSrs",
-    24: "Internal", 100: "Cuda", 101: "OutOfMemory", 103: "NoDevice",
+    24: "Internal", 25: "NoAllocTooLarge", 26: "Pending", 27: "UnknownTicket", 100: "Cuda", 101: "OutOfMemory",
+    103: "NoDevice",
 }
+PENDING = 26
 PCS_CODES = {2, 3, 4, 5, 6, 7, 8, 9, 10}
 
 
@@ -533,10 +535,26 @@ class Context:
         self._check(lib().apg_witness_digest(self._h, ptrs, ctypes.c_size_t(k), ctypes.c_size_t(num_vars), out))
         return from_mont_bytes(out.raw)[0]
 
-    TIMER_MSM_ACCUMULATE, TIMER_MSM_TOTAL, TIMER_SUMCHECK_ROUND, TIMER_GKR_FORWARD, TIMER_MERCURY_PASS = range(5)
+    (TIMER_MSM_ACCUMULATE, TIMER_MSM_TOTAL, TIMER_SUMCHECK_ROUND, TIMER_GKR_FORWARD, TIMER_MERCURY_PASS,
+     TIMER_KERNELS, TIMER_HOST_ROUND) = range(7)
 
-    def set_timing(self, on: bool):
-        self._check(lib().apg_ctx_set_timing(self._h, 1 if on else 0))
+    def set_timing(self, on, kernels: bool = False):
+        """Timers on or off; with kernels, every launch is timed too
+        (TIMER_KERNELS, the device's busy time)."""
+        self._check(lib().apg_ctx_set_timing(self._h, (2 if kernels else 1) if on else 0))
+
+    def device_bytes(self) -> int:
+        L = lib()
+        L.apg_ctx_device_bytes.restype = ctypes.c_size_t
+        L.apg_ctx_device_bytes.argtypes = [ctypes.c_void_p]
+        return L.apg_ctx_device_bytes(self._h)
+
+    def prove_shard(self, shard: "Shard") -> "ShardProof":
+        """Prove one shard (apg_prove_shard): commit, shard transcript, GKR
+        forward and proof, batched opening at the base point."""
+        proof = ShardProof(shard)
+        self._check(lib().apg_prove_shard(self._h, ctypes.byref(shard.c), ctypes.byref(proof.c)))
+        return proof
 
     def timer(self, which: int):
         ms = ctypes.c_double()
@@ -548,3 +566,169 @@ class Context:
         r = ctypes.c_double()
         self._check(lib().apg_probe_fq_mul_rate(self._h, ctypes.c_double(ms), ctypes.byref(r)))
         return r.value
+
+
+# ---------------------------------------------------------------------------
+# Shard proofs and the server
+# ---------------------------------------------------------------------------
+
+class _CShard(ctypes.Structure):
+    _fields_ = [("circuit", ctypes.c_char_p), ("circuit_len", ctypes.c_size_t),
+                ("cols", ctypes.POINTER(ctypes.c_void_p)), ("n_cols", ctypes.c_size_t),
+                ("cols_on_device", ctypes.c_int), ("num_vars", ctypes.c_size_t),
+                ("statement_digest", ctypes.c_char_p), ("family", ctypes.c_uint32), ("index", ctypes.c_uint32),
+                ("ts_lo", ctypes.c_uint64), ("ts_hi", ctypes.c_uint64)]
+
+
+class _CShardProof(ctypes.Structure):
+    _fields_ = [("cms", ctypes.c_void_p), ("gkr_proof", ctypes.c_void_p), ("gkr_cap", ctypes.c_size_t),
+                ("gkr_len", ctypes.c_size_t), ("point", ctypes.c_void_p), ("values", ctypes.c_void_p),
+                ("opening", ctypes.c_uint8 * PROOF_BYTES), ("transcript", ctypes.c_uint8 * TRANSCRIPT_BYTES),
+                ("phase_ms", ctypes.c_double * 4)]
+
+
+class _CTimes(ctypes.Structure):
+    _fields_ = [("submit_ns", ctypes.c_uint64), ("admit_ns", ctypes.c_uint64), ("start_ns", ctypes.c_uint64),
+                ("done_ns", ctypes.c_uint64), ("reserved_bytes", ctypes.c_uint64), ("worker", ctypes.c_int),
+                ("phase_ms", ctypes.c_double * 4)]
+
+
+class _CStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "completed", "failed", "queued", "in_flight", "workers",
+                                                "peak_workers", "peak_in_flight", "held_bytes", "reserved_bytes")]
+    _fields_ += [("kernel_ms", ctypes.c_double), ("host_round_ms", ctypes.c_double)]
+
+
+class _CServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget", ctypes.c_size_t), ("hbm_reserve", ctypes.c_size_t), ("max_workers", ctypes.c_int),
+                ("timing", ctypes.c_int)]
+
+
+class Shard:
+    """One shard request (apg_shard): the circuit blob, its committed columns
+    (device pointers, or host bytes with on_device=False; Fr in memory) and
+    the shard's identity for its transcript seed
+    (verifier_core::shard_transcript)."""
+
+    def __init__(self, circuit: bytes, cols, num_vars: int, digest: int, family: int, index: int, ts_lo: int,
+                 ts_hi: int, on_device: bool = True):
+        self.circuit = bytes(circuit)
+        self.cols = list(cols)  # keeps host buffers alive
+        self.num_vars = num_vars
+        if on_device:
+            ptrs = self.cols
+        else:
+            self._host = [ctypes.c_char_p(c) for c in self.cols]
+            ptrs = [ctypes.cast(h, ctypes.c_void_p).value for h in self._host]
+        self._ptrs = (ctypes.c_void_p * len(ptrs))(*ptrs)
+        self._digest = to_mont_bytes([digest])
+        self.c = _CShard(self.circuit, len(self.circuit), ctypes.cast(self._ptrs, ctypes.POINTER(ctypes.c_void_p)),
+                         len(self.cols), 1 if on_device else 0, num_vars, self._digest, family, index, ts_lo, ts_hi)
+
+
+class ShardProof:
+    """Where a shard proof lands (apg_shard_proof), with readers."""
+
+    def __init__(self, shard: Shard):
+        k, nv = len(shard.cols), shard.num_vars
+        L = lib()
+        L.apg_gkr_proof_len.restype = ctypes.c_size_t
+        cap = L.apg_gkr_proof_len(shard.circuit, ctypes.c_size_t(len(shard.circuit)))
+        self._cms = ctypes.create_string_buffer(64 * k)
+        self._gkr = ctypes.create_string_buffer(max(cap, 32))
+        self._point = ctypes.create_string_buffer(32 * max(nv, 1))
+        self._values = ctypes.create_string_buffer(32 * k)
+        self.k, self.nv = k, nv
+        self.c = _CShardProof(ctypes.cast(self._cms, ctypes.c_void_p), ctypes.cast(self._gkr, ctypes.c_void_p), cap,
+                              0, ctypes.cast(self._point, ctypes.c_void_p), ctypes.cast(self._values, ctypes.c_void_p))
+
+    @property
+    def cms(self):
+        return [self._cms.raw[64 * j:64 * j + 64] for j in range(self.k)]
+
+    @property
+    def gkr(self):
+        return from_mont_bytes(self._gkr.raw[:self.c.gkr_len])
+
+    @property
+    def point(self):
+        return from_mont_bytes(self._point.raw[:32 * self.nv])
+
+    @property
+    def values(self):
+        return from_mont_bytes(self._values.raw[:32 * self.k])
+
+    @property
+    def opening(self) -> bytes:
+        return bytes(self.c.opening)
+
+    @property
+    def transcript(self) -> bytes:
+        return bytes(self.c.transcript)
+
+    @property
+    def phase_ms(self):
+        return list(self.c.phase_ms)
+
+
+class Server:
+    """The library's shard-proof server (apg_server): continuous batching with
+    admission by measured free HBM. Workers share `owner`'s SRS and tables."""
+
+    def __init__(self, owner: Context, hbm_budget: int = 0, hbm_reserve: int = 0, max_workers: int = 0,
+                 timing: bool = False):
+        self.owner = owner
+        self._h = ctypes.c_void_p()
+        cfg = _CServerConfig(hbm_budget, hbm_reserve, max_workers, 1 if timing else 0)
+        st = lib().apg_server_create(owner.handle, ctypes.byref(cfg), ctypes.byref(self._h))
+        if st:
+            raise ApogeeError(st, "apg_server_create")
+        self._live = {}
+
+    def submit(self, shard: Shard) -> int:
+        proof = ShardProof(shard)
+        t = ctypes.c_uint64()
+        st = lib().apg_submit(self._h, ctypes.byref(shard.c), ctypes.byref(proof.c), ctypes.byref(t))
+        if st:
+            raise ApogeeError(st, "apg_submit")
+        self._live[t.value] = (shard, proof)
+        return t.value
+
+    def _result(self, st, ticket, tm):
+        if st == PENDING:
+            return None
+        if st:
+            raise ApogeeError(st, f"shard request {ticket}")
+        _, proof = self._live[ticket]
+        times = {"submit_ns": tm.submit_ns, "admit_ns": tm.admit_ns, "start_ns": tm.start_ns,
+                 "done_ns": tm.done_ns, "reserved_bytes": tm.reserved_bytes, "worker": tm.worker,
+                 "phase_ms": list(tm.phase_ms)}
+        return proof, times
+
+    def poll(self, ticket: int):
+        """None while pending, else (ShardProof, times)."""
+        tm = _CTimes()
+        return self._result(lib().apg_poll(self._h, ctypes.c_uint64(ticket), ctypes.byref(tm)), ticket, tm)
+
+    def wait(self, ticket: int):
+        tm = _CTimes()
+        return self._result(lib().apg_wait(self._h, ctypes.c_uint64(ticket), ctypes.byref(tm)), ticket, tm)
+
+    def stats(self) -> dict:
+        s = _CStats()
+        st = lib().apg_server_query(self._h, ctypes.byref(s))
+        if st:
+            raise ApogeeError(st, "apg_server_query")
+        return {n: getattr(s, n) for n, _ in _CStats._fields_}
+
+    def close(self):
+        if self._h:
+            lib().apg_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+            self._live.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

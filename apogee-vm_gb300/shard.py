@@ -1,6 +1,7 @@
 """Shard proving over the C ABI, and the shard workloads the benchmark runs.
 
-`prove_shard` is the hot-path slice of crates/prover's prove_shard_columns
+`prove_shard` (the library's apg_prove_shard) is the hot-path slice of
+crates/prover's prove_shard_columns
 (crates/prover/src/lib.rs:798-1102): commit every column (commit_all), seed the
 shard transcript and absorb the commitments, run the GKR forward and backward
 passes, and open every column at the base point GKR leaves with one batched
@@ -11,16 +12,14 @@ Workloads:
     the even heights 2^8 .. 2^22 (Mercury takes even variable counts only),
     4 to 16 columns each, values drawn like VM trace columns.
   * `prove_sequential`: one shard at a time on one context (the plain path).
-  * `prove_batched`: shards spread over several contexts (streams) proved
-    concurrently, largest first.
-  * `serve`: a seeded Poisson stream of shard requests, admitted as a context
-    and enough HBM (a fixed budget) free up, proved concurrently; latency is
-    completion minus arrival.
+  * `prove_batched`: every shard submitted at once to the library's server
+    (apg_server, continuous batching with admission by measured free HBM),
+    largest first.
+  * `serve`: a seeded Poisson stream of shard requests submitted to the
+    server as they arrive; latency is completion minus arrival.
 """
-import heapq
 import math
 import random
-import threading
 import time
 
 import apogee_gpu as A
@@ -125,9 +124,31 @@ def shard_transcript(spec, cms):
     return tr, g, beta
 
 
-def prove_shard(ctx, spec, cols):
-    """One shard's hot path; cols are device tensors. Returns the commitments,
-    the GKR proof, the base point, the opened values and the opening proof."""
+def make_shard(spec, cols, blob=None):
+    """The library's shard request for `spec` over device columns `cols`:
+    its circuit (the synthetic shard circuit unless `blob` is given) and its
+    transcript seed (statement digest, family, index, time window)."""
+    lo = spec["index"] << 22
+    return A.Shard(blob or shard_circuit(spec["log_rows"], spec["cols"]), [t.data_ptr() for t in cols],
+                   spec["log_rows"], statement_digest(spec), spec["family"], spec["index"], lo,
+                   lo + (1 << spec["log_rows"]))
+
+
+def _as_dict(p):
+    return {"cms": p.cms, "gkr": p.gkr, "point": p.point, "vs": p.values, "opening": p.opening,
+            "transcript": p.transcript, "phase_ms": p.phase_ms}
+
+
+def prove_shard(ctx, spec, cols, blob=None):
+    """One shard through the library's shard prover (apg_prove_shard): the
+    commitments, the GKR proof, the base point, the opened values, the
+    opening proof and the transcript after it."""
+    return _as_dict(ctx.prove_shard(make_shard(spec, cols, blob)))
+
+
+def prove_shard_composed(ctx, spec, cols):
+    """The same shard from the library's separate entry points, the schedule
+    driven from here: what apg_prove_shard must reproduce."""
     n_vars = spec["log_rows"]
     ptrs = [t.data_ptr() for t in cols]
     cms = ctx.commit_batch_device(ptrs, n_vars)
@@ -142,116 +163,68 @@ def prove_shard(ctx, spec, cols):
     return {"cms": cms, "gkr": proof, "point": u, "vs": vs, "opening": opening, "transcript": tr}
 
 
-def hbm_estimate(spec) -> int:
-    """Device bytes one shard proof holds at its peak: the columns, the GKR
-    layer values (about twice the base), MSM and sumcheck scratch."""
-    n = 1 << spec["log_rows"]
-    base = 32 * n * spec["cols"]
-    return 4 * base + 64 * 16 * n + (64 << 20)
-
-
-def prove_sequential(ctx, specs, columns):
+def prove_sequential(ctx, specs, columns, blobs=None):
+    """One shard at a time on one context (the plain path)."""
     t0 = time.perf_counter()
-    outs = [prove_shard(ctx, s, columns[s["index"]]) for s in specs]
+    outs = {s["index"]: prove_shard(ctx, s, columns[s["index"]], (blobs or {}).get(s["index"])) for s in specs}
     return time.perf_counter() - t0, outs
 
 
-def prove_batched(ctxs, specs, columns):
-    """Largest shards first, each context proving the next unclaimed shard."""
+def prove_batched(server, specs, columns, blobs=None):
+    """Every shard submitted at once to the library's server, largest first;
+    it admits them as workers and memory allow and runs them side by side."""
     order = sorted(specs, key=lambda s: -(s["cols"] << s["log_rows"]))
-    lock = threading.Lock()
-    nxt = [0]
-    outs = {}
-    errors = []
-
-    def worker(ctx):
-        while True:
-            with lock:
-                if nxt[0] >= len(order):
-                    return
-                s = order[nxt[0]]
-                nxt[0] += 1
-            try:
-                outs[s["index"]] = prove_shard(ctx, s, columns[s["index"]])
-            except Exception as e:  # surfaced after the join
-                errors.append(e)
-                return
-
     t0 = time.perf_counter()
-    threads = [threading.Thread(target=worker, args=(c,)) for c in ctxs]
-    for t in threads:
-        t.start()
-    for t in threads:
-        t.join()
-    dt = time.perf_counter() - t0
-    if errors:
-        raise errors[0]
-    return dt, outs
+    tickets = {s["index"]: server.submit(make_shard(s, columns[s["index"]], (blobs or {}).get(s["index"])))
+               for s in order}
+    outs, times = {}, {}
+    for i, t in tickets.items():
+        p, tm = server.wait(t)
+        outs[i], times[i] = _as_dict(p), tm
+    return time.perf_counter() - t0, outs, times
 
 
-def serve(ctxs, specs, columns, rate: float, budget_bytes: int, seed: int = 7):
-    """Poisson arrivals at `rate` requests/s over `specs` (in order), admitted
-    first-come first-served when a context is idle and the request's HBM
-    estimate fits the budget. Returns (wall seconds, sorted latencies in
-    seconds, each shard's proof by index)."""
+def serve(server, specs, columns, rate: float, seed: int = 7, blobs=None):
+    """A seeded Poisson stream of shard requests at `rate` a second, in the
+    order of `specs`, submitted to the library's server as they arrive.
+    Returns (wall seconds, sorted latencies in seconds, each shard's proof by
+    index, each request's times)."""
     rng = random.Random(seed)
     arrivals = []
     t = 0.0
     for s in specs:
         t += rng.expovariate(rate)
         arrivals.append((t, s))
-    cv = threading.Condition()
-    state = {"free": list(ctxs), "budget": budget_bytes, "queue": [], "done": 0}
-    lat = []
-    outputs = {}
-    errors = []
+    tickets = {}
     start = time.perf_counter()
-
-    def run(ctx, s, arrival, need):
-        try:
-            res = prove_shard(ctx, s, columns[s["index"]])
-            done = time.perf_counter() - start
-            with cv:
-                lat.append(done - arrival)
-                outputs[s["index"]] = res
-        except Exception as e:
-            errors.append(e)
-        finally:
-            with cv:
-                state["free"].append(ctx)
-                state["budget"] += need
-                state["done"] += 1
-                cv.notify_all()
-
-    def dispatcher():
-        i = 0
-        while True:
-            with cv:
-                now = time.perf_counter() - start
-                while i < len(arrivals) and arrivals[i][0] <= now:
-                    state["queue"].append(arrivals[i])
-                    i += 1
-                while state["queue"] and state["free"]:
-                    arr, s = state["queue"][0]
-                    need = hbm_estimate(s)
-                    if need > state["budget"] and state["budget"] < budget_bytes:
-                        break  # wait for memory to free up (head of line keeps its turn)
-                    state["queue"].pop(0)
-                    ctx = state["free"].pop()
-                    state["budget"] -= need
-                    threading.Thread(target=run, args=(ctx, s, arr, need), daemon=True).start()
-                if state["done"] == len(arrivals):
-                    return
-                wait = 0.05
-                if i < len(arrivals):
-                    wait = max(0.0, min(wait, arrivals[i][0] - (time.perf_counter() - start)))
-                cv.wait(timeout=wait)
-
-    dispatcher()
+    for at, s in arrivals:
+        delay = at - (time.perf_counter() - start)
+        if delay > 0:
+            time.sleep(delay)
+        tickets[s["index"]] = server.submit(make_shard(s, columns[s["index"]], (blobs or {}).get(s["index"])))
+    outs, times = {}, {}
+    for i, tk in tickets.items():
+        p, tm = server.wait(tk)
+        outs[i], times[i] = _as_dict(p), tm
     wall = time.perf_counter() - start
-    if errors:
-        raise errors[0]
-    return wall, sorted(lat), outputs
+    lat = sorted((tm["done_ns"] - tm["submit_ns"]) / 1e9 for tm in times.values())
+    return wall, lat, outs, times
+
+
+def latency_attribution(times, q=0.99):
+    """Where the slowest requests' time went: the requests at or above the
+    q-quantile of latency, their mean queueing (submit to admission), and
+    their mean phases (commit, forward, GKR proof, opening) in ms."""
+    lat = sorted(((tm["done_ns"] - tm["submit_ns"]) / 1e6, i) for i, tm in times.items())
+    if not lat:
+        return {}
+    k = max(0, min(len(lat) - 1, int(math.ceil(q * len(lat))) - 1))
+    tail = [i for _, i in lat[k:]]
+    n = len(tail)
+    qwait = sum((times[i]["admit_ns"] - times[i]["submit_ns"]) / 1e6 for i in tail) / n
+    phases = [sum(times[i]["phase_ms"][j] for i in tail) / n for j in range(4)]
+    return {"requests": n, "latency_ms": lat[k][0], "queue_ms": qwait, "commit_ms": phases[0],
+            "forward_ms": phases[1], "gkr_ms": phases[2], "open_ms": phases[3]}
 
 
 def percentile(xs, q):

@@ -531,7 +531,7 @@ def run_profile_discharge(args, ctx):
     return 0
 
 
-def run_shard_workloads(ctx, local, contexts=6, serve_budget_gb=150):
+def run_shard_workloads(ctx, local, serve_budget_gb=150):
     """Configs 1-5 beside the headline: the small plain case, one execution
     shard, the largest shard's commit + batched opening, the 207-shard mix
     proved one shard at a time vs concurrently, and Poisson serving."""
@@ -629,30 +629,64 @@ def run_shard_workloads(ctx, local, contexts=6, serve_budget_gb=150):
     del cols3
     torch.cuda.empty_cache()
 
-    # Configs 4 and 5: the 207-shard mix, columns resident in HBM.
+    # Configs 4 and 5: the 207-shard mix, columns resident in HBM, proved one
+    # shard at a time on this context and through the library's server
+    # (continuous batching, admission by measured free HBM under the budget).
     specs = shard.shard_mix(207)
     columns = {s["index"]: shard.device_columns(torch, 1 << s["log_rows"], s["cols"], SEED + 100 + s["index"], dev,
                                                 ctx) for s in specs}
     torch.cuda.synchronize()
+    budget = int(serve_budget_gb * 1e9)
     shard.prove_sequential(ctx, specs[:12], columns)  # warm the circuits and scratch
-    seq_t, _ = shard.prove_sequential(ctx, specs, columns)
-    extra = [A.Context(local) for _ in range(contexts - 1)]
-    for c in extra:
-        c.srs_share(ctx)
-    ctxs = [ctx] + extra
-    shard.prove_batched(ctxs, specs[:24], columns)
-    bat_t, _ = shard.prove_batched(ctxs, specs, columns)
+    seq_t, seq_out = shard.prove_sequential(ctx, specs, columns)
+    server = A.Server(ctx, hbm_budget=budget)
+    shard.prove_batched(server, specs[:24], columns)  # warm the workers
+    bat_t, _, _ = shard.prove_batched(server, specs, columns)
     cap = len(specs) / bat_t
-    wall, lat, _ = shard.serve(ctxs, specs, columns, rate=0.8 * cap, budget_bytes=int(serve_budget_gb * 1e9))
-    for c in extra:
-        c.close()
+    wall, lat, _, srv_times = shard.serve(server, specs, columns, rate=0.8 * cap)
+    srv_stats = server.stats()
+    server.close()
+
+    # Where the time goes: the same two runs with every kernel timed (the sum
+    # of kernel durations over the wall clock: the device's busy fraction,
+    # counted per stream, so side-by-side kernels can sum past 1) and the host
+    # steps between sumcheck rounds; per size class, one shard at a time.
+    ctx.set_timing(True, kernels=True)
+    seq_t2, _ = shard.prove_sequential(ctx, specs, columns)
+    seq_kernel_ms, _ = ctx.timer(A.Context.TIMER_KERNELS)
+    seq_host_ms, seq_rounds = ctx.timer(A.Context.TIMER_HOST_ROUND)
+    ctx.set_timing(False)
+    timed_server = A.Server(ctx, hbm_budget=budget, timing=True)
+    bat_t2, _, _ = shard.prove_batched(timed_server, specs, columns)
+    tstats = timed_server.stats()
+    timed_server.close()
+    per_size = {}
+    for s_ in specs:
+        ph = seq_out[s_["index"]]["phase_ms"]
+        d = per_size.setdefault(s_["log_rows"], {"shards": 0, "commit_ms": 0.0, "forward_ms": 0.0, "gkr_ms": 0.0,
+                                                 "open_ms": 0.0})
+        d["shards"] += 1
+        for key, v in zip(("commit_ms", "forward_ms", "gkr_ms", "open_ms"), ph):
+            d[key] += v
     out["cfg4"] = {"shards": len(specs), "points": sum(s["cols"] << s["log_rows"] for s in specs),
                    "sequential_shards_per_s": len(specs) / seq_t, "batched_shards_per_s": cap,
-                   "batched_over_sequential": seq_t / bat_t, "contexts": contexts,
-                   "mix": "207 shards, 23 families, 2^8..2^22 rows (even), 4-16 columns"}
+                   "batched_over_sequential": seq_t / bat_t,
+                   "server": f"apg_server (library), budget {serve_budget_gb} GB, workers added as memory admits",
+                   "peak_workers": srv_stats["peak_workers"], "peak_in_flight": srv_stats["peak_in_flight"],
+                   "mix": "207 shards, 23 families, 2^8..2^22 rows (even), 4-16 columns",
+                   "account": {
+                       "sequential_s": seq_t2, "sequential_kernel_s": seq_kernel_ms / 1e3,
+                       "sequential_busy_fraction": seq_kernel_ms / 1e3 / seq_t2,
+                       "sequential_host_round_s": seq_host_ms / 1e3, "sumcheck_rounds": seq_rounds,
+                       "batched_s": bat_t2, "batched_kernel_s": tstats["kernel_ms"] / 1e3,
+                       "batched_busy_fraction": tstats["kernel_ms"] / 1e3 / bat_t2,
+                       "batched_host_round_s": tstats["host_round_ms"] / 1e3,
+                       "per_size_alone_ms": per_size}}
     out["cfg5"] = {"rate_per_s": 0.8 * cap, "shards_per_s": len(lat) / wall,
                    "p50_ms": shard.percentile(lat, 0.50) * 1e3, "p99_ms": shard.percentile(lat, 0.99) * 1e3,
-                   "hbm_budget_gb": serve_budget_gb, "requests": len(lat)}
+                   "hbm_budget_gb": serve_budget_gb, "requests": len(lat),
+                   "p99_attribution": shard.latency_attribution(srv_times, 0.99),
+                   "median_attribution": shard.latency_attribution(srv_times, 0.5)}
     del columns
     torch.cuda.empty_cache()
     return out

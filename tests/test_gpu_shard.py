@@ -1,7 +1,10 @@
-"""End-to-end parity of the shard pipeline (commit every column, seed the shard
-transcript, GKR forward + prove, batched Mercury opening at the GKR base point)
-against the oracle driving the same schedule, and the serving invariant: a
-shard's proof is the same alone, in a concurrent batch and in the served mix."""
+"""End-to-end parity of the library's shard prover (apg_prove_shard: commit
+every column, seed the shard transcript, GKR forward + prove, batched Mercury
+opening at the GKR base point) against the oracle driving the same schedule
+and against the separate entry points, and the server's invariants
+(apg_server, apg_submit, apg_poll/apg_wait): a shard's proof is the same
+alone, in a concurrent batch and in the served mix; admission holds to the
+memory budget; failures stay with their request."""
 import ctypes
 import random
 
@@ -72,6 +75,7 @@ def test_shard_pipeline_matches_oracle(env):
         cols = shard.device_columns(torch, 1 << spec["log_rows"], spec["cols"], 99 + spec["index"], "cuda:0", ctx)
         torch.cuda.synchronize()
         out = shard.prove_shard(ctx, spec, cols)
+        assert _strip(out) == shard.prove_shard_composed(ctx, spec, cols)
         ints = [A.from_mont_bytes(bytes(c.cpu().numpy().tobytes())) for c in cols]
         cms, proof, snap, gamma = oracle_shard(spec, ints, srs, tau)
         assert out["cms"] == cms
@@ -96,7 +100,36 @@ def test_shard_pipeline_matches_oracle(env):
             assert t[0] == v
 
 
+def _strip(out):
+    return {k: v for k, v in out.items() if k != "phase_ms"}
+
+
+def test_shard_prover_equals_the_composed_entry_points(env):
+    """apg_prove_shard equals the same schedule driven from the host over the
+    separate entry points (commit_batch, the transcript, gkr_forward/prove,
+    batch_open), from device and from host columns."""
+    import apogee_gpu as A
+    import shard
+
+    ctx, torch, _ = env
+    spec = {"index": 21, "family": 4, "log_rows": 8, "cols": 6}
+    cols = shard.device_columns(torch, 1 << 8, 6, 1234, "cuda:0", ctx)
+    torch.cuda.synchronize()
+    want = shard.prove_shard_composed(ctx, spec, cols)
+    assert _strip(shard.prove_shard(ctx, spec, cols)) == want
+    host = [bytes(c.cpu().numpy().tobytes()) for c in cols]
+    lo = spec["index"] << 22
+    sh = A.Shard(shard.shard_circuit(8, 6), host, 8, shard.statement_digest(spec), spec["family"], spec["index"], lo,
+                 lo + 256, on_device=False)
+    p = ctx.prove_shard(sh)
+    assert (p.cms, p.gkr, p.point, p.values, p.opening, p.transcript) == (
+        want["cms"], want["gkr"], want["point"], want["vs"], want["opening"], want["transcript"])
+
+
 def test_alone_equals_batched_equals_served(env):
+    """The server's invariant: each shard's proof is the same alone (one
+    shard at a time on the caller's context), when every shard is submitted
+    at once, and in a Poisson stream; requests overlap on the device."""
     import apogee_gpu as A
     import shard
 
@@ -107,17 +140,61 @@ def test_alone_equals_batched_equals_served(env):
     columns = {s["index"]: shard.device_columns(torch, 1 << s["log_rows"], s["cols"], 500 + s["index"], "cuda:0",
                                                 ctx) for s in specs}
     torch.cuda.synchronize()
-    alone = {s["index"]: shard.prove_shard(ctx, s, columns[s["index"]]) for s in specs}
-    extra = [A.Context(0) for _ in range(3)]
-    for c in extra:
-        c.srs_share(ctx)
-    ctxs = [ctx] + extra
-    _, batched = shard.prove_batched(ctxs, specs, columns)
+    alone = {s["index"]: _strip(shard.prove_shard(ctx, s, columns[s["index"]])) for s in specs}
+    with A.Server(ctx, max_workers=4) as server:
+        _, batched, times = shard.prove_batched(server, specs, columns)
+        for s in specs:
+            assert _strip(batched[s["index"]]) == alone[s["index"]], f"shard {s['index']} differs in the batch"
+        wall, lat, served, _ = shard.serve(server, specs, columns, rate=200.0)
+        assert len(lat) == len(specs)
+        for s in specs:
+            assert _strip(served[s["index"]]) == alone[s["index"]], f"shard {s['index']} differs when served"
+        st = server.stats()
+        assert st["completed"] == 2 * len(specs) and st["failed"] == 0 and st["queued"] == 0
+        assert st["peak_in_flight"] > 1, "the requests ran side by side"
+        assert all(tm["submit_ns"] <= tm["admit_ns"] <= tm["start_ns"] <= tm["done_ns"] for tm in times.values())
+
+
+def test_server_admits_by_memory(env):
+    """With a budget no second request fits in, the server runs one request
+    at a time (the first is always admitted), and every request completes."""
+    import apogee_gpu as A
+    import shard
+
+    ctx, torch, _ = env
+    specs = [{"index": 40 + i, "family": i, "log_rows": 6, "cols": 4} for i in range(5)]
+    columns = {s["index"]: shard.device_columns(torch, 1 << 6, 4, 900 + s["index"], "cuda:0", ctx) for s in specs}
+    torch.cuda.synchronize()
+    with A.Server(ctx, hbm_budget=1) as server:
+        _, outs, _ = shard.prove_batched(server, specs, columns)
+        st = server.stats()
+    assert st["peak_in_flight"] == 1 and st["completed"] == len(specs)
     for s in specs:
-        assert batched[s["index"]] == alone[s["index"]], f"shard {s['index']} differs in the batch"
-    wall, lat, served = shard.serve(ctxs, specs, columns, rate=200.0, budget_bytes=1 << 30)
-    assert len(lat) == len(specs)
-    for s in specs:
-        assert served[s["index"]] == alone[s["index"]], f"shard {s['index']} differs when served"
-    for c in extra:
-        c.close()
+        assert _strip(outs[s["index"]]) == _strip(shard.prove_shard(ctx, s, columns[s["index"]]))
+
+
+def test_server_reports_each_requests_failure(env):
+    """A malformed circuit is refused at submission; a request whose digest
+    is not a field element fails with its own status while the others in the
+    same batch complete."""
+    import apogee_gpu as A
+    import shard
+
+    ctx, torch, _ = env
+    cols = shard.device_columns(torch, 1 << 4, 4, 77, "cuda:0", ctx)
+    torch.cuda.synchronize()
+    good = {"index": 60, "family": 1, "log_rows": 4, "cols": 4}
+    with A.Server(ctx) as server:
+        bad_blob = A.Shard(b"APGC" + bytes(12), [c.data_ptr() for c in cols], 4, 1, 1, 60, 0, 16)
+        with pytest.raises(A.ApogeeError):
+            server.submit(bad_blob)
+        bad = shard.make_shard(good, cols)
+        bad._digest = b"\xff" * 32
+        bad.c.statement_digest = bad._digest
+        t_bad = server.submit(bad)
+        t_good = server.submit(shard.make_shard(good, cols))
+        with pytest.raises(A.ApogeeError) as e:
+            server.wait(t_bad)
+        assert e.value.variant == "NonCanonical"
+        p, _ = server.wait(t_good)
+        assert p.cms == shard.prove_shard(ctx, good, cols)["cms"]
