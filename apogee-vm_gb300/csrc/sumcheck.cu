@@ -124,7 +124,12 @@ __device__ __forceinline__ void round_total(const RoundArgs& A, const Fr* partia
   if (threadIdx.x == 0) *A.done = 0;
 }
 
-__global__ void __launch_bounds__(kRoundThreads) k_round(RoundArgs A, DevProgram P, VirtualRound V, Fr* partials) {
+// Resident blocks a SM k_round is compiled for (1: the compiler's choice).
+#ifndef APG_ROUND_MIN_BLOCKS
+#define APG_ROUND_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(kRoundThreads, APG_ROUND_MIN_BLOCKS)
+    k_round(RoundArgs A, DevProgram P, VirtualRound V, Fr* partials) {
   extern __shared__ uint32_t sm_raw[];
   const Slots sm = thread_slots(sm_raw);
   __shared__ Fr red[kRoundThreads];

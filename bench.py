@@ -639,7 +639,12 @@ def run_shard_workloads(ctx, local, serve_budget_gb=150):
     budget = int(serve_budget_gb * 1e9)
     shard.prove_sequential(ctx, specs[:12], columns)  # warm the circuits and scratch
     seq_t, seq_out = shard.prove_sequential(ctx, specs, columns)
-    server = A.Server(ctx, hbm_budget=budget)
+    # At most eight requests run at once: on this mix 2, 4, 6, 8, 12 and an
+    # uncapped 24 workers measured 28.5, 35.0, 36.2, 36.8, 29.4 and 29.7
+    # shards/s (more side-by-side 2^22-row shards contend for the SMs and L2);
+    # memory admission still decides below the cap.
+    workers = 8
+    server = A.Server(ctx, hbm_budget=budget, max_workers=workers)
     shard.prove_batched(server, specs[:24], columns)  # warm the workers
     bat_t, _, _ = shard.prove_batched(server, specs, columns)
     cap = len(specs) / bat_t
@@ -656,7 +661,7 @@ def run_shard_workloads(ctx, local, serve_budget_gb=150):
     seq_kernel_ms, _ = ctx.timer(A.Context.TIMER_KERNELS)
     seq_host_ms, seq_rounds = ctx.timer(A.Context.TIMER_HOST_ROUND)
     ctx.set_timing(False)
-    timed_server = A.Server(ctx, hbm_budget=budget, timing=True)
+    timed_server = A.Server(ctx, hbm_budget=budget, max_workers=workers, timing=True)
     bat_t2, _, _ = shard.prove_batched(timed_server, specs, columns)
     tstats = timed_server.stats()
     timed_server.close()
@@ -671,7 +676,8 @@ def run_shard_workloads(ctx, local, serve_budget_gb=150):
     out["cfg4"] = {"shards": len(specs), "points": sum(s["cols"] << s["log_rows"] for s in specs),
                    "sequential_shards_per_s": len(specs) / seq_t, "batched_shards_per_s": cap,
                    "batched_over_sequential": seq_t / bat_t,
-                   "server": f"apg_server (library), budget {serve_budget_gb} GB, workers added as memory admits",
+                   "server": f"apg_server (library), budget {serve_budget_gb} GB, up to {workers} requests at once, "
+                             "admitted by measured free HBM",
                    "peak_workers": srv_stats["peak_workers"], "peak_in_flight": srv_stats["peak_in_flight"],
                    "mix": "207 shards, 23 families, 2^8..2^22 rows (even), 4-16 columns",
                    "account": {
