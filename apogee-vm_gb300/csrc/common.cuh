@@ -81,7 +81,7 @@ struct SrsTable {
 enum ScratchSlot {
   S_ENTRIES, S_SORTED, S_COUNTS, S_OFFSETS, S_SCANBLK, S_BUCKETS, S_HEAD, S_TAIL, S_FLAGS, S_LEVEL_A,
   S_LEVEL_B, S_LEVEL_T, S_TSUM, S_RESULT, S_BASES, S_SCALARS, S_TMP0, S_TMP1, S_TMP2, S_TMP3, S_TMP4,
-  S_TMP5, S_TMP6, S_TMP7, S_ROUND, S_PAIR_A, S_PAIR_B, S_PAIR_PP, S_PAIR_CNT, S_COUNT
+  S_TMP5, S_TMP6, S_TMP7, S_ROUND, S_PAIR_A, S_PAIR_B, S_PAIR_PP, S_PAIR_CNT, S_PAIR_TERMS, S_COUNT
 };
 
 // Per-kernel CUDA-event timers (ids are public: APG_TIMER_* in the header).

@@ -468,8 +468,10 @@ int gkr_prove_impl(Ctx& c, const uint8_t* blob, size_t blob_len, GkrValues* V, c
     }
     std::vector<std::array<F, 4>> rounds;
     std::vector<F> rho, finals;
+    HostPairTerms pairs;
+    const bool by_pairs = pair_terms_of(hp, (int)src.size(), pairs);
     run_sumcheck(c, P, (int)src.size(), vkinds, (int)L.cached.size(), src, point, tr, rounds, rho, finals,
-                 src_bits);
+                 src_bits, by_pairs ? &pairs : nullptr);
     // L3.
     std::vector<F> claims;
     if (L.halving) {

@@ -683,8 +683,11 @@ __global__ void __launch_bounds__(128, APG_ACC_MIN_BLOCKS) k_bucket_acc(const ui
 // output would not fit the scratch sets *mode = 1 and every later step takes
 // the references instead.
 
+// Four rounds (a bucket's run cut to a sixteenth before the XYZZ tail):
+// measured 1.2 % faster on the 2^22 commit than three; the fourth round's
+// lists are short, but its pair sums still replace XYZZ additions.
 #ifndef APG_PAIR_ROUNDS
-#define APG_PAIR_ROUNDS 3
+#define APG_PAIR_ROUNDS 4
 #endif
 constexpr int kPairRounds = APG_PAIR_ROUNDS;
 // Lists shorter than this per group are left to the XYZZ kernel alone (the
@@ -720,7 +723,15 @@ enum : int { kPairFirst = 0, kPairSecond = 1, kPairInf = 2, kPairAdd = 3, kPairD
 // The pair rounds' products are inlined (unlike the XYZZ formulas, whose ten
 // inlined products a step overflowed the instruction cache): the compiler
 // interleaves the independent ones, measured 2 % faster than calls.
+// APG_PAIR_CALLS=1 makes them out-of-line calls instead (a build knob for
+// measurement).
+#ifndef APG_PAIR_CALLS
+#define APG_PAIR_CALLS 0
+#endif
+__device__ __forceinline__ Fq pmul(const Fq& a, const Fq& b) { return APG_PAIR_CALLS ? cmul(a, b) : fe_mul(a, b); }
+__device__ __forceinline__ Fq psqr(const Fq& a) { return APG_PAIR_CALLS ? csqr(a) : fe_sqr(a); }
 __device__ __forceinline__ Fq2 pmul2(const Fq& a, const Fq& b, const Fq& c, const Fq& d) {
+  if (APG_PAIR_CALLS) return cmul2(a, b, c, d);
   Fq2 r;
   r.a = fe_mul(a, b);
   r.b = fe_mul(c, d);
@@ -919,7 +930,7 @@ __device__ __forceinline__ void pair_load(const uint32_t* refs, const Affine* sr
     t.num = fe_sub(p1.y, p0.y);
   } else if (t.kind == kPairDbl) {
     t.d = fe_add(p0.y, p0.y);
-    const Fq q = fe_sqr(p0.x);
+    const Fq q = psqr(p0.x);
     t.num = fe_add(q, fe_add(q, q));
   }
 }
@@ -938,16 +949,19 @@ __device__ __forceinline__ void pair_store(const uint32_t* refs, const Affine* s
     y = fe_zero<FqConsts>();
   } else if (t.kind != kPairFirst) {
     x = fe_sub(fe_sub(l2, t.x0), t.x1);
-    y = fe_sub(fe_mul(lam, fe_sub(t.x0, x)), t.y0);
+    y = fe_sub(pmul(lam, fe_sub(t.x0, x)), t.y0);
   }
   st_fe(&dst->x, x);
   st_fe(&dst->y, y);
 }
 
-// Resident blocks a SM for the two halves of a round (the backward half holds
-// a slot's two points, its running inverse and the slope: about 96 registers).
+// Resident blocks a SM for the backward half of a round (it holds a slot's two
+// points, its running inverse and the slope): six blocks cap it at 80
+// registers with a few bytes spilled, measured 1 % faster on the headline
+// step than five at 92 registers; seven (72 registers) spilled more and was
+// slower.
 #ifndef APG_PAIR_MIN_BLOCKS
-#define APG_PAIR_MIN_BLOCKS 5
+#define APG_PAIR_MIN_BLOCKS 6
 #endif
 // The slots of a pair round. A warp owns 32 * m consecutive output slots and
 // lane l takes slots base + 32 j + l, so the lanes' references, explicit input
@@ -1024,8 +1038,8 @@ __global__ void __launch_bounds__(kPairThreads, APG_PAIR_MIN_BLOCKS)
     }
     const Fq2 di = pmul2(inv, ld_fe(&pp[j * T + s]), inv, t.d);  // 1/d, and the running inverse one back
     inv = di.b;
-    const Fq lam = fe_mul(t.num, di.a);
-    pair_store<REFS>(refs, src, t, lam, fe_sqr(lam), &out[o]);
+    const Fq lam = pmul(t.num, di.a);
+    pair_store<REFS>(refs, src, t, lam, psqr(lam), &out[o]);
   }
 }
 

@@ -217,6 +217,74 @@ __global__ void __launch_bounds__(kRoundThreads, APG_ROUND_MIN_BLOCKS)
   round_total(A, partials, red);
 }
 
+// A summand S = sum_j c_j T_{a_j} T_{b_j} over data tables only (halving
+// lists of tree gates, a zerocheck's product gate): thread per pair, each
+// term's two lines read (and folded with the previous challenge) straight
+// into registers and multiplied at the round's nodes, with no operand slots
+// and no interpreter. Tables no term reads are folded too, so every table
+// is bound each round as the generic kernel binds it.
+struct PairTerms {
+  const uint16_t* a;
+  const uint16_t* b;
+  const Fr* c;
+  const uint8_t* unit;  // c_j == 1: its product is skipped
+  const uint16_t* rest;
+  int n, nrest;
+};
+
+// Four resident blocks a SM (128 registers a thread, no spills): the
+// two-table zerocheck's rounds take 16 % less time than at the compiler's
+// choice (166 registers, three blocks).
+#ifndef APG_PAIRS_MIN_BLOCKS
+#define APG_PAIRS_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(kRoundThreads, APG_PAIRS_MIN_BLOCKS) k_round_pairs(RoundArgs A, PairTerms T, Fr* partials) {
+  __shared__ Fr red[kRoundThreads];
+  const bool n1 = (A.nodes >> 1) & 1;
+  Fr acc0 = fe_zero<FrConsts>(), acc1 = fe_zero<FrConsts>(), acc2 = fe_zero<FrConsts>();
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < A.npairs; i += stride) {
+    Fr lo, hi;
+    for (int r = 0; r < T.nrest; ++r) load_line(A, T.rest[r], i, lo, hi);
+    Fr s0 = fe_zero<FrConsts>(), s1 = fe_zero<FrConsts>(), s2 = fe_zero<FrConsts>();
+    for (int j = 0; j < T.n; ++j) {
+      Fr alo, ahi, blo, bhi;
+      load_line(A, T.a[j], i, alo, ahi);
+      load_line(A, T.b[j], i, blo, bhi);
+      Fr p0 = rmul(alo, blo);
+      Fr p2 = rmul(fe_sub(fe_add(ahi, ahi), alo), fe_sub(fe_add(bhi, bhi), blo));  // the lines at X = 2
+      Fr p1 = n1 ? rmul(ahi, bhi) : fe_zero<FrConsts>();
+      if (!T.unit[j]) {
+        const Fr cj = ld_fe(&T.c[j]);
+        p0 = rmul(cj, p0);
+        p2 = rmul(cj, p2);
+        if (n1) p1 = rmul(cj, p1);
+      }
+      s0 = fe_add(s0, p0);
+      s2 = fe_add(s2, p2);
+      if (n1) s1 = fe_add(s1, p1);
+    }
+    Fr e_lo, e_hi;
+    load_line(A, A.nd, i, e_lo, e_hi);
+    const Fr w = fe_add(e_lo, e_hi);  // the pair's eq weight without the current variable's factor
+    acc0 = fe_add(acc0, rmul(w, s0));
+    acc2 = fe_add(acc2, rmul(w, s2));
+    if (n1) acc1 = fe_add(acc1, rmul(w, s1));
+  }
+  const Fr accs[4] = {acc0, acc1, acc2, fe_zero<FrConsts>()};
+  for (int x = 0; x < 4; ++x) {
+    red[threadIdx.x] = accs[x];
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+      if (threadIdx.x < (unsigned)off) red[threadIdx.x] = fe_add(red[threadIdx.x], red[threadIdx.x + off]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) st_fe(&partials[(size_t)blockIdx.x * 4 + x], red[0]);
+    __syncthreads();
+  }
+  round_total(A, partials, red);
+}
+
 // Wide gate lists (many gates, many tables): one warp per pair. The pair's
 // tables sit once in the warp's shared slots (values, then cached entries,
 // then steps, then eq's value and step), written lane-parallel; at each node
@@ -408,7 +476,7 @@ static VirtualRound virtual_round(const std::vector<F>& point, int nvars) {
 void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint8_t>& vkinds, int n_cached,
                   const std::vector<const Fr*>& src, const std::vector<F>& eq_point, host::Transcript& tr,
                   std::vector<std::array<F, 4>>& rounds, std::vector<F>& point, std::vector<F>& finals,
-                  const std::vector<uint8_t>& src_bits) {
+                  const std::vector<uint8_t>& src_bits, const HostPairTerms* pairs) {
   const int n = (int)eq_point.size();
   const int nt = nd + 1;  // with eq
   if (vkinds.size() > 8) throw Error(APG_ERR_BAD_CIRCUIT, "more than 8 virtual tables");
@@ -470,6 +538,35 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
   F* sums = reinterpret_cast<F*>(c.host_pinned());
   DevProgram P = prog;
   P.cached_slot0 = n_val;
+  // The pair-term kernel's tables on the device (when the summand has that form).
+  PairTerms PT;
+  memset(&PT, 0, sizeof(PT));
+  const bool use_pairs = pairs && vkinds.empty() && n_cached == 0 && !pairs->a.empty();
+  if (use_pairs) {
+    const size_t nt_ = pairs->a.size(), nr = pairs->rest.size();
+    const size_t cb = 32 * nt_, ab = 2 * nt_, rb = 2 * std::max<size_t>(nr, 1), ub = nt_;
+    const size_t total = cb + 2 * ab + rb + ub + 4 * 32;
+    uint8_t* d = c.scratch[S_PAIR_TERMS].as<uint8_t>(total);
+    std::vector<uint8_t> h(total, 0);
+    size_t off = 0;
+    auto put = [&](const void* p, size_t n) {
+      const size_t at = (off + 31) & ~(size_t)31;
+      if (n) memcpy(h.data() + at, p, n);
+      off = at + n;
+      return d + at;
+    };
+    std::vector<uint8_t> unit(nt_);
+    for (size_t j = 0; j < nt_; ++j) unit[j] = pairs->c[j] == host::fone() ? 1 : 0;
+    PT.c = reinterpret_cast<const Fr*>(put(pairs->c.data(), cb));
+    PT.a = reinterpret_cast<const uint16_t*>(put(pairs->a.data(), ab));
+    PT.b = reinterpret_cast<const uint16_t*>(put(pairs->b.data(), ab));
+    PT.rest = reinterpret_cast<const uint16_t*>(put(pairs->rest.data(), 2 * nr));
+    PT.unit = put(unit.data(), ub);
+    PT.n = (int)nt_;
+    PT.nrest = (int)nr;
+    APG_CUDA(cudaMemcpyAsync(d, h.data(), total, cudaMemcpyHostToDevice, c.stream));
+    APG_CUDA(cudaStreamSynchronize(c.stream));  // `h` is a host temporary
+  }
 
   // 1/r_j for every nonzero eq coordinate, from one inversion (Montgomery's
   // batch trick): the rounds divide by their coordinate.
@@ -524,7 +621,11 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
                                                    (size_t)warp_max_blocks)
                            : (int)std::min<size_t>((work + threads - 1) / threads, (size_t)max_blocks);
     cudaEvent_t t0 = c.timer_begin();
-    if (warp_mode) launch(c, k_round_warp, blocks, kRoundThreads, warp_smem, A, P, V, partials);
+    if (use_pairs && !A.xsplit)
+      launch(c, k_round_pairs, (int)std::min<size_t>((A.npairs + kRoundThreads - 1) / kRoundThreads,
+                                                     (size_t)c.sm_count * 8),
+             kRoundThreads, 0, A, PT, partials);
+    else if (warp_mode) launch(c, k_round_warp, blocks, kRoundThreads, warp_smem, A, P, V, partials);
     else launch(c, k_round, blocks, threads, smem, A, P, V, partials);
     c.timer_end(APG_TIMER_SUMCHECK_ROUND, t0);
     APG_CUDA(cudaMemcpyAsync(sums, d_out, 128, cudaMemcpyDeviceToHost, c.stream));
@@ -718,6 +819,66 @@ bool linearize(HostProgram& hp) {
 }
 
 }  // namespace
+
+bool pair_terms_of(const HostProgram& hp, int nd, HostPairTerms& out) {
+  out = HostPairTerms();
+  if (hp.n_cached != 0 || hp.n_weighted <= 0) return false;
+  const F one = host::fone(), zero = host::fzero();
+  // Terms over the same two tables merge (exact arithmetic: the sum is the
+  // same at every node).
+  std::map<std::pair<uint16_t, uint16_t>, F> merged;
+  auto term = [&](uint16_t a, uint16_t b, const F& cf) {
+    if (a >= nd || b >= nd) return false;
+    const auto k = a < b ? std::make_pair(a, b) : std::make_pair(b, a);
+    auto it = merged.find(k);
+    if (it == merged.end()) merged.emplace(k, cf);
+    else it->second = host::fadd(it->second, cf);
+    return true;
+  };
+  for (int j = 0; j < hp.n_weighted; ++j) {
+    const DevGate& g = hp.gates[j];
+    const F W = j < (int)hp.weights.size() ? hp.weights[j] : one;
+    const uint16_t* op = hp.ops.data() + g.op_off;
+    const F* cf = hp.coeffs.data() + g.cf_off;
+    bool ok = false;
+    switch (g.kind) {
+      case G_TREE_PRODUCT:  // v0 v1
+        ok = g.nops == 2 && term(op[0], op[1], W);
+        break;
+      case G_PRODUCT:  // c v0 v1
+        ok = g.nops == 2 && term(op[0], op[1], host::fmul(cf[0], W));
+        break;
+      case G_TREE_CROSS:  // v0 v3 + v1 v2
+        ok = g.nops == 4 && term(op[0], op[3], W) && term(op[1], op[2], W);
+        break;
+      case G_QUADRATIC:  // c0 + linear + products: products only
+        ok = g.p1 == 0 && cf[0] == zero && g.nops == 2 * g.p2;
+        for (uint32_t u = 0; ok && u < g.p2; ++u) ok = term(op[2 * u], op[2 * u + 1], host::fmul(cf[1 + u], W));
+        break;
+      default:
+        ok = false;
+    }
+    if (!ok) {
+      out = HostPairTerms();
+      return false;
+    }
+  }
+  for (auto& kv : merged) {
+    if (kv.second == zero) continue;
+    out.a.push_back(kv.first.first);
+    out.b.push_back(kv.first.second);
+    out.c.push_back(kv.second);
+  }
+  if (out.a.empty() || out.a.size() > 4096) {
+    out = HostPairTerms();
+    return false;
+  }
+  std::vector<char> used(nd, 0);
+  for (size_t j = 0; j < out.a.size(); ++j) used[out.a[j]] = used[out.b[j]] = 1;
+  for (int k = 0; k < nd; ++k)
+    if (!used[k]) out.rest.push_back((uint16_t)k);
+  return true;
+}
 
 void upload_program(Ctx& c, const HostProgram& hp_in, DevProgram& P, int slot_cap) {
   (void)slot_cap;

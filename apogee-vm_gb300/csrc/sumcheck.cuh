@@ -71,10 +71,24 @@ void build_eq_table(Ctx& c, const std::vector<host::F>& r, Fr* out);
 // `src_bits` (empty: every table Fr) gives each data table's stored width;
 // narrow tables are read through the lift in the first two rounds and the
 // first bind writes Fr (the lazy lift of crates/poly/src/lib.rs:156-185).
+// A summand that is a weighted sum of products of two data tables,
+// S = sum_j c_j T_{a_j} T_{b_j} (halving lists of TreeProduct / TreeCross
+// gates, a zerocheck's product gate): the round kernel for it reads each
+// term's two lines and multiplies, with no interpreter between. `rest` lists
+// the data tables no term reads (they are still bound every round).
+struct HostPairTerms {
+  std::vector<uint16_t> a, b, rest;
+  std::vector<host::F> c;
+};
+// The program's terms, when every weighted gate is such a product of data
+// tables (slots below nd) and nothing is cached; false otherwise.
+bool pair_terms_of(const HostProgram& hp, int nd, HostPairTerms& out);
+
 void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint8_t>& vkinds, int n_cached,
                   const std::vector<const Fr*>& src, const std::vector<host::F>& eq_point, host::Transcript& tr,
                   std::vector<std::array<host::F, 4>>& rounds, std::vector<host::F>& point,
-                  std::vector<host::F>& finals, const std::vector<uint8_t>& src_bits = {});
+                  std::vector<host::F>& finals, const std::vector<uint8_t>& src_bits = {},
+                  const HostPairTerms* pairs = nullptr);
 
 // `bits` (null: all Fr) is each table's stored width.
 int prove_zerocheck_impl(Ctx& c, size_t arity, const uint8_t* coefs, const uint32_t* ta, const uint32_t* tb,

@@ -114,7 +114,9 @@ int prove_zerocheck_impl(Ctx& c, size_t arity, const uint8_t* coefs, const uint3
   upload_program(c, hp, P, 0);
   std::vector<std::array<F, 4>> rounds;
   std::vector<F> point, finals;
-  run_sumcheck(c, P, (int)arity, {}, 0, src, r, tr, rounds, point, finals, src_bits);
+  HostPairTerms pairs;
+  const bool by_pairs = pair_terms_of(hp, (int)arity, pairs);
+  run_sumcheck(c, P, (int)arity, {}, 0, src, r, tr, rounds, point, finals, src_bits, by_pairs ? &pairs : nullptr);
   for (auto& f : finals)
     if (!host::below_p(f.w)) throw Error(APG_ERR_INTERNAL, "non-canonical device value");
   tr.absorb(host::T_SUMCHECK_FINAL_EVALS, finals);
