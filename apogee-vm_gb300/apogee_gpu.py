@@ -577,7 +577,8 @@ class _CShard(ctypes.Structure):
                 ("cols", ctypes.POINTER(ctypes.c_void_p)), ("n_cols", ctypes.c_size_t),
                 ("cols_on_device", ctypes.c_int), ("num_vars", ctypes.c_size_t),
                 ("statement_digest", ctypes.c_char_p), ("family", ctypes.c_uint32), ("index", ctypes.c_uint32),
-                ("ts_lo", ctypes.c_uint64), ("ts_hi", ctypes.c_uint64)]
+                ("ts_lo", ctypes.c_uint64), ("ts_hi", ctypes.c_uint64), ("ext_slots", ctypes.c_void_p),
+                ("ext_values", ctypes.c_char_p), ("n_ext", ctypes.c_size_t), ("decoder_width", ctypes.c_uint32)]
 
 
 class _CShardProof(ctypes.Structure):
@@ -611,7 +612,11 @@ class Shard:
     (verifier_core::shard_transcript)."""
 
     def __init__(self, circuit: bytes, cols, num_vars: int, digest: int, family: int, index: int, ts_lo: int,
-                 ts_hi: int, on_device: bool = True):
+                 ts_hi: int, on_device: bool = True, ext=None, decoder_width: int = 0):
+        """`ext`: {slot: value} for the statement-level challenge slots the
+        circuit reads (the memory challenges 1-4, a window's constant 5);
+        `decoder_width`: the circuit's decoder lookup tuple width (0 if it
+        has no decoder channel). The shard draws g and beta itself."""
         self.circuit = bytes(circuit)
         self.cols = list(cols)  # keeps host buffers alive
         self.num_vars = num_vars
@@ -622,8 +627,13 @@ class Shard:
             ptrs = [ctypes.cast(h, ctypes.c_void_p).value for h in self._host]
         self._ptrs = (ctypes.c_void_p * len(ptrs))(*ptrs)
         self._digest = to_mont_bytes([digest])
+        ext = dict(ext or {})
+        self._ext_slots = (ctypes.c_uint32 * max(len(ext), 1))(*sorted(ext))
+        self._ext_values = to_mont_bytes([ext[k] for k in sorted(ext)]) if ext else b""
         self.c = _CShard(self.circuit, len(self.circuit), ctypes.cast(self._ptrs, ctypes.POINTER(ctypes.c_void_p)),
-                         len(self.cols), 1 if on_device else 0, num_vars, self._digest, family, index, ts_lo, ts_hi)
+                         len(self.cols), 1 if on_device else 0, num_vars, self._digest, family, index, ts_lo, ts_hi,
+                         ctypes.cast(self._ext_slots, ctypes.c_void_p), self._ext_values or None, len(ext),
+                         decoder_width)
 
 
 class ShardProof:

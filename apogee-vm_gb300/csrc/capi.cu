@@ -917,6 +917,15 @@ static int prove_shard_common(Ctx& c, const apg_shard* sh, apg_shard_proof* out)
   if (!host::below_p(digest.w)) return APG_ERR_NONCANONICAL;
   for (size_t j = 0; j < k; ++j)
     if (!sh->cols[j]) return APG_ERR_INVALID_ARGUMENT;
+  if (sh->decoder_width > 7 || (sh->n_ext && (!sh->ext_slots || !sh->ext_values)) || sh->n_ext > 64)
+    return APG_ERR_INVALID_ARGUMENT;
+  for (size_t e = 0; e < sh->n_ext; ++e) {
+    const uint32_t sl = sh->ext_slots[e];
+    if (sl == 0 || (sl >= 6 && sl <= 13)) return APG_ERR_INVALID_ARGUMENT;  // drawn by the shard itself
+    for (size_t f = 0; f < e; ++f)
+      if (sh->ext_slots[f] == sl) return APG_ERR_INVALID_ARGUMENT;
+    if (!host::below_p(reinterpret_cast<const uint64_t*>(sh->ext_values + 32 * e))) return APG_ERR_NONCANONICAL;
+  }
   std::vector<const void*> d_cols(sh->cols, sh->cols + k);
   Fr* staged = nullptr;
   auto t0 = Clock::now();
@@ -949,21 +958,47 @@ static int prove_shard_common(Ctx& c, const apg_shard* sh, apg_shard_proof* out)
   tr.absorb(40, window, 2);  // SHARD_TS_WINDOW
   tr.absorb_g1(host::T_COMMITMENT, out->cms, k);
   const host::F g = tr.challenge(33), beta = tr.challenge(33);  // LOOKUP_CHALLENGE
-  const uint32_t slots[2] = {0, 1};
-  uint8_t slot_values[64];
-  memcpy(slot_values, g.w, 32);
-  memcpy(slot_values + 32, beta.w, 32);
+  // verifier_core::shard_challenges: the statement's slots from the caller,
+  // then insert_lookup_challenges (crates/gkr-verify/src/lookup.rs:28-61).
+  std::vector<uint32_t> slots;
+  std::vector<uint8_t> slot_values;
+  auto put = [&](uint32_t slot, const host::F& v) {
+    slots.push_back(slot);
+    slot_values.insert(slot_values.end(), (const uint8_t*)v.w, (const uint8_t*)v.w + 32);
+  };
+  put(0, g);  // the test circuits' one challenge
+  put(6, g);  // LOOKUP_G
+  host::F power = beta;
+  for (uint32_t j = 0; j < 6; ++j) {  // LOOKUP_BETA .. LOOKUP_BETA_6
+    put(7 + j, power);
+    power = host::fmul(power, beta);
+  }
+  if (sh->decoder_width > 0) {  // LOOKUP_DECODER_NEUTRAL = g - sum_{j<W} beta^j
+    host::F sum = host::fzero(), pw = host::fone();
+    for (uint32_t j = 0; j < sh->decoder_width; ++j) {
+      sum = host::fadd(sum, pw);
+      pw = host::fmul(pw, beta);
+    }
+    put(13, host::fsub(g, sum));
+  }
+  for (size_t e = 0; e < sh->n_ext; ++e) {
+    host::F v;
+    memcpy(v.w, sh->ext_values + 32 * e, 32);
+    put(sh->ext_slots[e], v);
+  }
   uint8_t snap[226];
   tr.save(snap);
 
   auto t1 = Clock::now();
   std::unique_ptr<GkrValues, void (*)(GkrValues*)> V(
-      gkr_forward_impl(c, sh->circuit, sh->circuit_len, d_cols.data(), nullptr, true, slots, slot_values, 2),
+      gkr_forward_impl(c, sh->circuit, sh->circuit_len, d_cols.data(), nullptr, true, slots.data(),
+                       slot_values.data(), slots.size()),
       gkr_values_free);
   APG_CUDA(cudaStreamSynchronize(c.stream));
   out->phase_ms[1] = ms_since(t1);
   auto t2 = Clock::now();
-  st = gkr_prove_impl(c, sh->circuit, sh->circuit_len, V.get(), slots, slot_values, 2, snap, out->gkr_proof,
+  st = gkr_prove_impl(c, sh->circuit, sh->circuit_len, V.get(), slots.data(), slot_values.data(), slots.size(), snap,
+                      out->gkr_proof,
                       out->gkr_cap, &out->gkr_len, out->point);
   if (st) return st;
   V.reset();
@@ -1002,6 +1037,13 @@ size_t apg_shard_device_bytes(const apg_shard* sh) {
 }
 
 int apg_ctx_device(apg_ctx* ctx) { return ctx ? ctx->c.device : -1; }
+
+size_t apg_abi_sizes(size_t* out, size_t n) {
+  const size_t sizes[5] = {sizeof(apg_shard), sizeof(apg_shard_proof), sizeof(apg_request_times),
+                           sizeof(apg_server_stats), sizeof(apg_server_config)};
+  for (size_t i = 0; out && i < n && i < 5; ++i) out[i] = sizes[i];
+  return 5;
+}
 
 size_t apg_ctx_device_bytes(apg_ctx* ctx) {
   if (!ctx) return 0;

@@ -234,7 +234,8 @@ struct PairTerms {
 
 // Four resident blocks a SM (128 registers a thread, no spills): the
 // two-table zerocheck's rounds take 16 % less time than at the compiler's
-// choice (166 registers, three blocks).
+// choice (166 registers, three blocks); five and six spill. The products are
+// the interpreter's out-of-line rmul: inlined, the rounds took 15 % longer.
 #ifndef APG_PAIRS_MIN_BLOCKS
 #define APG_PAIRS_MIN_BLOCKS 4
 #endif

@@ -11,6 +11,10 @@ Workloads:
   * `shard_mix`: 207 shards over 23 circuit families, sizes log-uniform over
     the even heights 2^8 .. 2^22 (Mercury takes even variable counts only),
     4 to 16 columns each, values drawn like VM trace columns.
+  * `family_mix`: 207 shards over 23 families proved with the reference's
+    own family circuits (its committed artifacts, decoded), the 13 artifacts
+    cycled over the families, each shard committing every column its
+    circuit's base layer reads (28 to 96).
   * `prove_sequential`: one shard at a time on one context (the plain path).
   * `prove_batched`: every shard submitted at once to the library's server
     (apg_server, continuous batching with admission by measured free HBM),
@@ -124,14 +128,87 @@ def shard_transcript(spec, cms):
     return tr, g, beta
 
 
-def make_shard(spec, cols, blob=None):
+# The 13 production family circuits among the reference's committed
+# artifacts (crates/constraints/tests/vectors/*.bin; the toy circuits left out).
+FAMILY_ARTIFACTS = ["add_sub", "atomics", "image_window", "jump_branch_slt", "mem_subword", "mem_word",
+                    "memory_frame_alu", "memory_frame_atomics", "memory_frame_mem", "memory_frame_reg", "mul_div",
+                    "shift_bitwise", "zero_window"]
+DECODER_CHANNEL = 3  # constants::lookup_channel::DECODER
+_families = {}
+
+
+def family_circuit(artifact_dir: str, name: str, log_rows: int):
+    """A family artifact over 2^log_rows rows: (APGC blob, committed columns,
+    decoder tuple width)."""
+    import os
+
+    import artifact
+
+    key = (artifact_dir, name, log_rows)
+    if key not in _families:
+        with open(os.path.join(artifact_dir, name + ".bin"), "rb") as f:
+            art = artifact.decode(f.read())
+        circ = artifact.to_circuit(art, log_rows)
+        width = max([len(lk[3]) for lk in art["lookups"] if lk[1] == DECODER_CHANNEL] or [0])
+        _families[key] = (circ.to_blob(), circ.n_committed, width)
+    return _families[key]
+
+
+def statement_challenges(seed: int = 0x57A7E):
+    """Stand-ins for the statement-level challenge slots a family circuit
+    reads (the memory challenges gamma_M, alpha_addr, alpha_ts, alpha_val in
+    slots 1-4, drawn once per statement by the global phase, and a window
+    shard's constant in slot 5): seeded, one set for the whole statement."""
+    rng = random.Random(seed)
+    return {slot: rng.randrange(C.P_R) for slot in (1, 2, 3, 4, 5)}
+
+
+def shard_challenges(g: int, beta: int, decoder_width: int = 0, ext=None):
+    """Every challenge slot the shard prover sets: the caller's statement
+    slots, slot 0 (the test circuits' one challenge) and slot 6 = g, slots
+    7-12 = beta^1..beta^6, and slot 13 = g - sum_{j<W} beta^j for a decoder
+    channel of width W (gkr_verify::insert_lookup_challenges,
+    crates/gkr-verify/src/lookup.rs:28-61)."""
+    p = C.P_R
+    ch = dict(ext or {})
+    ch[0] = g
+    ch[6] = g
+    for j in range(6):
+        ch[7 + j] = pow(beta, j + 1, p)
+    if decoder_width:
+        ch[13] = (g - sum(pow(beta, j, p) for j in range(decoder_width))) % p
+    return ch
+
+
+def family_mix(count: int = 207, seed: int = 20261204, sizes=(8, 10, 12, 14, 16)):
+    """`count` shards over 23 families, family f proved with artifact
+    FAMILY_ARTIFACTS[f % 13], sizes drawn uniformly from `sizes` (log2 of
+    the rows); `cols` is filled in from the circuit when it is built."""
+    rng = random.Random(seed)
+    return [{"index": i, "family": i % FAMILIES, "log_rows": rng.choice(sizes),
+             "artifact": FAMILY_ARTIFACTS[(i % FAMILIES) % len(FAMILY_ARTIFACTS)]} for i in range(count)]
+
+
+def spec_circuit(spec, artifact_dir=None):
+    """(blob, decoder width, statement challenges) of a spec: its family
+    artifact when it names one, else the synthetic shard circuit."""
+    if spec.get("artifact"):
+        blob, ncols, width = family_circuit(artifact_dir, spec["artifact"], spec["log_rows"])
+        spec.setdefault("cols", ncols)
+        return blob, width, statement_challenges()
+    return shard_circuit(spec["log_rows"], spec["cols"]), 0, None
+
+
+def make_shard(spec, cols, blob=None, artifact_dir=None):
     """The library's shard request for `spec` over device columns `cols`:
-    its circuit (the synthetic shard circuit unless `blob` is given) and its
-    transcript seed (statement digest, family, index, time window)."""
+    its circuit (the spec's family artifact, else the synthetic shard circuit,
+    unless `blob` is given), the statement-level challenges a family circuit
+    reads, and its transcript seed (statement digest, family, index, time
+    window)."""
     lo = spec["index"] << 22
-    return A.Shard(blob or shard_circuit(spec["log_rows"], spec["cols"]), [t.data_ptr() for t in cols],
-                   spec["log_rows"], statement_digest(spec), spec["family"], spec["index"], lo,
-                   lo + (1 << spec["log_rows"]))
+    own, width, ext = spec_circuit(spec, artifact_dir)
+    return A.Shard(blob or own, [t.data_ptr() for t in cols], spec["log_rows"], statement_digest(spec),
+                   spec["family"], spec["index"], lo, lo + (1 << spec["log_rows"]), ext=ext, decoder_width=width)
 
 
 def _as_dict(p):
@@ -139,22 +216,22 @@ def _as_dict(p):
             "transcript": p.transcript, "phase_ms": p.phase_ms}
 
 
-def prove_shard(ctx, spec, cols, blob=None):
+def prove_shard(ctx, spec, cols, blob=None, artifact_dir=None):
     """One shard through the library's shard prover (apg_prove_shard): the
     commitments, the GKR proof, the base point, the opened values, the
     opening proof and the transcript after it."""
-    return _as_dict(ctx.prove_shard(make_shard(spec, cols, blob)))
+    return _as_dict(ctx.prove_shard(make_shard(spec, cols, blob, artifact_dir)))
 
 
-def prove_shard_composed(ctx, spec, cols):
+def prove_shard_composed(ctx, spec, cols, artifact_dir=None):
     """The same shard from the library's separate entry points, the schedule
     driven from here: what apg_prove_shard must reproduce."""
     n_vars = spec["log_rows"]
     ptrs = [t.data_ptr() for t in cols]
     cms = ctx.commit_batch_device(ptrs, n_vars)
     tr, g, beta = shard_transcript(spec, cms)
-    blob = shard_circuit(n_vars, spec["cols"])
-    ch = {0: g, 1: beta}
+    blob, width, ext = spec_circuit(spec, artifact_dir)
+    ch = shard_challenges(g, beta, width, ext)
     values = ctx.gkr_forward(blob, ptrs, ch, on_device=True)
     proof, tr, point = ctx.gkr_prove(blob, values, ch, tr, with_point=True)
     values.free()
@@ -163,19 +240,21 @@ def prove_shard_composed(ctx, spec, cols):
     return {"cms": cms, "gkr": proof, "point": u, "vs": vs, "opening": opening, "transcript": tr}
 
 
-def prove_sequential(ctx, specs, columns, blobs=None):
+def prove_sequential(ctx, specs, columns, blobs=None, artifact_dir=None):
     """One shard at a time on one context (the plain path)."""
     t0 = time.perf_counter()
-    outs = {s["index"]: prove_shard(ctx, s, columns[s["index"]], (blobs or {}).get(s["index"])) for s in specs}
+    outs = {s["index"]: prove_shard(ctx, s, columns[s["index"]], (blobs or {}).get(s["index"]), artifact_dir)
+            for s in specs}
     return time.perf_counter() - t0, outs
 
 
-def prove_batched(server, specs, columns, blobs=None):
+def prove_batched(server, specs, columns, blobs=None, artifact_dir=None):
     """Every shard submitted at once to the library's server, largest first;
     it admits them as workers and memory allow and runs them side by side."""
     order = sorted(specs, key=lambda s: -(s["cols"] << s["log_rows"]))
     t0 = time.perf_counter()
-    tickets = {s["index"]: server.submit(make_shard(s, columns[s["index"]], (blobs or {}).get(s["index"])))
+    tickets = {s["index"]: server.submit(make_shard(s, columns[s["index"]], (blobs or {}).get(s["index"]),
+                                                    artifact_dir))
                for s in order}
     outs, times = {}, {}
     for i, t in tickets.items():
@@ -184,7 +263,7 @@ def prove_batched(server, specs, columns, blobs=None):
     return time.perf_counter() - t0, outs, times
 
 
-def serve(server, specs, columns, rate: float, seed: int = 7, blobs=None):
+def serve(server, specs, columns, rate: float, seed: int = 7, blobs=None, artifact_dir=None):
     """A seeded Poisson stream of shard requests at `rate` a second, in the
     order of `specs`, submitted to the library's server as they arrive.
     Returns (wall seconds, sorted latencies in seconds, each shard's proof by
@@ -201,7 +280,8 @@ def serve(server, specs, columns, rate: float, seed: int = 7, blobs=None):
         delay = at - (time.perf_counter() - start)
         if delay > 0:
             time.sleep(delay)
-        tickets[s["index"]] = server.submit(make_shard(s, columns[s["index"]], (blobs or {}).get(s["index"])))
+        tickets[s["index"]] = server.submit(make_shard(s, columns[s["index"]], (blobs or {}).get(s["index"]),
+                                                       artifact_dir))
     outs, times = {}, {}
     for i, tk in tickets.items():
         p, tm = server.wait(tk)

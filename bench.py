@@ -90,6 +90,22 @@ def own_windows(n, tuned=None):
     return -(-255 // c)
 
 
+def own_fqmul_accumulate(n, c, windows, pair_rounds=4):
+    """The library's own Fq-product count for one accumulation of n uniform
+    scalars at window width c: E = windows x n digits (a uniform digit is 0
+    with probability 2^-c) into K = 2^(c-1) shared buckets; every affine pair
+    round sums half of what is left (6 products a pair: one forward and two
+    backward products of the batched inversion, the slope, its square and
+    y3), and the XYZZ tail adds the remaining E / 2^rounds - K points at
+    8M + 2S each. Odd leftovers and the per-thread inversions are not counted,
+    so this is a lower bound on the products the kernels issue."""
+    E = windows * n
+    K = 1 << (c - 1)
+    pairs = sum(E / (2 << r) for r in range(pair_rounds))
+    tail = max(0.0, E / (1 << pair_rounds) - K)
+    return 6 * pairs + 10 * tail
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during a timed region."""
 
@@ -695,6 +711,32 @@ def run_shard_workloads(ctx, local, serve_budget_gb=150):
                    "median_attribution": shard.latency_attribution(srv_times, 0.5)}
     del columns
     torch.cuda.empty_cache()
+
+    # Config 4 over the reference's own family circuits: 207 shards, the 13
+    # production artifacts cycled over 23 families, 2^8..2^16 rows, each
+    # committing every column its circuit's base reads (2 to 96).
+    art_dir = os.path.join(ROOT, "tests", "golden", "artifacts")
+    fspecs = shard.family_mix(207)
+    for s_ in fspecs:
+        shard.spec_circuit(s_, art_dir)
+    fcols = {s_["index"]: shard.device_columns(torch, 1 << s_["log_rows"], s_["cols"], SEED + 700 + s_["index"], dev,
+                                               ctx) for s_ in fspecs}
+    torch.cuda.synchronize()
+    shard.prove_sequential(ctx, fspecs[:13], fcols, artifact_dir=art_dir)  # warm the circuits and scratch
+    fseq_t, _ = shard.prove_sequential(ctx, fspecs, fcols, artifact_dir=art_dir)
+    server = A.Server(ctx, hbm_budget=budget, max_workers=workers)
+    shard.prove_batched(server, fspecs[:24], fcols, artifact_dir=art_dir)  # warm the workers
+    fbat_t, _, _ = shard.prove_batched(server, fspecs, fcols, artifact_dir=art_dir)
+    fstats = server.stats()
+    server.close()
+    out["cfg4_families"] = {"shards": len(fspecs), "points": sum(s_["cols"] << s_["log_rows"] for s_ in fspecs),
+                            "sequential_shards_per_s": len(fspecs) / fseq_t,
+                            "batched_shards_per_s": len(fspecs) / fbat_t, "batched_over_sequential": fseq_t / fbat_t,
+                            "peak_in_flight": fstats["peak_in_flight"],
+                            "mix": "207 shards, the 13 production family artifacts over 23 families, "
+                                   "2^8..2^16 rows (even), 2-96 columns"}
+    del fcols
+    torch.cuda.empty_cache()
     return out
 
 
@@ -815,9 +857,13 @@ def run_gpu(args):
         hbm_gbs = traffic / (acc_ms / acc_n / 1e3) / 1e9
         hbm = {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
                "peak_source": f"{hbm_src} copy bandwidth", "basis": "the captured DRAM traffic over the phase's time"}
+    own_c = tuned.get(log2n) or 18
+    own = own_fqmul_accumulate(n, own_c, own_windows(n, tuned))
+    own_achieved = own / (acc_ms / acc_n / 1e3)
     roofline = {
         "bound": "int",
-        "kernel": f"bucket accumulation (k_pair_round x3 + k_bucket_acc), 2^{log2n} uniform scalars",
+        "kernel": f"bucket accumulation (k_pair_fwd + k_pair_bwd x4 rounds, k_bucket_acc), 2^{log2n} uniform "
+                  "scalars",
         "achieved": achieved / 1e9, "peak": fq_rate / 1e9, "unit": "G Fq-mul/s", "frac": achieved / fq_rate,
         "traffic": traffic, "hbm": hbm,
         "peak_source": "measured on this device in this run: dependency-free Fq Montgomery products on every SM",
@@ -826,9 +872,12 @@ def run_gpu(args):
         "algorithmic_basis": f"reference work: {reference_window_windows(n)[1]} windows x n mixed adds x 10 Fq-mul",
         "achieved_timad32_equiv": achieved * 264 / 1e12,
         "own_windows": own_windows(n, tuned),
-        "own_work": "affine pair sums (5M + 1S and a share of one inversion a thread) for the first three "
+        "own_work": "affine pair sums (5M + 1S and a share of one inversion a thread) for the first four "
                     "halvings of every bucket, mixed XYZZ adds (8M + 2S) for the rest: fewer products than "
                     "the reference basis, so frac may exceed 1",
+        "own_fqmul_per_launch": own, "own_achieved": own_achieved / 1e9, "own_frac": own_achieved / fq_rate,
+        "own_basis": "the library's own products (lower bound: odd leftovers and inversions not counted) over "
+                     "the same time and the same measured peak",
     }
 
     shards = None

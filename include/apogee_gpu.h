@@ -356,6 +356,23 @@ typedef struct apg_shard {
   const uint8_t* statement_digest;  /* 32 bytes, Fr in memory */
   uint32_t family, index;           /* the shard's family and index (u32 in the reference) */
   uint64_t ts_lo, ts_hi;            /* its timestamp window */
+  /* The challenge slots the circuit reads besides the ones the shard draws
+   * itself (verifier_core::shard_challenges,
+   * crates/verifier-core/src/statement.rs:616-635): n_ext (slot, value)
+   * pairs, values 32 bytes each (Fr in memory), for the statement's memory
+   * challenges (slots 1-4) and a window shard's constant (slot 5). The shard
+   * draws g and beta from its own transcript and sets slot 6 = g, slots 7-12
+   * = beta^1..beta^6 and, for a circuit with a decoder channel, slot 13 =
+   * g - sum_{j<W} beta^j (gkr_verify::insert_lookup_challenges,
+   * crates/gkr-verify/src/lookup.rs:28-61); slot 0, the test circuits' one
+   * challenge (read by no production circuit), is g as well. An external
+   * pair naming one of those slots, or a slot twice, is refused
+   * (APG_ERR_INVALID_ARGUMENT). The arrays must stay valid until the proof
+   * is done. */
+  const uint32_t* ext_slots;
+  const uint8_t* ext_values;
+  size_t n_ext;
+  uint32_t decoder_width;           /* W: the decoder lookup tuple's width, 0..7 (0: no decoder channel) */
 } apg_shard;
 
 /* Where a shard proof lands (caller-owned buffers, filled when it is done). */
@@ -370,6 +387,12 @@ typedef struct apg_shard_proof {
   uint8_t transcript[226];
   double phase_ms[4];   /* out: commit, forward, GKR proof, opening (host wall clock) */
 } apg_shard_proof;
+
+/* No reference counterpart: sizeof of the structs this header declares,
+ * for bindings to check their layouts against: apg_shard, apg_shard_proof,
+ * apg_request_times, apg_server_stats, apg_server_config, in that order.
+ * Writes min(n, 5) sizes; returns 5. */
+size_t apg_abi_sizes(size_t* out, size_t n);
 
 /* Prove one shard on the context (columns on its device or host). */
 int apg_prove_shard(apg_ctx* ctx, const apg_shard* shard, apg_shard_proof* out);

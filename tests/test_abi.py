@@ -54,3 +54,15 @@ def test_montgomery_encoding_round_trip():
     assert A.from_mont_bytes(A.to_mont_bytes(xs)) == xs
     # R itself is the in-memory form of one (crates/field/src/lib.rs:197).
     assert A.to_mont_bytes([1]) == A.R_MONT.to_bytes(32, "little")
+
+
+def test_binding_struct_layouts_match_the_header(built_lib):
+    """The ctypes mirrors of the header's structs have the C sizes (a field
+    added on one side only would shift every later field)."""
+    import apogee_gpu as A
+
+    built_lib.apg_abi_sizes.restype = ctypes.c_size_t
+    out = (ctypes.c_size_t * 5)()
+    assert built_lib.apg_abi_sizes(out, ctypes.c_size_t(5)) == 5
+    mirrors = [A._CShard, A._CShardProof, A._CTimes, A._CStats, A._CServerConfig]
+    assert list(out) == [ctypes.sizeof(m) for m in mirrors]

@@ -29,7 +29,11 @@ def env():
     ctx.close()
 
 
+ARTIFACTS = __import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "artifacts")
+
+
 def oracle_shard(spec, cols_ints, srs, tau):
+    import apogee_gpu as A
     import shard
 
     nv = spec["log_rows"]
@@ -51,15 +55,19 @@ def oracle_shard(spec, cols_ints, srs, tau):
     O.transcript_op(snap, 2, 3, b"".join(O.fe(x) for x in limbs), len(limbs))
     g = O.fe_int(O.transcript_op(snap, 4, 33))
     beta = O.fe_int(O.transcript_op(snap, 4, 33))
-    blob = shard.shard_circuit(nv, spec["cols"])
-    proof_elems = 4 * nv + spec["cols"] + sum(4 * (nv - 1 - k) + 2 * spec["cols"] for k in range(nv))
-    slots = (ctypes.c_uint32 * 2)(0, 1)
+    blob, width, ext = shard.spec_circuit(spec, ARTIFACTS)
+    ch = shard.shard_challenges(g, beta, width, ext)
+    L = A.lib()
+    L.apg_gkr_proof_len.restype = ctypes.c_size_t
+    proof_elems = L.apg_gkr_proof_len(blob, ctypes.c_size_t(len(blob))) // 32
+    slots = (ctypes.c_uint32 * len(ch))(*sorted(ch))
     s = (ctypes.c_uint8 * O.SNAP).from_buffer(snap)
     pr = O.buf(32 * proof_elems)
-    top = O.buf(32 * spec["cols"])
+    top = O.buf(32 * 128 * (1 << nv))
     base = b"".join(O.fe(x) for c in cols_ints for x in c)
-    assert O.lib().oracle_gkr_prove(blob, ctypes.c_size_t(len(blob)), base, slots, O.fe(g) + O.fe(beta),
-                                     ctypes.c_size_t(2), s, pr, top) == 0
+    assert O.lib().oracle_gkr_prove(blob, ctypes.c_size_t(len(blob)), base, slots,
+                                     b"".join(O.fe(ch[k]) for k in sorted(ch)), ctypes.c_size_t(len(ch)), s, pr,
+                                     top) == 0
     proof = [O.fe_int(pr.raw[32 * i:32 * i + 32]) for i in range(proof_elems)]
     return cms, proof, snap, g
 
@@ -70,12 +78,18 @@ def test_shard_pipeline_matches_oracle(env):
 
     ctx, torch, tau = env
     srs = O.toy_srs(tau, 1 << 10)
+    # Two synthetic shards, then the reference's own family circuits (69 and
+    # 3 committed columns; add_sub reads the lookup slots and slot 13 with a
+    # decoder channel, image_window a window's constant).
     for spec in ({"index": 3, "family": 7, "log_rows": 4, "cols": 4},
-                 {"index": 11, "family": 2, "log_rows": 6, "cols": 5}):
+                 {"index": 11, "family": 2, "log_rows": 6, "cols": 5},
+                 {"index": 40, "family": 0, "log_rows": 6, "artifact": "add_sub"},
+                 {"index": 41, "family": 2, "log_rows": 4, "artifact": "image_window"}):
+        shard.spec_circuit(spec, ARTIFACTS)  # fills in a family circuit's column count
         cols = shard.device_columns(torch, 1 << spec["log_rows"], spec["cols"], 99 + spec["index"], "cuda:0", ctx)
         torch.cuda.synchronize()
-        out = shard.prove_shard(ctx, spec, cols)
-        assert _strip(out) == shard.prove_shard_composed(ctx, spec, cols)
+        out = shard.prove_shard(ctx, spec, cols, artifact_dir=ARTIFACTS)
+        assert _strip(out) == shard.prove_shard_composed(ctx, spec, cols, artifact_dir=ARTIFACTS)
         ints = [A.from_mont_bytes(bytes(c.cpu().numpy().tobytes())) for c in cols]
         cms, proof, snap, gamma = oracle_shard(spec, ints, srs, tau)
         assert out["cms"] == cms
@@ -137,15 +151,23 @@ def test_alone_equals_batched_equals_served(env):
     rng = random.Random(5)
     specs = [{"index": i, "family": i % 23, "log_rows": rng.choice([2, 4, 6, 8, 10]), "cols": rng.randint(4, 8)}
              for i in range(12)]
+    # Family circuits in the same mix (each request carries its own
+    # statement challenges and decoder width through the server).
+    specs += [{"index": 12, "family": 5, "log_rows": 6, "artifact": "mem_word"},
+              {"index": 13, "family": 9, "log_rows": 4, "artifact": "memory_frame_reg"},
+              {"index": 14, "family": 12, "log_rows": 4, "artifact": "zero_window"}]
+    for s in specs:
+        shard.spec_circuit(s, ARTIFACTS)
     columns = {s["index"]: shard.device_columns(torch, 1 << s["log_rows"], s["cols"], 500 + s["index"], "cuda:0",
                                                 ctx) for s in specs}
     torch.cuda.synchronize()
-    alone = {s["index"]: _strip(shard.prove_shard(ctx, s, columns[s["index"]])) for s in specs}
+    alone = {s["index"]: _strip(shard.prove_shard(ctx, s, columns[s["index"]], artifact_dir=ARTIFACTS))
+             for s in specs}
     with A.Server(ctx, max_workers=4) as server:
-        _, batched, times = shard.prove_batched(server, specs, columns)
+        _, batched, times = shard.prove_batched(server, specs, columns, artifact_dir=ARTIFACTS)
         for s in specs:
             assert _strip(batched[s["index"]]) == alone[s["index"]], f"shard {s['index']} differs in the batch"
-        wall, lat, served, _ = shard.serve(server, specs, columns, rate=200.0)
+        wall, lat, served, _ = shard.serve(server, specs, columns, rate=200.0, artifact_dir=ARTIFACTS)
         assert len(lat) == len(specs)
         for s in specs:
             assert _strip(served[s["index"]]) == alone[s["index"]], f"shard {s['index']} differs when served"
@@ -198,3 +220,35 @@ def test_server_reports_each_requests_failure(env):
         assert e.value.variant == "NonCanonical"
         p, _ = server.wait(t_good)
         assert p.cms == shard.prove_shard(ctx, good, cols)["cms"]
+
+
+def test_shard_refuses_bad_external_challenges(env):
+    """External challenges may not name a slot the shard draws itself (0,
+    6-13), nor one slot twice, nor carry a value that is not a field element;
+    the decoder width is at most 7."""
+    import apogee_gpu as A
+    import shard
+
+    ctx, torch, _ = env
+    spec = {"index": 70, "family": 3, "log_rows": 4, "artifact": "memory_frame_reg"}
+    blob, width, ext = shard.spec_circuit(spec, ARTIFACTS)
+    cols = shard.device_columns(torch, 1 << 4, spec["cols"], 71, "cuda:0", ctx)
+    torch.cuda.synchronize()
+    lo = spec["index"] << 22
+    args = (blob, [c.data_ptr() for c in cols], 4, 5, spec["family"], spec["index"], lo, lo + 16)
+    for bad in ({**ext, 6: 1}, {**ext, 0: 1}, {**ext, 13: 1}):
+        with pytest.raises(A.ApogeeError) as e:
+            ctx.prove_shard(A.Shard(*args, ext=bad))
+        assert e.value.variant == "InvalidArgument"
+    sh = A.Shard(*args, ext=ext)
+    sh._ext_values = b"\xff" * 32 + sh._ext_values[32:]
+    sh.c.ext_values = sh._ext_values
+    with pytest.raises(A.ApogeeError) as e:
+        ctx.prove_shard(sh)
+    assert e.value.variant == "NonCanonical"
+    with pytest.raises(A.ApogeeError) as e:
+        ctx.prove_shard(A.Shard(*args, ext=ext, decoder_width=8))
+    assert e.value.variant == "InvalidArgument"
+    # Missing statement challenges: the circuit names slots nobody set.
+    with pytest.raises(A.ApogeeError):
+        ctx.prove_shard(A.Shard(*args))
