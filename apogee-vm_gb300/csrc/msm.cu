@@ -509,51 +509,16 @@ __device__ __forceinline__ uint32_t small_scalar(const void* col, uint32_t i, in
 // Lanes of a warp that hit the same bucket share one atomic: the leader adds
 // the group's size and hands each peer its rank, so a bucket that a large
 // share of the scalars hit (digit 1 from {0,1} columns and from the carries of
-// 32-bit values) costs one atomic per warp, not one per scalar.
-// Windows of a `bits`-bit scalar at width cb (one more bit for the last
-// signed digit's carry).
-__host__ __device__ constexpr int window_count(int bits, int cb) { return (bits + cb) / cb; }
-
-// Window w's signed digit of the scalar in `limbs` (canonical, little-endian
-// 32-bit limbs), given the carry out of window w - 1: the magnitude, its sign
-// and the carry into window w + 1. With w and c known at compile time the
-// window's bits are one funnel shift of two fixed limbs.
-__device__ __forceinline__ uint32_t window_digit(const uint32_t (&limbs)[8], int w, int c, bool last,
-                                                 uint32_t& carry, uint32_t& neg) {
-  const int off = w * c;
-  uint32_t raw = 0;
-  if (off < 256) {
-    const int limb = off >> 5, sh = off & 31;
-    uint64_t v = limbs[limb] >> sh;
-    if (limb + 1 < 8) v |= (uint64_t)limbs[limb + 1] << (32 - sh);
-    raw = (uint32_t)v & ((1u << c) - 1);
-  }
-  const uint32_t coef = raw + carry;
-  if (last || coef < (1u << (c - 1))) {
-    carry = 0;
-    neg = 0;
-    return coef;
-  }
-  carry = 1;
-  neg = 1;
-  return (1u << c) - coef;  // digit coef - 2^c < 0
-}
-
-// Digits of one scalar, counted (SCATTER = false) or placed (SCATTER = true).
-// Lanes of a warp that hit the same bucket share one atomic: the leader adds
-// the group's size and hands each peer its rank, so a bucket that a large
-// share of the scalars hit (digit 1 from {0,1} columns and from the carries of
-// 32-bit values) costs one atomic per warp, not one per scalar. (Aggregating
-// only the lanes that share the first active lane's bucket, with plain
-// atomics for the rest, was measured 13 % slower on mixed columns.)
-// CB > 0 compiles the window width in (the window loop unrolls and every
-// window's bits come from fixed limbs: the count pass is bound by the integer
-// ALU); CB = 0 takes it at run time.
-template <bool SMALL, bool SCATTER, int CB>
-__global__ void __launch_bounds__(256) k_digits(MsmCols cols, int c_rt, int windows_rt, int precomp, uint32_t tab_n,
+// 32-bit values) costs one atomic per warp, not one per scalar. Measured and
+// not kept: aggregating only the lanes that share the first active lane's
+// bucket, with plain atomics for the rest (13 % slower on mixed columns), and
+// the window width compiled in with the window loop unrolled and every
+// window's atomic issued before the first result is awaited (no change in
+// either pass at 2^22).
+template <bool SMALL, bool SCATTER>
+__global__ void __launch_bounds__(256) k_digits(MsmCols cols, int c, int windows, int precomp, uint32_t tab_n,
                                                 int canonical_in, uint32_t* cursor, uint32_t* sorted,
                                                 uint32_t* flags) {
-  const int c = CB ? CB : c_rt;
   const uint32_t col = blockIdx.y;
   const uint32_t n = cols.len[col];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -575,13 +540,30 @@ __global__ void __launch_bounds__(256) k_digits(MsmCols cols, int c_rt, int wind
     }
   }
   const uint32_t K = 1u << (c - 1);
-  const uint32_t spaces = precomp ? 1u : (uint32_t)(CB ? window_count(SMALL ? 32 : 254, CB) : windows_rt);
+  const uint32_t mask = (1u << c) - 1;
+  const uint32_t spaces = precomp ? 1u : (uint32_t)windows;
   const uint32_t key0 = cols.shared ? 0u : col * spaces * K;
   const uint32_t base_i = cols.off[col] + i;
   uint32_t carry = 0;
-  auto step = [&](int w, bool last) {
-    uint32_t neg;
-    uint32_t mag = window_digit(limbs, w, c, last, carry, neg);
+  for (int w = 0; w < windows; ++w) {
+    const int off = w * c;
+    uint32_t raw = 0;
+    if (off < 256) {
+      const int limb = off >> 5, sh = off & 31;
+      uint64_t v = limbs[limb] >> sh;
+      if (limb + 1 < 8) v |= (uint64_t)limbs[limb + 1] << (32 - sh);
+      raw = (uint32_t)v & mask;
+    }
+    const uint32_t coef = raw + carry;
+    uint32_t mag, neg = 0;
+    if (w == windows - 1 || coef < K) {
+      mag = coef;
+      carry = 0;
+    } else {
+      mag = (1u << c) - coef;  // digit coef - 2^c < 0
+      neg = 1;
+      carry = 1;
+    }
     if (!live) mag = 0;
     if (mag > K) {  // unreachable for values below r; never index past the bucket range
       if (!SCATTER) raise_flag(flags, DEV_NONCANONICAL);
@@ -602,63 +584,6 @@ __global__ void __launch_bounds__(256) k_digits(MsmCols cols, int c_rt, int wind
         atomicAdd(&cursor[key], (uint32_t)__popc(peers));
       }
     }
-  };
-  if constexpr (CB > 0 && SCATTER) {
-    // Every window's atomic is issued before the first one's result is
-    // waited for (the placement is the same as the one-window-at-a-time
-    // loop's): the scatter pass was bound by the atomics' round trips.
-    constexpr int W = window_count(SMALL ? 32 : 254, CB);
-    uint32_t base[W], peers[W], negs = 0;
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      uint32_t neg;
-      uint32_t mag = window_digit(limbs, w, c, w == W - 1, carry, neg);
-      if (!live || mag > K) mag = 0;  // (mag > K is unreachable below r; the count pass flags it)
-      negs |= neg << w;
-      const unsigned active = __ballot_sync(0xffffffffu, mag != 0);
-      const uint32_t key = key0 + (precomp ? 0u : (uint32_t)w * K) + mag - 1;
-      peers[w] = mag ? __match_any_sync(active, key) : 0u;
-      base[w] = 0;
-      if (mag && (int)lane == __ffs(peers[w]) - 1) base[w] = atomicAdd(&cursor[key], (uint32_t)__popc(peers[w]));
-    }
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      if (!peers[w]) continue;
-      const int leader = __ffs(peers[w]) - 1;
-      const uint32_t neg = (negs >> w) & 1u;
-      const uint32_t b = __shfl_sync(peers[w], base[w], leader);
-      const uint32_t idx = precomp ? (uint32_t)w * tab_n + base_i : base_i;
-      sorted[b + (uint32_t)__popc(peers[w] & ((1u << lane) - 1u))] = (neg << 31) | idx;
-    }
-  } else if constexpr (CB > 0) {
-    constexpr int W = window_count(SMALL ? 32 : 254, CB);
-#pragma unroll
-    for (int w = 0; w < W; ++w) step(w, w == W - 1);
-  } else {
-    for (int w = 0; w < windows_rt; ++w) step(w, w == windows_rt - 1);
-  }
-}
-
-// k_digits at the plan's width: compiled-in widths 8..22 (every width the
-// tuner and the default rule pick for the large sizes), the run-time form
-// otherwise.
-template <bool SMALL, bool SCATTER>
-void launch_digits(Ctx& c, dim3 grid, const MsmCols& cols, int cb, int windows, int precomp, uint32_t tab_n, int canon,
-                   uint32_t* counts, uint32_t* sorted) {
-  auto go = [&](auto kern) {
-    launch(c, kern, grid, 256, 0, cols, cb, windows, precomp, tab_n, canon, counts, sorted, c.d_flags);
-  };
-  if (windows != window_count(SMALL ? 32 : 254, cb)) return go(k_digits<SMALL, SCATTER, 0>);
-  switch (cb) {
-#define APG_DIGITS_CASE(W) \
-  case W:                  \
-    return go(k_digits<SMALL, SCATTER, W>);
-    APG_DIGITS_CASE(8) APG_DIGITS_CASE(9) APG_DIGITS_CASE(10) APG_DIGITS_CASE(11) APG_DIGITS_CASE(12)
-    APG_DIGITS_CASE(13) APG_DIGITS_CASE(14) APG_DIGITS_CASE(15) APG_DIGITS_CASE(16) APG_DIGITS_CASE(17)
-    APG_DIGITS_CASE(18) APG_DIGITS_CASE(19) APG_DIGITS_CASE(20) APG_DIGITS_CASE(21) APG_DIGITS_CASE(22)
-#undef APG_DIGITS_CASE
-    default:
-      return go(k_digits<SMALL, SCATTER, 0>);
   }
 }
 
@@ -1262,6 +1187,7 @@ static int default_window(size_t n, bool small) {
   return cb;
 }
 
+static int window_count(int bits, int cb) { return (bits + 1 + cb - 1) / cb; }
 
 const SrsTable* srs_table(Ctx& c, int cbits, size_t need) {
   for (auto& t : c.tables)
@@ -1450,16 +1376,20 @@ void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols
   const dim3 dgrid(blocks_for<int>(std::max<size_t>(nmax, 1), 256), (unsigned)ncols);
   const int canon = scalars_canonical ? 1 : 0;
   if (small_scalars)
-    launch_digits<true, false>(c, dgrid, cols, p.c, p.windows, (int)p.precomp, tab_n, canon, counts, nullptr);
+    launch(c, k_digits<true, false>, dgrid, 256, 0, cols, p.c, p.windows, (int)p.precomp, tab_n, canon, counts,
+           (uint32_t*)nullptr, c.d_flags);
   else
-    launch_digits<false, false>(c, dgrid, cols, p.c, p.windows, (int)p.precomp, tab_n, canon, counts, nullptr);
+    launch(c, k_digits<false, false>, dgrid, 256, 0, cols, p.c, p.windows, (int)p.precomp, tab_n, canon, counts,
+           (uint32_t*)nullptr, c.d_flags);
   launch(c, k_scan_local, (unsigned)scan_blocks, kScanBlock, 0, counts, nbins, blk);
   launch(c, k_scan_blocks, 1, kScanBlock, 0, blk, (int)scan_blocks);
   launch(c, k_scan_add, blocks_for<int>(nbins, 256), 256, 0, counts, nbins, (const uint32_t*)blk, total);
   if (small_scalars)
-    launch_digits<true, true>(c, dgrid, cols, p.c, p.windows, (int)p.precomp, tab_n, canon, counts, sorted);
+    launch(c, k_digits<true, true>, dgrid, 256, 0, cols, p.c, p.windows, (int)p.precomp, tab_n, canon, counts, sorted,
+           c.d_flags);
   else
-    launch_digits<false, true>(c, dgrid, cols, p.c, p.windows, (int)p.precomp, tab_n, canon, counts, sorted);
+    launch(c, k_digits<false, true>, dgrid, 256, 0, cols, p.c, p.windows, (int)p.precomp, tab_n, canon, counts,
+           sorted, c.d_flags);
   cudaEvent_t t_acc = c.timer_begin();
   const uint32_t* pair_mode = nullptr;
   const uint32_t* pair_ends = nullptr;

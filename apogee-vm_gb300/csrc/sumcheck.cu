@@ -286,6 +286,53 @@ __global__ void __launch_bounds__(kRoundThreads, APG_PAIRS_MIN_BLOCKS) k_round_p
   round_total(A, partials, red);
 }
 
+// The same summand in rounds with few pairs (the tops of halving lists): one
+// thread per (pair, term), or per (pair, table no term reads), which only
+// folds, so a pair's folds and products run side by side instead of as one
+// thread's chain of a hundred products. Each term thread weighs its own term
+// by c_j and the pair's eq weight; the block sums them all. The pair's eq
+// line is stored by its first term's thread; a table two terms share is
+// stored twice with the same value.
+__global__ void __launch_bounds__(kRoundThreads) k_round_pairs_small(RoundArgs A, PairTerms T, Fr* partials) {
+  __shared__ Fr red[kRoundThreads];
+  const bool n1 = (A.nodes >> 1) & 1;
+  const size_t per = (size_t)T.n + T.nrest;
+  Fr acc0 = fe_zero<FrConsts>(), acc1 = fe_zero<FrConsts>(), acc2 = fe_zero<FrConsts>();
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < A.npairs * per; t += stride) {
+    const size_t i = t / per;
+    const int j = (int)(t - i * per);
+    if (j >= T.n) {
+      Fr lo, hi;
+      load_line(A, T.rest[j - T.n], i, lo, hi);
+      continue;
+    }
+    Fr alo, ahi, blo, bhi, e_lo, e_hi;
+    load_line(A, T.a[j], i, alo, ahi);
+    load_line(A, T.b[j], i, blo, bhi);
+    load_line(A, A.nd, i, e_lo, e_hi, j == 0);
+    Fr cw = fe_add(e_lo, e_hi);  // the pair's eq weight without the current variable's factor
+    if (!T.unit[j]) cw = rmul(ld_fe(&T.c[j]), cw);
+    const Fr p0 = rmul(alo, blo);
+    const Fr p2 = rmul(fe_sub(fe_add(ahi, ahi), alo), fe_sub(fe_add(bhi, bhi), blo));  // the lines at X = 2
+    acc0 = fe_add(acc0, rmul(cw, p0));
+    acc2 = fe_add(acc2, rmul(cw, p2));
+    if (n1) acc1 = fe_add(acc1, rmul(cw, rmul(ahi, bhi)));
+  }
+  const Fr accs[4] = {acc0, acc1, acc2, fe_zero<FrConsts>()};
+  for (int x = 0; x < 4; ++x) {
+    red[threadIdx.x] = accs[x];
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+      if (threadIdx.x < (unsigned)off) red[threadIdx.x] = fe_add(red[threadIdx.x], red[threadIdx.x + off]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) st_fe(&partials[(size_t)blockIdx.x * 4 + x], red[0]);
+    __syncthreads();
+  }
+  round_total(A, partials, red);
+}
+
 // Wide gate lists (many gates, many tables): one warp per pair. The pair's
 // tables sit once in the warp's shared slots (values, then cached entries,
 // then steps, then eq's value and step), written lane-parallel; at each node
@@ -625,6 +672,11 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
     if (use_pairs && !A.xsplit)
       launch(c, k_round_pairs, (int)std::min<size_t>((A.npairs + kRoundThreads - 1) / kRoundThreads,
                                                      (size_t)c.sm_count * 8),
+             kRoundThreads, 0, A, PT, partials);
+    else if (use_pairs && PT.n + PT.nrest >= 4)  // (one or two terms: the node-split generic rounds were faster)
+      launch(c, k_round_pairs_small,
+             (int)std::min<size_t>((A.npairs * (size_t)(PT.n + PT.nrest) + kRoundThreads - 1) / kRoundThreads,
+                                   (size_t)c.sm_count * 8),
              kRoundThreads, 0, A, PT, partials);
     else if (warp_mode) launch(c, k_round_warp, blocks, kRoundThreads, warp_smem, A, P, V, partials);
     else launch(c, k_round, blocks, threads, smem, A, P, V, partials);

@@ -425,9 +425,10 @@ def run_profile_shard(args, ctx, torch, dev):
         cms = ctx.commit_batch_device(ptrs, n)
         t = tick("commit", t)
         tr, g, beta = shard.shard_transcript(spec, cms)
-        v = ctx.gkr_forward(blob, ptrs, {0: g, 1: beta}, on_device=True)
+        ch = shard.shard_challenges(g, beta)
+        v = ctx.gkr_forward(blob, ptrs, ch, on_device=True)
         t = tick("forward", t)
-        _, tr, point = ctx.gkr_prove(blob, v, {0: g, 1: beta}, tr, with_point=True)
+        _, tr, point = ctx.gkr_prove(blob, v, ch, tr, with_point=True)
         v.free()
         t = tick("gkr_prove", t)
         ctx.batch_open(ptrs, n, cms, A.from_mont_bytes(point), tr, on_device=True)
@@ -441,6 +442,7 @@ def run_profile_shard(args, ctx, torch, dev):
     out = {k: v * 1e3 / args.steps for k, v in phases.items()}
     timers = {name: ctx.timer(i) for i, name in enumerate(["msm_accumulate", "msm_total", "sumcheck_round",
                                                             "gkr_forward", "mercury_pass"])}
+    timers["host_round"] = ctx.timer(A.Context.TIMER_HOST_ROUND)
     print(json.dumps({"case": "shard", "log2n": n, "cols": args.cols, "ms_per_phase": out,
                       "ms_total": sum(out.values()), "timers_ms_launches": timers}), flush=True)
     ctx.close()

@@ -14,6 +14,7 @@ sys.path.insert(0, ROOT)
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300, sm_103a)")
     config.addinivalue_line("markers", "slow: larger CPU cases")
+    config.addinivalue_line("markers", "cpu_host: host-side library code that needs no GPU")
 
 
 @pytest.fixture(scope="session")
