@@ -834,8 +834,23 @@ def run_gpu(args):
               flush=True)
         raise SystemExit(3)
     del check_col
+    # The machine's host-to-device link, measured alone on the same pinned
+    # buffers (the end-to-end leg cannot beat one step's copies at this rate;
+    # the rate has varied several-fold between boxes).
+    land = torch.empty(k * n * 8, dtype=torch.int32, device=f"cuda:{local}")
+    best_copy = None
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for j, h in enumerate(host_cols):
+            land[j * n * 8:(j + 1) * n * 8].copy_(h, non_blocking=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        best_copy = dt if best_copy is None else min(best_copy, dt)
+    del land
     e2e = {"value": weak_value(world, k * n, t_e2e), "unit": UNIT, "h2d_bytes_per_step": k * n * 32,
-           "d2h_bytes_per_step": k * 64}
+           "d2h_bytes_per_step": k * 64, "ms_per_step": t_e2e * 1e3,
+           "h2d_copy_alone_ms": best_copy * 1e3, "h2d_gbs": k * n * 32 / best_copy / 1e9}
 
     # Roofline: the accumulation kernel on uniform 254-bit scalars.
     ucol = synth.uniform_column(n, SEED + 999)
