@@ -434,6 +434,11 @@ static void release_lane(Ctx& c) {
   c.lane.reset();
 }
 
+// Groups a batch commit is split into (build knob for measurement).
+#ifndef APG_BATCH_GROUPS
+#define APG_BATCH_GROUPS 4
+#endif
+
 // k commits of one size over the resident SRS. Columns go in groups (one
 // sort, accumulation and bucket reduction per group) that alternate between
 // the context's two lanes, so one group's latency-bound reduction (and the
@@ -456,7 +461,7 @@ static int commit_batch_lanes(Ctx& c, const void* const* cols, bool host, size_t
   APG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   APG_CUDA(cudaEventRecord(ev, c.stream));
   APG_CUDA(cudaStreamWaitEvent(L.stream, ev, 0));
-  const size_t group = std::max<size_t>(1, (k + 3) / 4);
+  const size_t group = std::max<size_t>(1, (k + APG_BATCH_GROUPS - 1) / APG_BATCH_GROUPS);
   const size_t ngroups = (k + group - 1) / group;
   std::vector<const void*> ptrs(cols, cols + k);
   std::vector<size_t> lens(k, n);

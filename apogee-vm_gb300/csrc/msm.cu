@@ -989,10 +989,68 @@ __device__ __forceinline__ PairLane pair_lane(size_t s, size_t E, size_t T) {
 // total in tot[s]. No barrier: the lanes of a block finish independently.
 // A round 0 whose output would not fit the scratch (E > cap) sets *mode = 1,
 // and every later step takes the references instead.
+// Slot inputs handed from the forward to the backward half (`idx`, one word a
+// slot in the same j * T + s layout as the running products): the first
+// input's position, and bit 31 when the slot has a second input. With it the
+// backward half neither searches the bucket offsets nor waits on them, and
+// issues a slot's reference loads one slot ahead and its word loads two
+// ahead (k_pair_bwd_pf). APG_PAIR_PF=0 keeps the searching k_pair_bwd (a
+// build knob for measurement). Measured on a GB300 (uniform 2^22
+// accumulation / mixed 16 x 2^22 commit): searching 11.86 / 56.6 ms; words
+// and references ahead 11.36 / 54.8 ms at five blocks an SM (11.23 / 56.1 at
+// four); also the points and running product one slot ahead (128 registers,
+// three or four blocks) 11.8-12.0 / 56.7-59.0; the x coordinates one slot
+// ahead with the slope's inverse started on x alone 11.35 / 56.0 at four
+// blocks, 12.1 / 57.7 at five.
+#ifndef APG_PAIR_PF
+#define APG_PAIR_PF 1
+#endif
+constexpr uint32_t kPairTwo = 0x80000000u;
+// APG_PAIR_FWD_AHEAD: the forward half also loads the next slot's word and
+// references while the current slot's x coordinates are in flight.
+#ifndef APG_PAIR_FWD_AHEAD
+#define APG_PAIR_FWD_AHEAD 1
+#endif
+
+// A slot word's references: table references in round 0, list positions
+// after it (a one-input slot repeats its first).
+template <bool REFS>
+__device__ __forceinline__ void pair_refs(const uint32_t* refs, uint32_t w, uint32_t& e0, uint32_t& e1) {
+  const uint32_t i0 = w & ~kPairTwo;
+  const bool two = (w & kPairTwo) != 0;
+  if (REFS) {
+    e0 = refs[i0];
+    e1 = two ? refs[i0 + 1] : e0;
+  } else {
+    e0 = i0;
+    e1 = two ? i0 + 1 : i0;
+  }
+}
+
+// pair_denominator with the two x coordinates already loaded.
+template <bool REFS>
+__device__ __forceinline__ bool pair_denominator_x(const Affine* src, uint32_t e0, uint32_t e1, const Fq& x0,
+                                                   const Fq& x1, Fq& d) {
+  const uint32_t j0 = REFS ? (e0 & 0x7fffffffu) : e0, j1 = REFS ? (e1 & 0x7fffffffu) : e1;
+  if (!fe_eq(x0, x1)) {
+    if (fe_is_zero(x0) && fe_is_zero(ld_fe(&src[j0].y))) return false;
+    if (fe_is_zero(x1) && fe_is_zero(ld_fe(&src[j1].y))) return false;
+    d = fe_sub(x1, x0);
+    return true;
+  }
+  Fq y0 = ld_fe(&src[j0].y), y1 = ld_fe(&src[j1].y);
+  if (REFS && (e0 >> 31)) y0 = fe_neg(y0);
+  if (REFS && (e1 >> 31)) y1 = fe_neg(y1);
+  if (fe_is_zero(x0) && (fe_is_zero(y0) || fe_is_zero(y1))) return false;  // an infinity
+  if (!fe_eq(y0, y1)) return false;                                        // P + (-P)
+  d = fe_add(y0, y0);
+  return true;
+}
+
 template <bool REFS>
 __global__ void __launch_bounds__(kPairThreads)
     k_pair_fwd(const uint32_t* refs, const Affine* src, const uint32_t* ends_in, const uint32_t* start_out,
-               uint32_t nbins, size_t cap, uint32_t* mode, size_t T, Fq* pp, Fq* tot) {
+               uint32_t nbins, size_t cap, uint32_t* mode, size_t T, Fq* pp, Fq* tot, uint32_t* idx) {
   const size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (s >= T || *mode) return;
   const size_t E = start_out[nbins];
@@ -1003,11 +1061,47 @@ __global__ void __launch_bounds__(kPairThreads)
   const PairLane L = pair_lane(s, E, T);
   uint32_t b = L.steps ? pair_bucket(start_out, nbins, L.o0) : 0u;
   Fq acc = fe_one<FqConsts>();
+  if (APG_PAIR_PF && APG_PAIR_FWD_AHEAD) {
+    // The next slot's bucket search, word and references are issued while
+    // this slot's x coordinates are in flight.
+    uint32_t wa = 0, ea0 = 0, ea1 = 0;
+    if (L.steps) {
+      bool two;
+      wa = pair_input(ends_in, start_out, b, L.o0, two);
+      wa |= two ? kPairTwo : 0u;
+      pair_refs<REFS>(refs, wa, ea0, ea1);
+    }
+    for (size_t j = 0; j < L.steps; ++j) {
+      const Fq x0 = ld_fe(&src[REFS ? (ea0 & 0x7fffffffu) : ea0].x);
+      const Fq x1 = ld_fe(&src[REFS ? (ea1 & 0x7fffffffu) : ea1].x);
+      uint32_t wb = 0, eb0 = 0, eb1 = 0;
+      if (j + 1 < L.steps) {
+        const size_t o = L.o0 + 32 * (j + 1);
+        b = pair_seek_up(start_out, nbins, b, o);
+        bool two;
+        wb = pair_input(ends_in, start_out, b, o, two);
+        wb |= two ? kPairTwo : 0u;
+        pair_refs<REFS>(refs, wb, eb0, eb1);
+      }
+      idx[j * T + s] = wa;
+      Fq d;
+      if ((wa & kPairTwo) && pair_denominator_x<REFS>(src, ea0, ea1, x0, x1, d)) {
+        st_fe(&pp[j * T + s], acc);
+        acc = fe_mul(acc, d);
+      }
+      wa = wb;
+      ea0 = eb0;
+      ea1 = eb1;
+    }
+    st_fe(&tot[s], acc);
+    return;
+  }
   for (size_t j = 0; j < L.steps; ++j) {
     const size_t o = L.o0 + 32 * j;
     b = pair_seek_up(start_out, nbins, b, o);
     bool two;
     const uint32_t i0 = pair_input(ends_in, start_out, b, o, two);
+    if (APG_PAIR_PF) idx[j * T + s] = i0 | (two ? kPairTwo : 0u);
     Fq d;
     if (!two || !pair_denominator<REFS>(refs, src, i0, d)) continue;
     st_fe(&pp[j * T + s], acc);
@@ -1045,6 +1139,97 @@ __global__ void __launch_bounds__(kPairThreads, APG_PAIR_MIN_BLOCKS)
     inv = di.b;
     const Fq lam = pmul(t.num, di.a);
     pair_store<REFS>(refs, src, t, lam, psqr(lam), &out[o]);
+  }
+}
+
+// The backward half over the forward half's slot words (see `idx` above). A
+// slot's chain of dependent loads (its word, then its references, then its
+// points) is spread over consecutive iterations: the word and the
+// references are loaded while the two slots before it are summed, so only
+// the point gather itself waits at the slot's start.
+template <bool REFS>
+__device__ __forceinline__ Affine pair_fetch(const Affine* src, uint32_t e) {
+  return ld_affine(&src[REFS ? (e & 0x7fffffffu) : e]);
+}
+
+template <bool REFS>
+__device__ __forceinline__ void pair_sign(Affine& p, uint32_t e) {
+  if (REFS && (e >> 31)) p.y = fe_neg(p.y);
+}
+
+// One slot from its loaded inputs: the same kinds, running inverse and sum
+// as pair_load/pair_store.
+__device__ __forceinline__ void pair_finish(const Affine& p0, const Affine& p1, bool two, const Fq& ppj, Fq& inv,
+                                            Affine* dst) {
+  const int kind = two ? pair_kind(p0, p1) : (int)kPairFirst;
+  if (kind < kPairAdd) {
+    Fq x = p0.x, y = p0.y;
+    if (kind == kPairSecond) {
+      x = p1.x;
+      y = p1.y;
+    } else if (kind == kPairInf) {
+      x = fe_zero<FqConsts>();
+      y = fe_zero<FqConsts>();
+    }
+    st_fe(&dst->x, x);
+    st_fe(&dst->y, y);
+    return;
+  }
+  Fq d, num;
+  if (kind == kPairAdd) {
+    d = fe_sub(p1.x, p0.x);
+    num = fe_sub(p1.y, p0.y);
+  } else {
+    d = fe_add(p0.y, p0.y);
+    const Fq q = psqr(p0.x);
+    num = fe_add(q, fe_add(q, q));
+  }
+  const Fq2 di = pmul2(inv, ppj, inv, d);  // 1/d, and the running inverse one back
+  inv = di.b;
+  const Fq lam = pmul(num, di.a);
+  const Fq x = fe_sub(fe_sub(psqr(lam), p0.x), p1.x);
+  st_fe(&dst->x, x);
+  st_fe(&dst->y, fe_sub(pmul(lam, fe_sub(p0.x, x)), p0.y));
+}
+
+#ifndef APG_PAIR_PF_MIN_BLOCKS
+#define APG_PAIR_PF_MIN_BLOCKS 5
+#endif
+
+template <bool REFS>
+__global__ void __launch_bounds__(kPairThreads, APG_PAIR_PF_MIN_BLOCKS)
+    k_pair_bwd_pf(const uint32_t* refs, const Affine* src, const uint32_t* idx, const uint32_t* start_out,
+                  uint32_t nbins, const uint32_t* mode, size_t T, const Fq* pp, const Fq* tot, Affine* out,
+                  uint32_t* flags) {
+  const size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (*mode) return;  // uniform across the grid: set before this launch
+  const size_t E = start_out[nbins];
+  const PairLane L = pair_lane(s, E, T);
+  Fq inv = block_inverse(s < T ? ld_fe(&tot[s]) : fe_one<FqConsts>(), flags);  // every thread of the block
+  if (s >= T || !L.steps) return;
+  // Entering the loop for slot j: slot j's word and references, slot j - 1's
+  // word. Each pass issues slot j's point and running-product loads, slot
+  // j - 1's reference loads and slot j - 2's word load together, then sums
+  // slot j.
+  size_t j = L.steps - 1;
+  uint32_t wa = idx[j * T + s], ea0, ea1;
+  pair_refs<REFS>(refs, wa, ea0, ea1);
+  uint32_t wb = j >= 1 ? idx[(j - 1) * T + s] : 0u;
+  for (;;) {
+    Affine p0 = pair_fetch<REFS>(src, ea0), p1 = pair_fetch<REFS>(src, ea1);
+    const Fq ppj = ld_fe(&pp[j * T + s]);
+    uint32_t nb0 = 0, nb1 = 0, nw = 0;
+    if (j >= 1) pair_refs<REFS>(refs, wb, nb0, nb1);
+    if (j >= 2) nw = idx[(j - 2) * T + s];
+    pair_sign<REFS>(p0, ea0);
+    pair_sign<REFS>(p1, ea1);
+    pair_finish(p0, p1, (wa & kPairTwo) != 0, ppj, inv, &out[L.o0 + 32 * j]);
+    if (j == 0) break;
+    --j;
+    wa = wb;
+    ea0 = nb0;
+    ea1 = nb1;
+    wb = nw;
   }
 }
 
@@ -1310,8 +1495,16 @@ size_t pair_resident_threads(Ctx& c) {
   static int per_sm = 0;
   std::call_once(once, [] {
     int a = 0, b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_pair_bwd<true>, kPairThreads, 0) != cudaSuccess) a = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_bwd<false>, kPairThreads, 0) != cudaSuccess) b = 1;
+    if (APG_PAIR_PF) {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_pair_bwd_pf<true>, kPairThreads, 0) != cudaSuccess)
+        a = 1;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_bwd_pf<false>, kPairThreads, 0) != cudaSuccess)
+        b = 1;
+    } else {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_pair_bwd<true>, kPairThreads, 0) != cudaSuccess) a = 1;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_bwd<false>, kPairThreads, 0) != cudaSuccess)
+        b = 1;
+    }
     per_sm = std::max(1, std::min(a, b));
   });
   return (size_t)c.sm_count * (size_t)per_sm * kPairThreads;
@@ -1403,8 +1596,12 @@ void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols
     const size_t T = pair_resident_threads(c);
     Affine* lst[2] = {c.scratch[S_PAIR_A].as<Affine>(cap[0]),
                       c.scratch[S_PAIR_B].as<Affine>(kPairRounds > 1 ? cap[1] : 1)};
-    Fq* pp = c.scratch[S_PAIR_PP].as<Fq>((cap[0] + T - 1) / T * T + T);
-    Fq* tot = pp + (cap[0] + T - 1) / T * T;
+    // Running products (one a slot, j * T + s), the lanes' totals and, with
+    // APG_PAIR_PF, the slot words (4 bytes a slot) after them.
+    const size_t P = (cap[0] + T - 1) / T * T;
+    Fq* pp = c.scratch[S_PAIR_PP].as<Fq>(P + T + (APG_PAIR_PF ? (P + 7) / 8 : 0));
+    Fq* tot = pp + P;
+    uint32_t* idx = APG_PAIR_PF ? reinterpret_cast<uint32_t*>(tot + T) : nullptr;
     uint32_t* cnt = c.scratch[S_PAIR_CNT].as<uint32_t>((size_t)kPairRounds * (nbins + 1) + 2);
     uint32_t* mode = cnt + (size_t)kPairRounds * (nbins + 1);
     APG_CUDA(cudaMemsetAsync(mode, 0, 2 * sizeof(uint32_t), c.stream));
@@ -1422,14 +1619,23 @@ void msm_group(Ctx& c, const Affine* bases, const SrsTable* table, const MsmCols
       const Affine* in = r == 0 ? src : lst[(r - 1) & 1];
       if (r == 0) {
         launch(c, k_pair_fwd<true>, pblocks, kPairThreads, 0, rr, in, ends_in, (const uint32_t*)st, (uint32_t)nbins,
-               cap[0], mode, T, pp, tot);
-        launch(c, k_pair_bwd<true>, pblocks, kPairThreads, 0, rr, in, ends_in, (const uint32_t*)st, (uint32_t)nbins,
-               (const uint32_t*)mode, T, (const Fq*)pp, (const Fq*)tot, lst[0], c.d_flags);
+               cap[0], mode, T, pp, tot, idx);
+        if (APG_PAIR_PF)
+          launch(c, k_pair_bwd_pf<true>, pblocks, kPairThreads, 0, rr, in, (const uint32_t*)idx, (const uint32_t*)st,
+                 (uint32_t)nbins, (const uint32_t*)mode, T, (const Fq*)pp, (const Fq*)tot, lst[0], c.d_flags);
+        else
+          launch(c, k_pair_bwd<true>, pblocks, kPairThreads, 0, rr, in, ends_in, (const uint32_t*)st,
+                 (uint32_t)nbins, (const uint32_t*)mode, T, (const Fq*)pp, (const Fq*)tot, lst[0], c.d_flags);
       } else {
         launch(c, k_pair_fwd<false>, pblocks, kPairThreads, 0, rr, in, ends_in, (const uint32_t*)st, (uint32_t)nbins,
-               cap[r], mode, T, pp, tot);
-        launch(c, k_pair_bwd<false>, pblocks, kPairThreads, 0, rr, in, ends_in, (const uint32_t*)st, (uint32_t)nbins,
-               (const uint32_t*)mode, T, (const Fq*)pp, (const Fq*)tot, lst[r & 1], c.d_flags);
+               cap[r], mode, T, pp, tot, idx);
+        if (APG_PAIR_PF)
+          launch(c, k_pair_bwd_pf<false>, pblocks, kPairThreads, 0, rr, in, (const uint32_t*)idx,
+                 (const uint32_t*)st, (uint32_t)nbins, (const uint32_t*)mode, T, (const Fq*)pp, (const Fq*)tot,
+                 lst[r & 1], c.d_flags);
+        else
+          launch(c, k_pair_bwd<false>, pblocks, kPairThreads, 0, rr, in, ends_in, (const uint32_t*)st,
+                 (uint32_t)nbins, (const uint32_t*)mode, T, (const Fq*)pp, (const Fq*)tot, lst[r & 1], c.d_flags);
       }
       ends_in = st + 1;
     }

@@ -291,20 +291,25 @@ def serve(server, specs, columns, rate: float, seed: int = 7, blobs=None, artifa
     return wall, lat, outs, times
 
 
-def latency_attribution(times, q=0.99):
-    """Where the slowest requests' time went: the requests at or above the
-    q-quantile of latency, their mean queueing (submit to admission), and
-    their mean phases (commit, forward, GKR proof, opening) in ms."""
+def latency_attribution(times, q_lo=0.99, q_hi=1.0):
+    """Where a band of requests' time went: the requests whose latency lies
+    between the q_lo- and q_hi-quantiles (0.99-1.0: the tail; 0.45-0.55:
+    around the median), their mean latency, mean queueing (submit to
+    admission) and mean phases (commit, forward, GKR proof, opening) in ms.
+    Queueing plus the phases is about the latency; the rest is the host work
+    between admission and the first phase and after the last."""
     lat = sorted(((tm["done_ns"] - tm["submit_ns"]) / 1e6, i) for i, tm in times.items())
     if not lat:
         return {}
-    k = max(0, min(len(lat) - 1, int(math.ceil(q * len(lat))) - 1))
-    tail = [i for _, i in lat[k:]]
-    n = len(tail)
-    qwait = sum((times[i]["admit_ns"] - times[i]["submit_ns"]) / 1e6 for i in tail) / n
-    phases = [sum(times[i]["phase_ms"][j] for i in tail) / n for j in range(4)]
-    return {"requests": n, "latency_ms": lat[k][0], "queue_ms": qwait, "commit_ms": phases[0],
-            "forward_ms": phases[1], "gkr_ms": phases[2], "open_ms": phases[3]}
+    lo = max(0, min(len(lat) - 1, int(math.ceil(q_lo * len(lat))) - 1))
+    hi = max(lo + 1, min(len(lat), int(math.ceil(q_hi * len(lat)))))
+    band = lat[lo:hi]
+    n = len(band)
+    qwait = sum((times[i]["admit_ns"] - times[i]["submit_ns"]) / 1e6 for _, i in band) / n
+    phases = [sum(times[i]["phase_ms"][j] for _, i in band) / n for j in range(4)]
+    return {"requests": n, "quantiles": [q_lo, q_hi], "latency_ms": sum(x for x, _ in band) / n,
+            "queue_ms": qwait, "commit_ms": phases[0], "forward_ms": phases[1], "gkr_ms": phases[2],
+            "open_ms": phases[3]}
 
 
 def percentile(xs, q):
