@@ -54,7 +54,18 @@ __device__ __forceinline__ const Fr* table_in(const RoundArgs& A, int k) {
 
 // Pair i of table k: (lo, hi) = entries (2i, 2i + 1) of this round's level,
 // folded from the previous level with c first when the round binds (the
-// folded pair is stored when `store` is set).
+// folded pair is stored when `store` is set). OUTLINE: the fold's two
+// products are one call of the shared out-of-line rmul2 instead of two
+// inlined multiplies, for the kernels of small rounds, where a launch runs its
+// code once and fetching inlined copies of the multiply costs more than the
+// call (APG_SMALL_OUTLINE; 0 inlines them everywhere).
+#ifndef APG_SMALL_OUTLINE
+#define APG_SMALL_OUTLINE 1
+#endif
+#ifndef APG_SMALL_WARP
+#define APG_SMALL_WARP 1
+#endif
+template <bool OUTLINE = false>
 __device__ __forceinline__ void load_line(const RoundArgs& A, int k, size_t i, Fr& lo, Fr& hi, bool store = true) {
   const Fr* t = table_in(A, k);
   const int bits = A.in_is_src && A.src_bits ? A.src_bits[k] : 0;
@@ -75,8 +86,14 @@ __device__ __forceinline__ void load_line(const RoundArgs& A, int k, size_t i, F
     a2 = ld_fe(&t[4 * i + 2]);
     a3 = ld_fe(&t[4 * i + 3]);
   }
-  lo = fe_add(a0, fe_mul(A.c, fe_sub(a1, a0)));
-  hi = fe_add(a2, fe_mul(A.c, fe_sub(a3, a2)));
+  if (OUTLINE) {
+    const FrPair f = rmul2(A.c, fe_sub(a1, a0), A.c, fe_sub(a3, a2));
+    lo = fe_add(a0, f.a);
+    hi = fe_add(a2, f.b);
+  } else {
+    lo = fe_add(a0, fe_mul(A.c, fe_sub(a1, a0)));
+    hi = fe_add(a2, fe_mul(A.c, fe_sub(a3, a2)));
+  }
   if (!store) return;
   Fr* o = A.out_base + (size_t)k * (A.in_len / 2);
   st_fe(&o[2 * i], lo);
@@ -304,19 +321,21 @@ __global__ void __launch_bounds__(kRoundThreads) k_round_pairs_small(RoundArgs A
     const int j = (int)(t - i * per);
     if (j >= T.n) {
       Fr lo, hi;
-      load_line(A, T.rest[j - T.n], i, lo, hi);
+      load_line<APG_SMALL_OUTLINE>(A, T.rest[j - T.n], i, lo, hi);
       continue;
     }
     Fr alo, ahi, blo, bhi, e_lo, e_hi;
-    load_line(A, T.a[j], i, alo, ahi);
-    load_line(A, T.b[j], i, blo, bhi);
-    load_line(A, A.nd, i, e_lo, e_hi, j == 0);
+    load_line<APG_SMALL_OUTLINE>(A, T.a[j], i, alo, ahi);
+    load_line<APG_SMALL_OUTLINE>(A, T.b[j], i, blo, bhi);
+    load_line<APG_SMALL_OUTLINE>(A, A.nd, i, e_lo, e_hi, j == 0);
     Fr cw = fe_add(e_lo, e_hi);  // the pair's eq weight without the current variable's factor
+    // The term's products at X = 0 and 2 (the lines at X = 2 are 2 hi - lo)
+    // and its weight, two at a time.
+    const FrPair p = rmul2(alo, blo, fe_sub(fe_add(ahi, ahi), alo), fe_sub(fe_add(bhi, bhi), blo));
     if (!T.unit[j]) cw = rmul(ld_fe(&T.c[j]), cw);
-    const Fr p0 = rmul(alo, blo);
-    const Fr p2 = rmul(fe_sub(fe_add(ahi, ahi), alo), fe_sub(fe_add(bhi, bhi), blo));  // the lines at X = 2
-    acc0 = fe_add(acc0, rmul(cw, p0));
-    acc2 = fe_add(acc2, rmul(cw, p2));
+    const FrPair wp = rmul2(cw, p.a, cw, p.b);
+    acc0 = fe_add(acc0, wp.a);
+    acc2 = fe_add(acc2, wp.b);
     if (n1) acc1 = fe_add(acc1, rmul(cw, rmul(ahi, bhi)));
   }
   const Fr accs[4] = {acc0, acc1, acc2, fe_zero<FrConsts>()};
@@ -342,6 +361,7 @@ __global__ void __launch_bounds__(kRoundThreads) k_round_pairs_small(RoundArgs A
 #ifndef APG_ROUND_WARP_MIN_BLOCKS
 #define APG_ROUND_WARP_MIN_BLOCKS 5
 #endif
+template <bool OUTLINE>
 __global__ void __launch_bounds__(kRoundThreads, APG_ROUND_WARP_MIN_BLOCKS) k_round_warp(RoundArgs A, DevProgram P, VirtualRound V,
                                                               Fr* partials) {
   extern __shared__ uint32_t sm_raw[];
@@ -357,7 +377,7 @@ __global__ void __launch_bounds__(kRoundThreads, APG_ROUND_WARP_MIN_BLOCKS) k_ro
   for (size_t i = (size_t)blockIdx.x * nwarps + warp; i < A.npairs; i += wstride) {
     Fr lo, hi;
     for (int k = lane; k <= A.nd; k += 32) {
-      load_line(A, k, i, lo, hi);
+      load_line<OUTLINE>(A, k, i, lo, hi);
       if (k < A.nd) {
         sm_st(S, k, lo);
         sm_st(S, A.slots_step0 + k, fe_sub(hi, lo));
@@ -385,7 +405,7 @@ __global__ void __launch_bounds__(kRoundThreads, APG_ROUND_WARP_MIN_BLOCKS) k_ro
           for (int w = 0; w < 8; ++w) o.v[w] = __shfl_xor_sync(0xffffffffu, part.v[w], off);
           part = fe_add(part, o);
         }
-        if (lane == 0) acc[x] = fe_add(acc[x], fe_mul(sm_ld(S, eq_slot), part));
+        if (lane == 0) acc[x] = fe_add(acc[x], OUTLINE ? rmul(sm_ld(S, eq_slot), part) : fe_mul(sm_ld(S, eq_slot), part));
       }
       __syncwarp();
       if (x == 0 && !((A.nodes >> 1) & 1)) {  // straight to node 2: lo + 2 step
@@ -577,7 +597,14 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
   const int warp_slots = n_val + n_cached + n_val + 2;
   const size_t warp_smem = (size_t)(kRoundThreads / 32) * warp_slots * 32;
   if (warp_mode && warp_smem > 200 * 1024) throw Error(APG_ERR_BAD_CIRCUIT, "gate list too wide for one thread block");
-  if (warp_mode) APG_CUDA(cudaFuncSetAttribute(k_round_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  if (warp_mode) APG_CUDA(cudaFuncSetAttribute(k_round_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  // Rounds with few enough pairs for one warp each in a single wave run one
+  // pair per warp whatever the list's width (APG_SMALL_WARP): the lanes fold
+  // the tables and evaluate the gates side by side, so a round's latency is a
+  // fold and a gate, not one thread's chain through every fold and gate.
+  const bool small_warp_ok = APG_SMALL_WARP && warp_smem <= 200 * 1024;
+  if (small_warp_ok)
+    APG_CUDA(cudaFuncSetAttribute(k_round_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   const int warp_max_blocks = c.sm_count * 16;
   Fr* partials = c.scratch[S_TMP6].as<Fr>((size_t)std::max(max_blocks, warp_max_blocks) * 4);
   Fr* d_out = c.scratch[S_RESULT].as<Fr>(4);
@@ -678,7 +705,10 @@ void run_sumcheck(Ctx& c, const DevProgram& prog, int nd, const std::vector<uint
              (int)std::min<size_t>((A.npairs * (size_t)(PT.n + PT.nrest) + kRoundThreads - 1) / kRoundThreads,
                                    (size_t)c.sm_count * 8),
              kRoundThreads, 0, A, PT, partials);
-    else if (warp_mode) launch(c, k_round_warp, blocks, kRoundThreads, warp_smem, A, P, V, partials);
+    else if (small_warp_ok && A.npairs * 32 <= (size_t)kRoundThreads * c.sm_count * 4)
+      launch(c, k_round_warp<true>, (int)((A.npairs + kRoundThreads / 32 - 1) / (kRoundThreads / 32)), kRoundThreads,
+             warp_smem, A, P, V, partials);
+    else if (warp_mode) launch(c, k_round_warp<false>, blocks, kRoundThreads, warp_smem, A, P, V, partials);
     else launch(c, k_round, blocks, threads, smem, A, P, V, partials);
     c.timer_end(APG_TIMER_SUMCHECK_ROUND, t0);
     APG_CUDA(cudaMemcpyAsync(sums, d_out, 128, cudaMemcpyDeviceToHost, c.stream));

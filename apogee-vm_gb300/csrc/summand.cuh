@@ -111,6 +111,19 @@ __device__ __forceinline__ Fr ld_g(const Fr* p) { return ld_fe(p); }
 // the round loop (no_instruction was the top stall of the round kernel).
 static __device__ __noinline__ Fr rmul(const Fr a, const Fr b) { return fe_mul(a, b); }
 
+// Two independent products in one out-of-line call, so their dependency
+// chains interleave (a small round's thread otherwise waits for each call in
+// turn).
+struct FrPair {
+  Fr a, b;
+};
+static __device__ __noinline__ FrPair rmul2(const Fr a, const Fr b, const Fr c, const Fr d) {
+  FrPair r;
+  r.a = fe_mul(a, b);
+  r.b = fe_mul(c, d);
+  return r;
+}
+
 // c[i] * x, skipping the product when bit i of `ones` marks c[i] = 1.
 __device__ __forceinline__ Fr cmul_coef(const Fr* c, int i, uint32_t ones, const Fr& x) {
   return (i < 32 && ((ones >> i) & 1u)) ? x : rmul(ld_g(&c[i]), x);
