@@ -19,6 +19,7 @@ restatement in oracle/, all host threads) on a bounded sample of the same
 workload and prints the same line with "impl": "reference".
 """
 import argparse
+import gc
 import json
 import math
 import os
@@ -813,9 +814,11 @@ def run_gpu(args):
     launches0 = ctx.launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     # The clock samples cover both timed legs; the sampler stops after the
-    # end-to-end leg, so its own shutdown falls in neither.
+    # end-to-end leg, so its own shutdown falls in neither. Python's garbage
+    # collector is paused over both legs (host pauses stall the steps).
     clk = ClockSampler(local)
     clk.__enter__()
+    gc.disable()
     ev0.record(stream)
     for _ in range(args.steps):
         cms = ctx.commit_batch_device(ptrs, log2n)
@@ -828,7 +831,7 @@ def run_gpu(args):
     value = weak_value(world, k * n, ms_step / 1e3)
 
     # End to end through the public API with host buffers.
-    for _ in range(1):
+    for _ in range(2):
         ctx.commit_batch_host(hptrs, log2n)
     e2e_steps = max(1, args.steps)
     barrier()
@@ -840,6 +843,7 @@ def run_gpu(args):
         marks.append(time.perf_counter())
     torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / e2e_steps
+    gc.enable()
     clk.__exit__(None, None, None)
     e2e_step_ms = [(b - a) * 1e3 for a, b in zip(marks, marks[1:])]
     barrier()
