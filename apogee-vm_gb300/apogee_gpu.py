@@ -525,6 +525,32 @@ class Context:
             return proof, snap.raw, point.raw[:32 * nv]
         return proof, snap.raw
 
+    def gkr_prove_sumcheck(self, blob: bytes, layer: int, weights, challenges: dict, eq_point, d_lower,
+                           d_upper, transcript: bytes):
+        """gkr::prove_sumcheck for gate list `layer` over device tables
+        (d_lower, and d_upper for a halving list: pointers to 2^len(eq_point)
+        Fr each). Returns (rounds as 4-tuples, point, finals, transcript), the
+        field elements as canonical ints."""
+        L = lib()
+        n, width = len(eq_point), len(d_lower)
+        slots = sorted(challenges)
+        sarr = (ctypes.c_uint32 * max(len(slots), 1))(*slots)
+        vals = to_mont_bytes([challenges[s] for s in slots])
+        lo = (ctypes.c_void_p * max(width, 1))(*d_lower)
+        up = (ctypes.c_void_p * max(width, 1))(*(d_upper or [0] * width))
+        snap = ctypes.create_string_buffer(bytes(transcript), TRANSCRIPT_BYTES)
+        rounds = ctypes.create_string_buffer(128 * max(n, 1))
+        point = ctypes.create_string_buffer(32 * max(n, 1))
+        finals = ctypes.create_string_buffer(64 * max(width, 1))
+        self._check(L.apg_gkr_prove_sumcheck(self._h, blob, ctypes.c_size_t(len(blob)), ctypes.c_size_t(layer),
+                                             to_mont_bytes(weights), ctypes.c_size_t(len(weights)), sarr, vals,
+                                             ctypes.c_size_t(len(slots)), to_mont_bytes(eq_point), ctypes.c_size_t(n),
+                                             lo, up, ctypes.c_size_t(width), snap, rounds, point, finals))
+        r = from_mont_bytes(rounds.raw[:128 * n])
+        nf = width * (2 if d_upper else 1)
+        return ([tuple(r[4 * i:4 * i + 4]) for i in range(n)], from_mont_bytes(point.raw[:32 * n]),
+                from_mont_bytes(finals.raw[:32 * nf]), snap.raw)
+
     def srs_share(self, src: "Context"):
         self._check(lib().apg_srs_share(self._h, src._h))
 

@@ -765,6 +765,18 @@ int apg_gkr_prove(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, apg_
   });
 }
 
+int apg_gkr_prove_sumcheck(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, size_t layer,
+                           const uint8_t* weights, size_t n_weights, const uint32_t* slots, const uint8_t* slot_values,
+                           size_t n_slots, const uint8_t* eq_point, size_t num_vars, const void* const* d_lower,
+                           const void* const* d_upper, size_t width, uint8_t* transcript, uint8_t* rounds_out,
+                           uint8_t* point_out, uint8_t* finals_out) {
+  return guarded(ctx, [&](Ctx& c) {
+    return gkr_prove_sumcheck_impl(c, circuit, circuit_len, layer, weights, n_weights, slots, slot_values, n_slots,
+                                   eq_point, num_vars, d_lower, d_upper, width, transcript, rounds_out, point_out,
+                                   finals_out);
+  });
+}
+
 int apg_gkr_forward_device(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, const void* const* d_base,
                            const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, apg_gkr_values** out) {
   if (!out) return APG_ERR_INVALID_ARGUMENT;

@@ -502,6 +502,74 @@ int gkr_prove_impl(Ctx& c, const uint8_t* blob, size_t blob_len, GkrValues* V, c
   return APG_OK;
 }
 
+// gkr::prove_sumcheck (crates/gkr/src/lib.rs:792-899) on its own: gate list
+// `layer`'s summand with the caller's weights over the caller's device tables
+// (the list's columns, and for a halving list their upper children), every
+// round absorbed and challenged on the caller's transcript. The same program,
+// tables and round kernels as gkr_prove_impl's step L2 for that list.
+int gkr_prove_sumcheck_impl(Ctx& c, const uint8_t* blob, size_t blob_len, size_t layer, const uint8_t* weights,
+                            size_t n_weights, const uint32_t* slots, const uint8_t* slot_values, size_t n_slots,
+                            const uint8_t* eq_point, size_t n, const void* const* d_lower,
+                            const void* const* d_upper, size_t width, uint8_t* transcript, uint8_t* rounds_out,
+                            uint8_t* point_out, uint8_t* finals_out) {
+  if (!transcript || !rounds_out || !point_out || !finals_out || (n && !eq_point) || (n_weights && !weights) ||
+      (n_slots && (!slots || !slot_values)))
+    return APG_ERR_INVALID_ARGUMENT;
+  const Circuit C = parse_circuit_blob(blob, blob_len);
+  if (layer >= C.layers.size()) {
+    c.last_error = "no such gate list";
+    return APG_ERR_INVALID_ARGUMENT;
+  }
+  const CLayer& L = C.layers[layer];
+  if (width != C.width(layer) || n != C.vars(layer + 1)) {
+    c.last_error = "the tables do not match the gate list (width, or the eq point's variables)";
+    return APG_ERR_INVALID_ARGUMENT;
+  }
+  if (n_weights != L.producing.size() + L.enforcing.size()) {
+    c.last_error = "one weight per producing and enforcing gate";
+    return APG_ERR_INVALID_ARGUMENT;
+  }
+  if (width && (!d_lower || (L.halving && !d_upper))) return APG_ERR_INVALID_ARGUMENT;
+  const Challenges ch = read_challenges(slots, slot_values, n_slots);
+  auto read_frs = [](const uint8_t* p, size_t k, std::vector<F>& out) {
+    out.resize(k);
+    for (size_t i = 0; i < k; ++i) {
+      memcpy(out[i].w, p + 32 * i, 32);
+      if (!host::below_p(out[i].w)) throw Error(APG_ERR_NONCANONICAL, "a field element is not below the modulus");
+    }
+  };
+  std::vector<F> w, point;
+  read_frs(weights, n_weights, w);
+  read_frs(eq_point, n, point);
+  host::Transcript tr;
+  if (!tr.load(transcript)) {
+    c.last_error = "malformed transcript snapshot";
+    return APG_ERR_INVALID_ARGUMENT;
+  }
+  HostProgram hp = layer_program(C, layer, ch, true, w);
+  DevProgram P;
+  upload_program(c, hp, P, 0);
+  std::vector<const Fr*> src;
+  std::vector<uint8_t> vkinds;
+  for (size_t x = 0; x < width; ++x) src.push_back(static_cast<const Fr*>(d_lower[x]));
+  if (L.halving)
+    for (size_t x = 0; x < width; ++x) src.push_back(static_cast<const Fr*>(d_upper[x]));
+  else
+    for (auto k : C.virtuals) vkinds.push_back((uint8_t)k);
+  std::vector<std::array<F, 4>> rounds;
+  std::vector<F> rho, finals;
+  HostPairTerms pairs;
+  const bool by_pairs = pair_terms_of(hp, (int)src.size(), pairs);
+  run_sumcheck(c, P, (int)src.size(), vkinds, (int)L.cached.size(), src, point, tr, rounds, rho, finals, {},
+               by_pairs ? &pairs : nullptr);
+  for (size_t r = 0; r < rounds.size(); ++r) memcpy(rounds_out + 128 * r, rounds[r].data(), 128);
+  memcpy(point_out, rho.data(), 32 * rho.size());
+  memcpy(finals_out, finals.data(), 32 * finals.size());
+  tr.save(transcript);
+  c.check_flags();
+  return APG_OK;
+}
+
 void gkr_values_free(GkrValues* v) { delete v; }
 
 size_t gkr_proof_len_impl(const uint8_t* blob, size_t len) { return 32 * gkr_proof_elems(parse_circuit_blob(blob, len)); }

@@ -108,6 +108,11 @@ GkrValues* gkr_forward_impl(Ctx& c, const uint8_t* blob, size_t blob_len, const 
 int gkr_prove_impl(Ctx& c, const uint8_t* blob, size_t blob_len, GkrValues* V, const uint32_t* slots,
                    const uint8_t* slot_values, size_t n_slots, uint8_t* transcript, uint8_t* proof_out,
                    size_t proof_cap, size_t* proof_len, uint8_t* point_out);
+int gkr_prove_sumcheck_impl(Ctx& c, const uint8_t* blob, size_t blob_len, size_t layer, const uint8_t* weights,
+                            size_t n_weights, const uint32_t* slots, const uint8_t* slot_values, size_t n_slots,
+                            const uint8_t* eq_point, size_t n, const void* const* d_lower,
+                            const void* const* d_upper, size_t width, uint8_t* transcript, uint8_t* rounds_out,
+                            uint8_t* point_out, uint8_t* finals_out);
 void gkr_values_free(GkrValues* v);
 int gkr_values_read_impl(GkrValues* v, size_t layer, size_t col, uint8_t* out);
 size_t gkr_values_len(GkrValues* v, size_t layer);

@@ -316,6 +316,31 @@ size_t apg_gkr_proof_len(const uint8_t* circuit, size_t circuit_len);
 int apg_gkr_prove(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, apg_gkr_values* values,
                   const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, uint8_t* transcript,
                   uint8_t* proof_out, size_t proof_cap, size_t* proof_len, uint8_t* point_out);
+/* gkr::prove_sumcheck (crates/gkr/src/lib.rs:792): one gate list's sumcheck
+ * of claim = sum_y eq(eq_point, y) S(y), S = sum_j weights[j] gate_j over the
+ * list's producing then enforcing gates (with the challenges of `slots`),
+ * one cubic per variable absorbed as SUMCHECK_ROUND and followed by its
+ * SUMCHECK_CHALLENGE on the caller's transcript (226-byte snapshot, in/out).
+ *   layer:    the gate list's index in the circuit blob;
+ *   weights:  n_weights Fr in memory, one per producing and enforcing gate;
+ *   eq_point: num_vars Fr in memory, num_vars = the variables of the list's
+ *             output (its rows' log, one less than its input's for a
+ *             halving list);
+ *   d_lower:  width device pointers to 2^num_vars Fr each, the list's input
+ *             columns (child 0 of each column for a halving list);
+ *   d_upper:  for a halving list, width device pointers to child 1 of each
+ *             column (ignored otherwise);
+ * Out: rounds_out 4 x num_vars Fr (ascending coefficients), point_out
+ * num_vars Fr (the bound point), finals_out the tables bound to that point
+ * (width Fr, then width more for a halving list). The caller's tables are
+ * read, not bound in place (the reference binds its tables; their bound
+ * values are finals_out). Virtual tables are evaluated in closed form, as in
+ * the reference. */
+int apg_gkr_prove_sumcheck(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, size_t layer,
+                           const uint8_t* weights, size_t n_weights, const uint32_t* slots, const uint8_t* slot_values,
+                           size_t n_slots, const uint8_t* eq_point, size_t num_vars, const void* const* d_lower,
+                           const void* const* d_upper, size_t width, uint8_t* transcript, uint8_t* rounds_out,
+                           uint8_t* point_out, uint8_t* finals_out);
 /* As apg_gkr_forward with the base columns already in device memory. */
 int apg_gkr_forward_device(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, const void* const* d_base,
                            const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, apg_gkr_values** out);

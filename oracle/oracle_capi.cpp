@@ -263,6 +263,43 @@ int oracle_gkr_prove(const uint8_t* blob, size_t blob_len, const uint8_t* base, 
   }
 }
 
+// gkr::prove_sumcheck (crates/gkr/src/lib.rs:792-899) for gate list `layer`
+// over the caller's tables (canonical Fr): `lower` holds width tables of 2^n
+// entries, `upper` (a halving list's child-1 tables) width more. Writes the
+// rounds (4n), the point (n) and the tables' bound values (lower then upper).
+int oracle_gkr_prove_sumcheck(const uint8_t* blob, size_t blob_len, size_t layer, const uint8_t* weights,
+                              size_t n_weights, const uint32_t* slots, const uint8_t* slot_values, size_t nslots,
+                              const uint8_t* eq_point, size_t n, const uint8_t* lower, const uint8_t* upper,
+                              size_t width, uint8_t* snap, uint8_t* rounds_out, uint8_t* point_out,
+                              uint8_t* finals_out) {
+  try {
+    Circuit c = parse_circuit(blob, blob_len);
+    if (layer >= c.layers.size()) return 2;
+    Challenges ch = read_challenges(slots, slot_values, nslots);
+    std::vector<Fr> w = n_weights ? read_tables(weights, 1, n_weights)[0] : std::vector<Fr>();
+    std::vector<Fr> pt = n ? read_tables(eq_point, 1, n)[0] : std::vector<Fr>();
+    std::vector<Table> lo = read_tables(lower, width, (size_t)1 << n), up;
+    if (c.layers[layer].halving) up = read_tables(upper, width, (size_t)1 << n);
+    Transcript tr;
+    if (!tr.restore(snap)) return 2;
+    auto rp = prove_layer_sumcheck(c, layer, pt, w, lo, up, ch, tr);
+    size_t off = 0;
+    for (auto& g : rp.first)
+      for (int j = 0; j < 4; ++j, off += 32) g[j].to_bytes(rounds_out + off);
+    for (size_t i = 0; i < rp.second.size(); ++i) rp.second[i].to_bytes(point_out + 32 * i);
+    off = 0;
+    for (auto* ts : {&lo, &up})
+      for (auto& t : *ts) {
+        t[0].to_bytes(finals_out + off);
+        off += 32;
+      }
+    tr.snapshot(snap);
+    return 0;
+  } catch (...) {
+    return 9;
+  }
+}
+
 int oracle_toy_srs(const uint8_t* tau, size_t count, size_t threads, uint8_t* out) {
   Fr t;
   if (!read_fr(tau, t)) return 2;
