@@ -111,9 +111,8 @@ __device__ __forceinline__ Fr ld_g(const Fr* p) { return ld_fe(p); }
 // the round loop (no_instruction was the top stall of the round kernel).
 static __device__ __noinline__ Fr rmul(const Fr a, const Fr b) { return fe_mul(a, b); }
 
-// Two independent products in one out-of-line call, so their dependency
-// chains interleave (a small round's thread otherwise waits for each call in
-// turn).
+// Two independent products in one out-of-line call: half the calls of a
+// small round's thread (its folds and node products come in pairs).
 struct FrPair {
   Fr a, b;
 };
