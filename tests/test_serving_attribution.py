@@ -1,6 +1,7 @@
 """The serving report's latency attribution (shard.latency_attribution): a
 band of requests between two latency quantiles, its mean latency, queueing
 and phases. Synthetic request times, no GPU."""
+import math
 import os
 import random
 import sys
@@ -42,8 +43,9 @@ def test_band_is_the_quantile_range_and_queue_stays_below_latency():
     assert top["requests"] == 3 and abs(top["latency_ms"] - sum(lat[197:]) / 3) < 1e-9
     assert lat[197] == shard.percentile(lat, 0.99)
     mid = shard.latency_attribution(times, 0.45, 0.55)
-    assert mid["requests"] == 21
-    assert lat[89] <= mid["latency_ms"] <= lat[109]
+    lo, hi = math.ceil(0.45 * 200) - 1, math.ceil(0.55 * 200)
+    assert mid["requests"] == hi - lo
+    assert abs(mid["latency_ms"] - sum(lat[lo:hi]) / (hi - lo)) < 1e-9
 
 
 def test_empty_and_single():
