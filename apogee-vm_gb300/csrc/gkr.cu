@@ -530,6 +530,11 @@ int gkr_prove_sumcheck_impl(Ctx& c, const uint8_t* blob, size_t blob_len, size_t
     return APG_ERR_INVALID_ARGUMENT;
   }
   if (width && (!d_lower || (L.halving && !d_upper))) return APG_ERR_INVALID_ARGUMENT;
+  for (size_t x = 0; x < width; ++x)
+    if (!d_lower[x] || (L.halving && !d_upper[x])) {
+      c.last_error = "a table pointer is null";
+      return APG_ERR_INVALID_ARGUMENT;
+    }
   const Challenges ch = read_challenges(slots, slot_values, n_slots);
   auto read_frs = [](const uint8_t* p, size_t k, std::vector<F>& out) {
     out.resize(k);

@@ -126,7 +126,8 @@ def test_refusals(ctx):
     for layer, weights, pt, tables in ((1, [1], point, ptrs),      # no such list
                                        (0, [1, 2], point, ptrs),   # one weight a gate
                                        (0, [1], point[:3], ptrs),  # eq point of the wrong length
-                                       (0, [1], point, ptrs[:1])):  # a column missing
+                                       (0, [1], point, ptrs[:1]),   # a column missing
+                                       (0, [1], point, [ptrs[0], 0])):  # a null table
         with pytest.raises(A.ApogeeError) as e:
             ctx.gkr_prove_sumcheck(blob, layer, weights, {}, pt, tables, None, snap)
         assert e.value.variant == "InvalidArgument"
