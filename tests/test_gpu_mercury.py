@@ -119,7 +119,9 @@ def test_open_matches_oracle(ctx, nv):
     assert after == bytes(osnap)
 
 
-@pytest.mark.parametrize("nv,k", [(4, 2), (8, 5), (10, 16)])
+# 32 and 40 columns: cm* summed on the host up to 32 commitments, through the
+# device MSM above that.
+@pytest.mark.parametrize("nv,k", [(4, 2), (8, 5), (10, 16), (6, 32), (6, 40)])
 def test_batch_open_matches_oracle(ctx, nv, k):
     import apogee_gpu as A
 
