@@ -360,6 +360,13 @@ class Context:
     def fr_to_mont_device(self, d_ptr: int, n: int):
         self._check(lib().apg_fr_to_mont_device(self._h, ctypes.c_void_p(d_ptr), ctypes.c_size_t(n)))
 
+    def synth_column(self, seed: int, kind: int, n: int, d_ptr: int):
+        """n seeded benchmark Fr (canonical, 8 LE u32 words each) into device
+        memory at d_ptr from the ChaCha20 keystream: kind 0 trace-like, kind 1
+        uniform Fr (the layout synth.py restates in numpy)."""
+        self._check(lib().apg_synth_column(self._h, ctypes.c_uint64(seed), ctypes.c_int(kind), ctypes.c_size_t(n),
+                                           ctypes.c_void_p(d_ptr)))
+
     def launch_count(self) -> int:
         f = lib().apg_ctx_launch_count
         f.restype = ctypes.c_uint64

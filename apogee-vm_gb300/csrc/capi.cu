@@ -524,6 +524,15 @@ int apg_fr_to_mont_device(apg_ctx* ctx, void* d_vals, size_t n) {
   });
 }
 
+int apg_synth_column(apg_ctx* ctx, uint64_t seed, int kind, size_t n, void* d_out) {
+  return guarded(ctx, [&](Ctx& c) {
+    if ((!d_out && n) || (kind != 0 && kind != 1) || n > ((size_t)1 << 32)) return (int)APG_ERR_INVALID_ARGUMENT;
+    synth_column(c, seed, kind, n, d_out);
+    c.check_flags();
+    return (int)APG_OK;
+  });
+}
+
 int apg_prove_zerocheck(apg_ctx* ctx, size_t arity, const uint8_t* coefs, const uint32_t* a, const uint32_t* b,
                         size_t nterms, const uint8_t* const* polys, size_t num_vars, uint8_t* transcript,
                         uint8_t* rounds_out, uint8_t* finals_out) {

@@ -217,6 +217,9 @@ void upload_points_async(Ctx& c, const uint8_t* host, size_t n, Affine* dst);
 void download_points(Ctx& c, const Affine* src, size_t n, uint8_t* host);
 // SRS [tau^i]G for i < n, generated on the device.
 void generate_srs(Ctx& c, const uint8_t tau_canonical[32], size_t n, Affine* dst);
+// n seeded benchmark Fr (canonical, 8 LE words each) from the ChaCha20 keystream:
+// kind 0 trace-like (bits, register words, uniform Fr), kind 1 uniform Fr.
+void synth_column(Ctx& c, uint64_t seed, int kind, size_t n, void* d_out);
 
 // Pippenger over device inputs; the result (canonical affine bytes, 64) is
 // written to device memory `out64` when non-null and returned to `host_out`

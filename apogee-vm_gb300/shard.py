@@ -28,6 +28,7 @@ import time
 
 import apogee_gpu as A
 import circuits as C
+import synth
 
 TAG_COMMITMENT = 3
 TAG_SHARD_SEED = 39
@@ -81,20 +82,13 @@ def shard_circuit(log_rows: int, cols: int) -> bytes:
 
 
 def device_columns(torch, n: int, k: int, seed: int, device: str, ctx):
-    """k columns of n Fr on the device (Montgomery), mixed like VM traces:
-    25% in {0,1}, 60% uniform u32, 15% uniform Fr below p's top limb."""
-    g = torch.Generator(device=device)
-    g.manual_seed(seed)
+    """k columns of n Fr on the device (Montgomery), mixed like VM traces
+    (25% in {0,1}, 60% uniform u32, 15% uniform Fr), generated by the
+    library from the ChaCha20 keystream of seed (seed << 16) + j for column
+    j: the same values synth.mixed_column gives on the host."""
     cols = []
-    for _ in range(k):
-        w = torch.randint(-(1 << 31), 1 << 31, (n, 8), dtype=torch.int32, device=device, generator=g)
-        cls = torch.rand(n, device=device, generator=g)
-        w[:, 7] &= 0x2FFFFFFF
-        small = cls < 0.85
-        w[small, 1:] = 0
-        bits = cls < 0.25
-        w[bits, 0] &= 1
-        flat = w.reshape(-1).contiguous()
+    for j in range(k):
+        flat = synth.device_column(ctx, torch, n, (seed << 16) + j, "mixed", device)
         ctx.fr_to_mont_device(flat.data_ptr(), n)
         cols.append(flat)
     return cols

@@ -306,7 +306,7 @@ def run_msm_only(args):
     ctx = A.Context(local)
     ctx.srs_generate((TAU_SEED * 0x9E3779B97F4A7C15) % A.P_R, n)
     ctx.srs_prepare()
-    tsample = torch.from_numpy(synth.mixed_column(n, SEED + 4242).view(np.int32).reshape(-1)).to(f"cuda:{local}")
+    tsample = synth.device_column(ctx, torch, n, SEED + 4242, "mixed", f"cuda:{local}")
     ctx.fr_to_mont_device(tsample.data_ptr(), n)
     # A fixed --window-bits keeps a profiled run's width independent of the
     # autotuner, whose timings a profiler distorts.
@@ -315,8 +315,7 @@ def run_msm_only(args):
     del tsample
     cols = []
     for j in range(args.cols):
-        gen = synth.mixed_column if args.scalars == "mixed" else synth.uniform_column
-        t = torch.from_numpy(gen(n, SEED + j).view(np.int32).reshape(-1)).to(f"cuda:{local}")
+        t = synth.device_column(ctx, torch, n, SEED + j, args.scalars, f"cuda:{local}")
         ctx.fr_to_mont_device(t.data_ptr(), n)
         cols.append(t)
     ptrs = [t.data_ptr() for t in cols]
@@ -471,16 +470,16 @@ def run_profile_family(args, ctx, torch, dev):
         # the rest 32-bit values.
         import numpy as np
 
-        nrng = np.random.Generator(np.random.PCG64(SEED))
+        import synth
+
+        key = synth.seed_key(SEED)
         n = 1 << args.log2n
         widths = [1 if j % 3 == 0 else 32 for j in range(circ.n_committed)]
         cols = []
-        for b in widths:
-            if b == 1:
-                raw = nrng.integers(0, 1 << 63, size=(n + 63) // 64, dtype=np.uint64)
-            else:
-                raw = nrng.integers(0, 1 << 32, size=n, dtype=np.uint64).astype(np.uint32)
-            cols.append(torch.from_numpy(raw.view(np.uint8).copy()).to(dev))
+        for j, b in enumerate(widths):
+            words = 2 * ((n + 63) // 64) if b == 1 else n  # 64-bit bitset words, or u32 values
+            raw = synth.chacha20_blocks(key, synth.stream_nonce(1000 + j), np.arange((words + 15) // 16))
+            cols.append(torch.from_numpy(raw.reshape(-1)[:words].view(np.uint8).copy()).to(dev))
     else:
         cols = shard.device_columns(torch, 1 << args.log2n, circ.n_committed, SEED, dev, ctx)
     ptrs = [t.data_ptr() for t in cols]
@@ -783,17 +782,18 @@ def run_gpu(args):
     ctx.srs_prepare()
     # Window widths per size class from the library's autotuner, on a sample
     # column drawn like the workload's (untimed setup).
-    tsample = torch.from_numpy(synth.mixed_column(n, SEED + 4242).view(np.int32).reshape(-1)).to(f"cuda:{local}")
+    tsample = synth.device_column(ctx, torch, n, SEED + 4242, "mixed", f"cuda:{local}")
     ctx.fr_to_mont_device(tsample.data_ptr(), n)
     tuned = ctx.msm_autotune(tsample.data_ptr(), n, 8, log2n, cands=TUNE_WIDTHS)
     del tsample
 
-    # Inputs: k mixed columns per rank, canonical on the host, Montgomery on
-    # the device and in a pinned host mirror for the end-to-end leg.
+    # Inputs: k mixed columns per rank, generated on the device from the
+    # seeded ChaCha20 keystream (the values synth.mixed_column gives on the
+    # host), Montgomery on the device and in a pinned host mirror for the
+    # end-to-end leg.
     dev_cols, host_cols = [], []
     for j in range(k):
-        col = synth.mixed_column(n, SEED + 1000 * rank + j)
-        t = torch.from_numpy(col.view(np.int32).reshape(-1)).to(f"cuda:{local}")
+        t = synth.device_column(ctx, torch, n, SEED + 1000 * rank + j, "mixed", f"cuda:{local}")
         ctx.fr_to_mont_device(t.data_ptr(), n)
         dev_cols.append(t)
         h = torch.empty_like(t, device="cpu").pin_memory()
@@ -850,7 +850,9 @@ def run_gpu(args):
     t_e2e = max_over_ranks(t_e2e, dist, f"cuda:{local}")
     assert cms_h == cms, "device-resident and host-buffer commits disagree"
     # The commitments timed above are checked, outside the timed region,
-    # against the known-tau identity cm = [f(tau)]G for one column per rank.
+    # against the known-tau identity cm = [f(tau)]G for one column per rank,
+    # the column drawn again on the host (so the check also holds the device
+    # generator to the host one).
     check_col = synth.mixed_column(n, SEED + 1000 * rank + (rank % k))
     if g1_generator_mul(poly_at_tau(check_col, tau, A.P_R)) != cms[rank % k]:
         print(json.dumps({"metric": METRIC, "error": f"column {rank % k}'s commitment is not [f(tau)]G"}),
@@ -876,8 +878,7 @@ def run_gpu(args):
            "h2d_copy_alone_ms": best_copy * 1e3, "h2d_gbs": k * n * 32 / best_copy / 1e9}
 
     # Roofline: the accumulation kernel on uniform 254-bit scalars.
-    ucol = synth.uniform_column(n, SEED + 999)
-    ut = torch.from_numpy(ucol.view(np.int32).reshape(-1)).to(f"cuda:{local}")
+    ut = synth.device_column(ctx, torch, n, SEED + 999, "uniform", f"cuda:{local}")
     ctx.fr_to_mont_device(ut.data_ptr(), n)
     ctx.commit_device(ut.data_ptr(), log2n)
     ctx.set_timing(True)

@@ -541,6 +541,13 @@ int apg_poseidon2_permute(uint8_t state[96]);
 /* Canonical Fr values in device memory -> Montgomery (in-memory) form, in
  * place; APG_ERR_NONCANONICAL if any value is >= p. */
 int apg_fr_to_mont_device(apg_ctx* ctx, void* d_vals, size_t n);
+/* Seeded benchmark input, not a reference interface: n canonical Fr (eight
+ * little-endian u32 words each) written to device memory from the ChaCha20
+ * keystream keyed by `seed`, the generator the reference's bench tool draws
+ * its inputs from (tools/bench/src/timing.rs:56-67 for the Fr rule: 32 bytes,
+ * top two bits cleared, rejected while >= r or zero). kind 0: trace-like
+ * (25% {0,1}, 60% u32, 15% uniform Fr); kind 1: uniform Fr. n <= 2^32. */
+int apg_synth_column(apg_ctx* ctx, uint64_t seed, int kind, size_t n, void* d_out);
 /* Kernels this context has launched since it was created. */
 uint64_t apg_ctx_launch_count(apg_ctx* ctx);
 
