@@ -27,7 +27,8 @@ STATUS = {
     0: "Ok", 1: "LengthMismatch", 2: "UnsupportedNumVars", 3: "PointLengthMismatch", 4: "SrsTooSmall",
     5: "DegenerateChallenge", 6: "EmptyBatch", 7: "BatchLengthMismatch", 8: "MixedColumnSizes",
     9: "InvalidPoint", 10: "MalformedAccumulator", 20: "NonCanonical", 21: "InvalidArgument", 22: "BadCircuit", 23: "NoSrs",
-    24: "Internal", 25: "NoAllocTooLarge", 26: "Pending", 27: "UnknownTicket", 100: "Cuda", 101: "OutOfMemory",
+    24: "Internal", 25: "NoAllocTooLarge", 26: "Pending", 27: "UnknownTicket", 28: "MissingChallenge",
+    29: "OutputShape", 30: "ProofShape", 31: "LayerInconsistency", 100: "Cuda", 101: "OutOfMemory",
     103: "NoDevice",
 }
 PENDING = 26
@@ -163,6 +164,50 @@ def transcript_challenge(snap: bytes, tag: int):
     if st:
         raise ApogeeError(st, "apg_transcript_challenge")
     return buf.raw, from_mont_bytes(out.raw)[0]
+
+
+# ---------------------------------------------------------------------------
+# The GKR verifier (crates/gkr-verify/src/lib.rs:647), host only
+# ---------------------------------------------------------------------------
+
+class GkrError(ApogeeError):
+    """gkr_verify::GkrError: `variant` is MissingChallenge, OutputShape,
+    ProofShape or LayerInconsistency; `info` the slot or gate list."""
+
+    def __init__(self, status: int, info: int):
+        super().__init__(status, f"info {info}")
+        self.info = info
+
+
+def gkr_verify(circuit: bytes, outputs, proof: bytes, challenges: dict, snap: bytes):
+    """gkr_verify::verify: the output tables (each a bytes of Fr in memory,
+    in the circuit's output-map order), the proof as apg_gkr_prove writes it,
+    the external challenges {slot: int} and the transcript bound to the base.
+    Returns (base point, base claim values, the advanced transcript) with
+    canonical ints; raises GkrError where the reference returns a GkrError."""
+    n_out = len(outputs)
+    bufs = [ctypes.create_string_buffer(bytes(o), max(len(o), 1)) for o in outputs]
+    ptrs = (ctypes.c_void_p * max(n_out, 1))(*[ctypes.cast(b, ctypes.c_void_p).value for b in bufs])
+    lens = (ctypes.c_size_t * max(n_out, 1))(*[len(o) // 32 for o in outputs])
+    slots = sorted(challenges)
+    sarr = (ctypes.c_uint32 * max(len(slots), 1))(*slots)
+    vals = to_mont_bytes([challenges[k] for k in slots])
+    tr = ctypes.create_string_buffer(bytes(snap), TRANSCRIPT_BYTES)
+    # The APGC header: magic, version, trace_vars, n_committed (u32 LE).
+    nv, ncols = (int.from_bytes(circuit[o:o + 4], "little") for o in (8, 12)) if len(circuit) >= 16 else (0, 0)
+    if nv > 40 or ncols > 1 << 20:
+        raise ApogeeError(22, "apg_gkr_verify: bad base shape")
+    point = ctypes.create_string_buffer(32 * max(nv, 1))
+    values = ctypes.create_string_buffer(32 * max(ncols, 1))
+    info = ctypes.c_uint64(0)
+    st = lib().apg_gkr_verify(circuit, ctypes.c_size_t(len(circuit)), ptrs, lens, ctypes.c_size_t(n_out), proof,
+                              ctypes.c_size_t(len(proof)), sarr, vals, ctypes.c_size_t(len(slots)), tr, point, values,
+                              ctypes.byref(info))
+    if st in (28, 29, 30, 31):
+        raise GkrError(st, info.value)
+    if st:
+        raise ApogeeError(st, "apg_gkr_verify")
+    return from_mont_bytes(point.raw[:32 * nv]), from_mont_bytes(values.raw[:32 * ncols]), tr.raw
 
 
 # ---------------------------------------------------------------------------

@@ -764,6 +764,20 @@ size_t apg_gkr_proof_len(const uint8_t* circuit, size_t circuit_len) {
   }
 }
 
+int apg_gkr_verify(const uint8_t* circuit, size_t circuit_len, const uint8_t* const* outputs,
+                   const size_t* output_lens, size_t n_outputs, const uint8_t* proof, size_t proof_len,
+                   const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, uint8_t* transcript,
+                   uint8_t* point_out, uint8_t* values_out, uint64_t* info) {
+  try {
+    return gkr_verify_impl(circuit, circuit_len, outputs, output_lens, n_outputs, proof, proof_len, slots,
+                           slot_values, n_slots, transcript, point_out, values_out, info);
+  } catch (const Error& e) {
+    return e.status;
+  } catch (...) {
+    return APG_ERR_INTERNAL;
+  }
+}
+
 int apg_gkr_prove(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, apg_gkr_values* values,
                   const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, uint8_t* transcript,
                   uint8_t* proof_out, size_t proof_cap, size_t* proof_len, uint8_t* point_out) {

@@ -18,27 +18,6 @@ namespace apg {
 
 using host::F;
 
-// ---- the circuit ------------------------------------------------------------
-
-struct CGate {
-  uint32_t kind, p1, p2;
-  std::vector<std::pair<uint32_t, uint32_t>> ops;  // (source, index)
-  std::vector<std::pair<bool, F>> coeffs;          // (is_challenge, literal value)
-  std::vector<uint32_t> slots;                     // challenge slots (parallel to coeffs)
-};
-struct CLayer {
-  bool halving;
-  uint32_t num_vars, width;
-  std::vector<CGate> cached, producing, enforcing;
-};
-struct Circuit {
-  uint32_t trace_vars = 0, n_committed = 0;
-  std::vector<uint32_t> virtuals, outputs;
-  std::vector<CLayer> layers;
-  uint32_t vars(size_t k) const { return k == 0 ? trace_vars : layers[k - 1].num_vars; }
-  uint32_t width(size_t k) const { return k == 0 ? n_committed : layers[k - 1].width; }
-};
-
 namespace {
 
 struct Cursor {
@@ -155,15 +134,6 @@ Circuit parse_circuit_blob(const uint8_t* blob, size_t len) {
   if (r.p != r.end) throw Error(APG_ERR_BAD_CIRCUIT, "trailing bytes after the circuit");
   return c;
 }
-
-struct Challenges {
-  std::vector<std::pair<uint32_t, F>> kv;
-  F get(uint32_t slot) const {
-    for (auto& p : kv)
-      if (p.first == slot) return p.second;
-    throw Error(APG_ERR_INVALID_ARGUMENT, "external challenge slot " + std::to_string(slot) + " has no value");
-  }
-};
 
 // Layer k's gate list as a device program. Slots: row-wise lists read the
 // layer's columns [0, w), the virtual tables [w, w + nv) and the cached
@@ -293,7 +263,7 @@ struct GkrValues {
   }
 };
 
-static Challenges read_challenges(const uint32_t* slots, const uint8_t* values, size_t n) {
+Challenges read_challenges(const uint32_t* slots, const uint8_t* values, size_t n) {
   Challenges ch;
   for (size_t i = 0; i < n; ++i) {
     F v;

@@ -97,7 +97,44 @@ int prove_zerocheck_impl(Ctx& c, size_t arity, const uint8_t* coefs, const uint3
                          const uint8_t* bits = nullptr);
 int witness_digest_impl(Ctx& c, const uint8_t* const* cols, size_t k, size_t num_vars, uint8_t out[32]);
 
-struct Circuit;
+// ---- a circuit in its resolved (APGC) form -------------------------------------
+
+struct CGate {
+  uint32_t kind, p1, p2;
+  std::vector<std::pair<uint32_t, uint32_t>> ops;  // (source, index)
+  std::vector<std::pair<bool, host::F>> coeffs;    // (is_challenge, literal value)
+  std::vector<uint32_t> slots;                     // challenge slots (parallel to coeffs)
+};
+struct CLayer {
+  bool halving;
+  uint32_t num_vars, width;
+  std::vector<CGate> cached, producing, enforcing;
+};
+struct Circuit {
+  uint32_t trace_vars = 0, n_committed = 0;
+  std::vector<uint32_t> virtuals, outputs;
+  std::vector<CLayer> layers;
+  uint32_t vars(size_t k) const { return k == 0 ? trace_vars : layers[k - 1].num_vars; }
+  uint32_t width(size_t k) const { return k == 0 ? n_committed : layers[k - 1].width; }
+};
+
+// The external challenges, slot -> value (Fr in memory).
+struct Challenges {
+  std::vector<std::pair<uint32_t, host::F>> kv;
+  bool has(uint32_t slot) const {
+    for (auto& p : kv)
+      if (p.first == slot) return true;
+    return false;
+  }
+  host::F get(uint32_t slot) const {
+    for (auto& p : kv)
+      if (p.first == slot) return p.second;
+    throw Error(APG_ERR_INVALID_ARGUMENT, "external challenge slot " + std::to_string(slot) + " has no value");
+  }
+};
+// Values below p or APG_ERR_NONCANONICAL.
+Challenges read_challenges(const uint32_t* slots, const uint8_t* values, size_t n);
+
 struct GkrValues;
 Circuit parse_circuit_blob(const uint8_t* blob, size_t len);
 size_t gkr_proof_elems(const Circuit& C);
@@ -118,6 +155,11 @@ int gkr_values_read_impl(GkrValues* v, size_t layer, size_t col, uint8_t* out);
 size_t gkr_values_len(GkrValues* v, size_t layer);
 size_t gkr_proof_len_impl(const uint8_t* blob, size_t len);
 size_t gkr_device_bytes_impl(const uint8_t* blob, size_t len);
+// gkr_verify::verify on the host; `info` receives the failing slot or layer.
+int gkr_verify_impl(const uint8_t* blob, size_t blob_len, const uint8_t* const* outputs, const size_t* output_lens,
+                    size_t n_outputs, const uint8_t* proof, size_t proof_len, const uint32_t* slots,
+                    const uint8_t* slot_values, size_t n_slots, uint8_t* transcript, uint8_t* point_out,
+                    uint8_t* values_out, uint64_t* info);
 
 int mercury_open_impl(Ctx& c, const Fr* d_f, size_t nv, const uint8_t cm[64], const std::vector<host::F>& u,
                       host::Transcript& tr, host::F& v_out, uint8_t proof_out[704]);

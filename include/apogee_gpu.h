@@ -57,6 +57,10 @@ enum apg_status {
   APG_ERR_NOALLOC_TOO_LARGE = 25,     /* apg_msm_noalloc: more bases than its fixed scratch holds */
   APG_PENDING = 26,                   /* apg_poll: the request is queued or running */
   APG_ERR_UNKNOWN_TICKET = 27,        /* apg_poll / apg_wait: no such request */
+  APG_ERR_MISSING_CHALLENGE = 28,     /* GkrError::MissingChallenge (info: the slot) */
+  APG_ERR_OUTPUT_SHAPE = 29,          /* GkrError::OutputShape */
+  APG_ERR_PROOF_SHAPE = 30,           /* GkrError::ProofShape (info: the gate list) */
+  APG_ERR_LAYER_INCONSISTENCY = 31,   /* GkrError::LayerInconsistency (info: the gate list) */
   APG_ERR_CUDA = 100,                 /* a CUDA call failed */
   APG_ERR_OUT_OF_MEMORY = 101,        /* device allocation refused */
   APG_ERR_NO_DEVICE = 103             /* no usable CUDA device */
@@ -316,6 +320,29 @@ size_t apg_gkr_proof_len(const uint8_t* circuit, size_t circuit_len);
 int apg_gkr_prove(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, apg_gkr_values* values,
                   const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, uint8_t* transcript,
                   uint8_t* proof_out, size_t proof_cap, size_t* proof_len, uint8_t* point_out);
+/* gkr_verify::verify (crates/gkr-verify/src/lib.rs:647): reduce the output
+ * claims to claims about the committed base columns, or reject. Host only
+ * (no context, no device work).
+ *   outputs:   n_outputs tables in the circuit's output-map order, table i
+ *              output_lens[i] Fr in memory (2^top_vars each);
+ *   proof:     as apg_gkr_prove writes it (proof_len bytes);
+ *   slots / slot_values: the external challenges (Fr in memory);
+ *   transcript: 226-byte snapshot bound to the base as the prover's was;
+ *              advanced in place on success, left unchanged on failure.
+ * Out: point_out (trace_vars Fr) and values_out (n_committed Fr): the base
+ * claims (BaseClaim, one per committed column, all at one point).
+ * Checks in the reference's order: APG_ERR_MISSING_CHALLENGE (*info = the
+ * first missing slot, lists bottom up), APG_ERR_OUTPUT_SHAPE,
+ * APG_ERR_PROOF_SHAPE (*info = the first gate list whose rounds and claims
+ * do not fit in proof_len, or depth when bytes are left over),
+ * APG_ERR_LAYER_INCONSISTENCY (*info = the gate list whose round or final
+ * check failed). info is nullable. As in the reference, the enforcing gates'
+ * claims are zero: a circuit whose enforcing gates do not vanish is
+ * rejected. */
+int apg_gkr_verify(const uint8_t* circuit, size_t circuit_len, const uint8_t* const* outputs,
+                   const size_t* output_lens, size_t n_outputs, const uint8_t* proof, size_t proof_len,
+                   const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, uint8_t* transcript,
+                   uint8_t* point_out, uint8_t* values_out, uint64_t* info);
 /* gkr::prove_sumcheck (crates/gkr/src/lib.rs:792): one gate list's sumcheck
  * of claim = sum_y eq(eq_point, y) S(y), S = sum_j weights[j] gate_j over the
  * list's producing then enforcing gates (with the challenges of `slots`),
