@@ -558,6 +558,7 @@ def run_shard_workloads(ctx, local, serve_budget_gb=150):
     import apogee_gpu as A
     import circuits as Cm
     import shard
+    import synth
 
     dev = f"cuda:{local}"
     out = {}
@@ -574,8 +575,13 @@ def run_shard_workloads(ctx, local, serve_budget_gb=150):
         return best
 
     # Config 1: commit one 2^16 column, then zerocheck of a*b over two columns
-    # (witness digest absorbed first), challenges from the seeded duplex.
-    cols = shard.device_columns(torch, 1 << 16, 2, SEED + 1, dev, ctx)
+    # (witness digest absorbed first), challenges from the seeded duplex. The
+    # two columns are uniform Fr.
+    cols = []
+    for j in range(2):
+        c = synth.device_column(ctx, torch, 1 << 16, ((SEED + 1) << 16) + j, "uniform", dev)
+        ctx.fr_to_mont_device(c.data_ptr(), 1 << 16)
+        cols.append(c)
     host_cols = [bytes(c.cpu().numpy().tobytes()) for c in cols]
 
     def cfg1():
