@@ -28,7 +28,8 @@ STATUS = {
     5: "DegenerateChallenge", 6: "EmptyBatch", 7: "BatchLengthMismatch", 8: "MixedColumnSizes",
     9: "InvalidPoint", 10: "MalformedAccumulator", 20: "NonCanonical", 21: "InvalidArgument", 22: "BadCircuit", 23: "NoSrs",
     24: "Internal", 25: "NoAllocTooLarge", 26: "Pending", 27: "UnknownTicket", 28: "MissingChallenge",
-    29: "OutputShape", 30: "ProofShape", 31: "LayerInconsistency", 100: "Cuda", 101: "OutOfMemory",
+    29: "OutputShape", 30: "ProofShape", 31: "LayerInconsistency", 32: "RoundCountMismatch",
+    33: "FinalEvalCountMismatch", 34: "RoundSumMismatch", 35: "FinalEvalMismatch", 100: "Cuda", 101: "OutOfMemory",
     103: "NoDevice",
 }
 PENDING = 26
@@ -208,6 +209,40 @@ def gkr_verify(circuit: bytes, outputs, proof: bytes, challenges: dict, snap: by
     if st:
         raise ApogeeError(st, "apg_gkr_verify")
     return from_mont_bytes(point.raw[:32 * nv]), from_mont_bytes(values.raw[:32 * ncols]), tr.raw
+
+
+class SumcheckError(ApogeeError):
+    """sumcheck::SumcheckError: `variant` is RoundCountMismatch,
+    FinalEvalCountMismatch, RoundSumMismatch or FinalEvalMismatch; `info`
+    the count found or the round."""
+
+    def __init__(self, status: int, info: int):
+        super().__init__(status, f"info {info}")
+        self.info = info
+
+
+def verify_zerocheck(terms, arity: int, num_vars: int, rounds, finals, snap: bytes):
+    """sumcheck::verify_zerocheck over the gate `terms` ((coef, a, b-or-None),
+    as prove_zerocheck takes them) of `arity` inputs: rounds as 4-tuples and
+    finals as canonical ints. Returns (the claim's point, the advanced
+    transcript); raises SumcheckError where the reference does."""
+    nt = len(terms)
+    coefs = to_mont_bytes([t[0] for t in terms])
+    ta = (ctypes.c_uint32 * max(nt, 1))(*[t[1] for t in terms])
+    tb = (ctypes.c_uint32 * max(nt, 1))(*[0xFFFFFFFF if t[2] is None else t[2] for t in terms])
+    rb = to_mont_bytes([x for g in rounds for x in g])
+    fb = to_mont_bytes(list(finals))
+    tr = ctypes.create_string_buffer(bytes(snap), TRANSCRIPT_BYTES)
+    point = ctypes.create_string_buffer(32 * max(num_vars, 1))
+    info = ctypes.c_uint64(0)
+    st = lib().apg_verify_zerocheck(ctypes.c_size_t(arity), coefs, ta, tb, ctypes.c_size_t(nt),
+                                    ctypes.c_size_t(num_vars), rb, ctypes.c_size_t(len(rounds)), fb,
+                                    ctypes.c_size_t(len(finals)), tr, point, ctypes.byref(info))
+    if st in (32, 33, 34, 35):
+        raise SumcheckError(st, info.value)
+    if st:
+        raise ApogeeError(st, "apg_verify_zerocheck")
+    return from_mont_bytes(point.raw[:32 * num_vars]), tr.raw
 
 
 # ---------------------------------------------------------------------------

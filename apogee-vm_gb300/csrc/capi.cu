@@ -778,6 +778,19 @@ int apg_gkr_verify(const uint8_t* circuit, size_t circuit_len, const uint8_t* co
   }
 }
 
+int apg_verify_zerocheck(size_t arity, const uint8_t* coefs, const uint32_t* a, const uint32_t* b, size_t nterms,
+                         size_t num_vars, const uint8_t* rounds, size_t n_rounds, const uint8_t* finals,
+                         size_t n_finals, uint8_t* transcript, uint8_t* point_out, uint64_t* info) {
+  try {
+    return verify_zerocheck_impl(arity, coefs, a, b, nterms, num_vars, rounds, n_rounds, finals, n_finals,
+                                 transcript, point_out, info);
+  } catch (const Error& e) {
+    return e.status;
+  } catch (...) {
+    return APG_ERR_INTERNAL;
+  }
+}
+
 int apg_gkr_prove(apg_ctx* ctx, const uint8_t* circuit, size_t circuit_len, apg_gkr_values* values,
                   const uint32_t* slots, const uint8_t* slot_values, size_t n_slots, uint8_t* transcript,
                   uint8_t* proof_out, size_t proof_cap, size_t* proof_len, uint8_t* point_out) {

@@ -1,6 +1,8 @@
-// The GKR verifier on the host: gkr_verify::verify
+// The verifiers on the host: gkr_verify::verify
 // (crates/gkr-verify/src/lib.rs:647-748) over a circuit in its APGC form and
-// a proof as apg_gkr_prove writes it.
+// a proof as apg_gkr_prove writes it, and sumcheck::verify_zerocheck
+// (crates/sumcheck/src/lib.rs:418-473) over a proof as apg_prove_zerocheck
+// writes it.
 //
 // Every step is a few field products a round except the first: the output
 // tables are absorbed into the transcript (one Poseidon2 permutation per two
@@ -308,6 +310,63 @@ int gkr_verify_impl(const uint8_t* blob, size_t blob_len, const uint8_t* const* 
   // The base claims: every committed column at one point.
   memcpy(point_out, point.data(), 32 * point.size());
   memcpy(values_out, values.data(), 32 * values.size());
+  tr.save(transcript);
+  return APG_OK;
+}
+
+// sumcheck::verify_zerocheck (crates/sumcheck/src/lib.rs:418-473): the round
+// and final counts, the n point challenges drawn up front (the eq point r),
+// each round's g(0) + g(1) against the claim (zero in round 0), the finals
+// absorbed, then eq(r, point) G(finals) against the last claim. `info`
+// receives the count found or the failing round.
+int verify_zerocheck_impl(size_t arity, const uint8_t* coefs, const uint32_t* ta, const uint32_t* tb, size_t nterms,
+                          size_t num_vars, const uint8_t* rounds, size_t n_rounds, const uint8_t* finals,
+                          size_t n_finals, uint8_t* transcript, uint8_t* point_out, uint64_t* info) {
+  if (info) *info = 0;
+  if (arity == 0 || !transcript || !point_out || (nterms && (!coefs || !ta || !tb)) || (n_rounds && !rounds) ||
+      (n_finals && !finals))
+    return APG_ERR_INVALID_ARGUMENT;
+  std::vector<F> cf(nterms);
+  for (size_t t = 0; t < nterms; ++t) {
+    cf[t] = read_fr(coefs + 32 * t);
+    if (ta[t] >= arity || (tb[t] != 0xffffffffu && tb[t] >= arity)) return APG_ERR_INVALID_ARGUMENT;
+  }
+  auto fail = [&](int status, uint64_t what) {
+    if (info) *info = what;
+    return status;
+  };
+  if (n_rounds != num_vars) return fail(APG_ERR_ROUND_COUNT_MISMATCH, n_rounds);
+  if (n_finals != arity) return fail(APG_ERR_FINAL_COUNT_MISMATCH, n_finals);
+  std::vector<std::array<F, 4>> g(n_rounds);
+  for (size_t i = 0; i < n_rounds; ++i)
+    for (int e = 0; e < 4; ++e) g[i][e] = read_fr(rounds + 32 * (4 * i + e));
+  std::vector<F> fin(n_finals);
+  for (size_t k = 0; k < n_finals; ++k) fin[k] = read_fr(finals + 32 * k);
+
+  host::Transcript tr;
+  if (!tr.load(transcript)) return APG_ERR_INVALID_ARGUMENT;
+  std::vector<F> r;
+  for (size_t i = 0; i < num_vars; ++i) r.push_back(tr.challenge(host::T_SUMCHECK_CHALLENGE));
+  F claim = host::fzero();
+  std::vector<F> point;
+  for (size_t i = 0; i < n_rounds; ++i) {
+    if (host::fadd(cubic(g[i].data(), host::fzero()), cubic(g[i].data(), host::fone())) != claim)
+      return fail(APG_ERR_ROUND_SUM_MISMATCH, i);
+    tr.absorb(host::T_SUMCHECK_ROUND, g[i].data(), 4);
+    const F c = tr.challenge(host::T_SUMCHECK_CHALLENGE);
+    claim = cubic(g[i].data(), c);
+    point.push_back(c);
+  }
+  tr.absorb(host::T_SUMCHECK_FINAL_EVALS, fin);
+  // Gate::evaluate (lib.rs:151-165): sum_t coef_t x_a (x_b).
+  F gate = host::fzero();
+  for (size_t t = 0; t < nterms; ++t) {
+    F term = host::fmul(cf[t], fin[ta[t]]);
+    if (tb[t] != 0xffffffffu) term = host::fmul(term, fin[tb[t]]);
+    gate = host::fadd(gate, term);
+  }
+  if (host::fmul(eq_eval(r, point), gate) != claim) return fail(APG_ERR_FINAL_EVAL_MISMATCH, 0);
+  memcpy(point_out, point.data(), 32 * point.size());
   tr.save(transcript);
   return APG_OK;
 }

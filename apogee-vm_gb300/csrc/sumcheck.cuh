@@ -160,6 +160,10 @@ int gkr_verify_impl(const uint8_t* blob, size_t blob_len, const uint8_t* const* 
                     size_t n_outputs, const uint8_t* proof, size_t proof_len, const uint32_t* slots,
                     const uint8_t* slot_values, size_t n_slots, uint8_t* transcript, uint8_t* point_out,
                     uint8_t* values_out, uint64_t* info);
+// sumcheck::verify_zerocheck on the host; `info` receives a count or a round.
+int verify_zerocheck_impl(size_t arity, const uint8_t* coefs, const uint32_t* ta, const uint32_t* tb, size_t nterms,
+                          size_t num_vars, const uint8_t* rounds, size_t n_rounds, const uint8_t* finals,
+                          size_t n_finals, uint8_t* transcript, uint8_t* point_out, uint64_t* info);
 
 int mercury_open_impl(Ctx& c, const Fr* d_f, size_t nv, const uint8_t cm[64], const std::vector<host::F>& u,
                       host::Transcript& tr, host::F& v_out, uint8_t proof_out[704]);

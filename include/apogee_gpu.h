@@ -61,6 +61,10 @@ enum apg_status {
   APG_ERR_OUTPUT_SHAPE = 29,          /* GkrError::OutputShape */
   APG_ERR_PROOF_SHAPE = 30,           /* GkrError::ProofShape (info: the gate list) */
   APG_ERR_LAYER_INCONSISTENCY = 31,   /* GkrError::LayerInconsistency (info: the gate list) */
+  APG_ERR_ROUND_COUNT_MISMATCH = 32,  /* SumcheckError::RoundCountMismatch (info: rounds found) */
+  APG_ERR_FINAL_COUNT_MISMATCH = 33,  /* SumcheckError::FinalEvalCountMismatch (info: finals found) */
+  APG_ERR_ROUND_SUM_MISMATCH = 34,    /* SumcheckError::RoundSumMismatch (info: the round) */
+  APG_ERR_FINAL_EVAL_MISMATCH = 35,   /* SumcheckError::FinalEvalMismatch */
   APG_ERR_CUDA = 100,                 /* a CUDA call failed */
   APG_ERR_OUT_OF_MEMORY = 101,        /* device allocation refused */
   APG_ERR_NO_DEVICE = 103             /* no usable CUDA device */
@@ -242,6 +246,21 @@ int apg_mercury_batch_open_stacked_device(apg_ctx* ctx, const void* const* d_col
 
 /* ---- zerocheck (crates/sumcheck/src/lib.rs) ------------------------------ */
 
+/* sumcheck::verify_zerocheck (lib.rs:418): check a zerocheck proof of the
+ * gate (terms as for apg_prove_zerocheck) over num_vars variables. Host only
+ * (no context). rounds: n_rounds x 4 Fr in memory (ascending coefficients),
+ * finals: n_finals Fr in memory, as apg_prove_zerocheck writes them. The
+ * transcript (226-byte snapshot) must have been driven as the prover's was,
+ * the witness digest included; it is advanced in place on success and left
+ * unchanged on failure. point_out (num_vars Fr) receives SumcheckClaim::point
+ * (its final_evals are the caller's finals). Errors in the reference's order:
+ * APG_ERR_ROUND_COUNT_MISMATCH (*info = n_rounds), APG_ERR_FINAL_COUNT_MISMATCH
+ * (*info = n_finals), APG_ERR_ROUND_SUM_MISMATCH (*info = the round),
+ * APG_ERR_FINAL_EVAL_MISMATCH; a gate with no inputs or a term naming an
+ * undeclared input is APG_ERR_INVALID_ARGUMENT (GateError). */
+int apg_verify_zerocheck(size_t arity, const uint8_t* coefs, const uint32_t* a, const uint32_t* b, size_t nterms,
+                         size_t num_vars, const uint8_t* rounds, size_t n_rounds, const uint8_t* finals,
+                         size_t n_finals, uint8_t* transcript, uint8_t* point_out, uint64_t* info);
 /* sumcheck::prove_zerocheck (lib.rs:359): prove that the gate
  *   G = sum_t coefs[t] * x_{a[t]} * x_{b[t]}   (b[t] = 0xffffffff: no 2nd factor)
  * over `arity` columns of 2^num_vars evaluations vanishes on the hypercube.

@@ -143,3 +143,23 @@ def test_zerocheck_narrow_rejects_bad_width(ctx):
     with pytest.raises(A.ApogeeError) as e:
         ctx.prove_zerocheck_narrow([(1, 0, 1)], cols, [1, 4], 6, A.transcript_init())
     assert e.value.variant == "InvalidArgument"
+
+
+@pytest.mark.parametrize("nv", [3, 16])
+def test_device_proof_of_a_vanishing_gate_verifies(ctx, nv):
+    """The device's proof of a gate that vanishes on its columns passes the
+    library's verifier (sumcheck::verify_zerocheck on the host), which
+    leaves the transcript where the prover left it."""
+    import apogee_gpu as A
+    from test_verify_zerocheck import _satisfied
+
+    rng = random.Random(80 + nv)
+    terms, cols = _satisfied(rng, nv)
+    snap = A.transcript_append_scalars(A.transcript_init(), 8, [nv])
+    rounds, finals, after = ctx.prove_zerocheck(terms, [A.to_mont_bytes(c) for c in cols], nv, snap)
+    point, tr = A.verify_zerocheck(terms, len(cols), nv, rounds, finals, snap)
+    assert tr == after and len(point) == nv
+    bad = list(finals)
+    bad[0] = (bad[0] + 1) % O.P_R
+    with pytest.raises(A.SumcheckError):
+        A.verify_zerocheck(terms, len(cols), nv, rounds, bad, snap)
