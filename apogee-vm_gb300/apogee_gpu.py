@@ -211,6 +211,49 @@ def gkr_verify(circuit: bytes, outputs, proof: bytes, challenges: dict, snap: by
     return from_mont_bytes(point.raw[:32 * nv]), from_mont_bytes(values.raw[:32 * ncols]), tr.raw
 
 
+class VerifyPcsError(PcsError):
+    """pcs_verify::PcsError from a verification: `info` names the refused
+    point (0..7 the proof's h, q, g, s, d, pi_z, w, w'; 8 a commitment)."""
+
+    def __init__(self, status: int, info: int):
+        super().__init__(status, f"info {info}")
+        self.info = info
+
+
+def _deferred_result(st, info, sides, scalars, points, tr, name):
+    if st in PCS_CODES:
+        raise VerifyPcsError(st, info.value)
+    if st:
+        raise ApogeeError(st, name)
+    return (bytes(sides.raw[:12]), from_mont_bytes(scalars.raw[:12 * 32]),
+            [points.raw[64 * i:64 * i + 64] for i in range(12)], tr.raw)
+
+
+def mercury_verify_deferred(cm: bytes, u, v: int, proof: bytes, snap: bytes):
+    """pcs::verify_deferred: the commitment (64 bytes), the point u and the
+    value v (canonical ints), the 704-byte proof and the transcript before
+    the opening. Returns (sides, scalars, points, transcript after): the
+    twelve accumulator entries, scalars as canonical ints."""
+    sides, scalars, points = (ctypes.create_string_buffer(n) for n in (12, 12 * 32, 12 * 64))
+    tr = ctypes.create_string_buffer(bytes(snap), TRANSCRIPT_BYTES)
+    info = ctypes.c_uint64(0)
+    st = lib().apg_mercury_verify_deferred(bytes(cm), to_mont_bytes(u), ctypes.c_size_t(len(u)), to_mont_bytes([v]),
+                                           bytes(proof), tr, sides, scalars, points, ctypes.byref(info))
+    return _deferred_result(st, info, sides, scalars, points, tr, "apg_mercury_verify_deferred")
+
+
+def mercury_batch_verify_deferred(cms, u, vs, proof: bytes, snap: bytes):
+    """pcs::batch_verify_deferred over k commitments (64 bytes each) claimed
+    to open to vs at u. Returns what mercury_verify_deferred returns."""
+    sides, scalars, points = (ctypes.create_string_buffer(n) for n in (12, 12 * 32, 12 * 64))
+    tr = ctypes.create_string_buffer(bytes(snap), TRANSCRIPT_BYTES)
+    info = ctypes.c_uint64(0)
+    st = lib().apg_mercury_batch_verify_deferred(b"".join(cms), ctypes.c_size_t(len(cms)), to_mont_bytes(u),
+                                                 ctypes.c_size_t(len(u)), to_mont_bytes(vs), ctypes.c_size_t(len(vs)),
+                                                 bytes(proof), tr, sides, scalars, points, ctypes.byref(info))
+    return _deferred_result(st, info, sides, scalars, points, tr, "apg_mercury_batch_verify_deferred")
+
+
 class SumcheckError(ApogeeError):
     """sumcheck::SumcheckError: `variant` is RoundCountMismatch,
     FinalEvalCountMismatch, RoundSumMismatch or FinalEvalMismatch; `info`

@@ -778,6 +778,33 @@ int apg_gkr_verify(const uint8_t* circuit, size_t circuit_len, const uint8_t* co
   }
 }
 
+int apg_mercury_verify_deferred(const uint8_t cm[64], const uint8_t* u, size_t u_len, const uint8_t v[32],
+                                const uint8_t proof[704], uint8_t* transcript, uint8_t sides_out[12],
+                                uint8_t* scalars_out, uint8_t* points_out, uint64_t* info) {
+  try {
+    return mercury_verify_deferred_impl(cm, u, u_len, v, proof, transcript, sides_out, scalars_out, points_out,
+                                        info);
+  } catch (const Error& e) {
+    return e.status;
+  } catch (...) {
+    return APG_ERR_INTERNAL;
+  }
+}
+
+int apg_mercury_batch_verify_deferred(const uint8_t* cms, size_t k, const uint8_t* u, size_t u_len,
+                                      const uint8_t* vs, size_t n_vs, const uint8_t proof[704], uint8_t* transcript,
+                                      uint8_t sides_out[12], uint8_t* scalars_out, uint8_t* points_out,
+                                      uint64_t* info) {
+  try {
+    return mercury_batch_verify_deferred_impl(cms, k, u, u_len, vs, n_vs, proof, transcript, sides_out, scalars_out,
+                                              points_out, info);
+  } catch (const Error& e) {
+    return e.status;
+  } catch (...) {
+    return APG_ERR_INTERNAL;
+  }
+}
+
 int apg_verify_zerocheck(size_t arity, const uint8_t* coefs, const uint32_t* a, const uint32_t* b, size_t nterms,
                          size_t num_vars, const uint8_t* rounds, size_t n_rounds, const uint8_t* finals,
                          size_t n_finals, uint8_t* transcript, uint8_t* point_out, uint64_t* info) {

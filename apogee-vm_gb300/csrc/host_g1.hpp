@@ -260,6 +260,22 @@ inline std::vector<Aff> to_affine(const std::vector<Jac>& pts) {
 // A canonical 64-byte encoding (x || y, little-endian; all zero = infinity)
 // as a Jacobian point. The caller has validated it (coordinates below q, on
 // the curve).
+// A canonical 64-byte encoding (x then y, little-endian) of a point on
+// y^2 = x^3 + 3, or all zero (the point at infinity). G1 has cofactor 1, so a
+// point on the curve is in the order-r subgroup.
+inline bool valid_encoding(const uint8_t b[64]) {
+  bool inf = true;
+  for (int i = 0; i < 64; ++i) inf &= b[i] == 0;
+  if (inf) return true;
+  uint64_t x[4], y[4];
+  memcpy(x, b, 32);
+  memcpy(y, b + 32, 32);
+  if (QConsts::geq_q(x) || QConsts::geq_q(y)) return false;
+  const uint64_t three[4] = {3, 0, 0, 0};
+  const Q X = q_from_canonical(x), Y = q_from_canonical(y);
+  return qeq(qmul(Y, Y), qadd(qmul(qmul(X, X), X), q_from_canonical(three)));
+}
+
 inline Jac jfrom_bytes(const uint8_t b[64]) {
   bool inf = true;
   for (int i = 0; i < 64; ++i) inf &= b[i] == 0;

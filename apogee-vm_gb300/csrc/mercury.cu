@@ -360,6 +360,204 @@ F tensor_eval(const std::vector<F>& u, F x) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// The verifier's field side (crates/pcs-verify/src/lib.rs:355-434) and the
+// point checks around it (crates/pcs/src/lib.rs:509-548, 586-602): the
+// opening's transcript schedule replayed, h(alpha) and D(z) derived, the
+// BDFG20 batch at z', and the twelve accumulator entries of a deferred check.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct Entries {
+  uint8_t side[12];
+  F scalar[12];
+  uint8_t point[12][64];
+};
+
+// pcs::accumulate (lib.rs:509-548) with pcs_verify::scalars (:366-434).
+// `info` names the refused point: 0..7 the proof's points in field order
+// (h, q, g, s, d, pi_z, w, w'), 8 the commitment.
+int accumulate(const uint8_t cm[64], const std::vector<F>& u, const F& v, const uint8_t proof[704],
+               host::Transcript& tr, Entries& out, uint64_t* info) {
+  using namespace host;
+  const size_t nv = u.size();
+  if (nv < 2 || nv > 54 || nv % 2) return APG_ERR_UNSUPPORTED_NUM_VARS;
+  for (int i = 0; i < 8; ++i)
+    if (!host::g1::valid_encoding(proof + 64 * i)) {
+      if (info) *info = (uint64_t)i;
+      return APG_ERR_INVALID_POINT;
+    }
+  if (!host::g1::valid_encoding(cm)) {
+    if (info) *info = 8;
+    return APG_ERR_INVALID_POINT;
+  }
+  F ev[6];
+  for (int i = 0; i < 6; ++i)
+    if (!from_bytes(proof + 512 + 32 * i, ev[i])) return APG_ERR_NONCANONICAL;
+  const size_t t = nv / 2, b = (size_t)1 << t;
+  const std::vector<F> u1(u.begin(), u.begin() + t), u2(u.begin() + t, u.end());
+  const uint8_t* pt[8];
+  for (int i = 0; i < 8; ++i) pt[i] = proof + 64 * i;
+
+  // The opening's schedule, step for step.
+  tr.absorb(T_MERCURY_INSTANCE, std::vector<F>{from_u64((uint64_t)1 << nv)});
+  tr.absorb_g1(T_COMMITMENT, cm, 1);
+  std::vector<F> claim = u;
+  claim.push_back(v);
+  tr.absorb(T_EVALUATION_CLAIM, claim);
+  tr.absorb_g1(T_PCS_OPENING, pt[0], 1);
+  const F alpha = tr.challenge(T_MERCURY_ALPHA);
+  tr.absorb_g1(T_PCS_OPENING, pt[1], 2);
+  const F gamma = tr.challenge(T_MERCURY_GAMMA);
+  tr.absorb_g1(T_PCS_OPENING, pt[3], 2);
+  F z;
+  do {
+    z = tr.challenge(T_MERCURY_Z);
+  } while (z.zero());
+  if (fsqr(z) == fone() || z == alpha || fmul(z, alpha) == fone()) return APG_ERR_DEGENERATE_CHALLENGE;
+  const F zi = finv(z);
+  tr.absorb(T_PCS_OPENING, ev, 6);
+  tr.absorb_g1(T_PCS_OPENING, pt[5], 1);
+  const F delta = tr.challenge(T_BDFG_BATCH);
+  tr.absorb_g1(T_PCS_OPENING, pt[6], 1);
+  const F zp = tr.challenge(T_BDFG_POINT);
+  tr.absorb_g1(T_PCS_OPENING, pt[7], 1);
+  const F rho = tr.challenge(T_PAIRING_MERGE);
+
+  // h(alpha) from the symmetrized identity at z (derive_h_alpha, :205-227)
+  // and D(z) = z^(b-1) g(1/z).
+  F inner = fadd(fadd(fmul(ev[0], tensor_eval(u1, zi)), fmul(ev[1], tensor_eval(u1, z))),
+                 fmul(gamma, fsub(fsub(fadd(fmul(ev[2], tensor_eval(u2, zi)), fmul(ev[3], tensor_eval(u2, z))), v), v)));
+  inner = fsub(fsub(inner, fmul(z, ev[4])), fmul(zi, ev[5]));
+  const F h_alpha = fmul(inner, finv(from_u64(2)));
+  const F d_z = fmul(fpow_u64(z, b - 1), ev[1]);
+  // The BDFG20 batch at z' (bdfg::items, crates/pcs-verify/src/bdfg.rs):
+  // c_i = delta^i Z_{T minus S_i}(z'), constant = sum_i c_i r_i(z').
+  const Poly wa = uvanishing({alpha});
+  const Poly zc[4] = {wa, Poly{fone()}, wa, uvanishing({zi, alpha})};
+  const Poly rr[4] = {uinterpolate({{z, ev[0]}, {zi, ev[1]}}),
+                      uinterpolate({{z, ev[2]}, {zi, ev[3]}, {alpha, h_alpha}}),
+                      uinterpolate({{z, ev[4]}, {zi, ev[5]}}), Poly{d_z}};
+  F c[4], constant = fzero(), dp = fone();
+  for (int i = 0; i < 4; ++i) {
+    c[i] = fmul(dp, ueval(zc[i], zp));
+    constant = fadd(constant, fmul(c[i], ueval(rr[i], zp)));
+    dp = fmul(dp, delta);
+  }
+  const F z_t = ueval(uvanishing({z, zi, alpha}), zp);
+  const F z_pow_b = fpow_u64(z, b);
+  // Check A (the fold identity at z) plus rho times check B (the batch).
+  const F sc[12] = {fone(),
+                    fmul(rho, c[1]),
+                    fneg(fsub(z_pow_b, alpha)),
+                    fmul(rho, c[0]),
+                    fmul(rho, c[2]),
+                    fmul(rho, c[3]),
+                    z,
+                    fneg(fmul(rho, z_t)),
+                    fmul(rho, zp),
+                    fneg(fadd(ev[0], fmul(rho, constant))),
+                    fone(),
+                    rho};
+  // ENTRY_POINTS (:271-284): the points [cm, h, q, g, s, d, pi_z, w, w',
+  // [1]_1], ten on the [1]_2 side, then pi_z and w' on the [x]_2 side.
+  uint8_t gen[64] = {0};
+  gen[0] = 1;
+  gen[32] = 2;
+  const uint8_t* at[10] = {cm, pt[0], pt[1], pt[2], pt[3], pt[4], pt[5], pt[6], pt[7], gen};
+  const int idx[12] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 6, 8};
+  for (int i = 0; i < 12; ++i) {
+    out.side[i] = i < 10 ? 0 : 1;
+    out.scalar[i] = sc[i];
+    memcpy(out.point[i], at[idx[i]], 64);
+  }
+  return APG_OK;
+}
+
+void write_entries(const Entries& e, uint8_t* sides, uint8_t* scalars, uint8_t* points) {
+  memcpy(sides, e.side, 12);
+  memcpy(scalars, e.scalar, 12 * 32);
+  memcpy(points, e.point, 12 * 64);
+}
+
+bool read_frs_mem(const uint8_t* p, size_t n, std::vector<F>& out) {
+  out.resize(n);
+  for (size_t i = 0; i < n; ++i) {
+    memcpy(out[i].w, p + 32 * i, 32);
+    if (!host::below_p(out[i].w)) return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+// pcs::verify_deferred (crates/pcs/src/lib.rs:632-641).
+int mercury_verify_deferred_impl(const uint8_t cm[64], const uint8_t* u, size_t u_len, const uint8_t v[32],
+                                 const uint8_t proof[704], uint8_t* transcript, uint8_t* sides, uint8_t* scalars,
+                                 uint8_t* points, uint64_t* info) {
+  if (info) *info = 0;
+  if (!cm || (u_len && !u) || !v || !proof || !transcript || !sides || !scalars || !points)
+    return APG_ERR_INVALID_ARGUMENT;
+  std::vector<F> uu, vv;
+  if (!read_frs_mem(u, u_len, uu) || !read_frs_mem(v, 1, vv)) return APG_ERR_NONCANONICAL;
+  host::Transcript tr;
+  if (!tr.load(transcript)) return APG_ERR_INVALID_ARGUMENT;
+  Entries e;
+  const int st = accumulate(cm, uu, vv[0], proof, tr, e, info);
+  if (st) return st;
+  write_entries(e, sides, scalars, points);
+  tr.save(transcript);
+  return APG_OK;
+}
+
+// pcs::batch_verify_deferred (crates/pcs/src/lib.rs:661-670) through
+// batch_accumulate (:586-602): check_batch, every commitment validated, the
+// preamble (the commitments as passed, u || vs, rho), cm* = sum rho^i cm_i
+// and v* = sum rho^i v_i, then the single-instance core.
+int mercury_batch_verify_deferred_impl(const uint8_t* cms, size_t k, const uint8_t* u, size_t u_len,
+                                       const uint8_t* vs, size_t n_vs, const uint8_t proof[704], uint8_t* transcript,
+                                       uint8_t* sides, uint8_t* scalars, uint8_t* points, uint64_t* info) {
+  using namespace host;
+  if (info) *info = 0;
+  if ((k && !cms) || (u_len && !u) || (n_vs && !vs) || !proof || !transcript || !sides || !scalars || !points)
+    return APG_ERR_INVALID_ARGUMENT;
+  if (k == 0) return APG_ERR_EMPTY_BATCH;
+  if (k != n_vs) return APG_ERR_BATCH_LENGTH_MISMATCH;
+  if (u_len < 2 || u_len > 54 || u_len % 2) return APG_ERR_UNSUPPORTED_NUM_VARS;
+  for (size_t j = 0; j < k; ++j)
+    if (!host::g1::valid_encoding(cms + 64 * j)) {
+      if (info) *info = 8;
+      return APG_ERR_INVALID_POINT;
+    }
+  std::vector<F> uu, vals;
+  if (!read_frs_mem(u, u_len, uu) || !read_frs_mem(vs, n_vs, vals)) return APG_ERR_NONCANONICAL;
+  Transcript tr;
+  if (!tr.load(transcript)) return APG_ERR_INVALID_ARGUMENT;
+  // pcs_verify::batch_preamble (:333-347).
+  tr.absorb_g1(T_COMMITMENT, cms, k);
+  std::vector<F> claim = uu;
+  claim.insert(claim.end(), vals.begin(), vals.end());
+  tr.absorb(T_EVALUATION_CLAIM, claim);
+  const F rho = tr.challenge(T_MERCURY_BATCH);
+  std::vector<F> wts(k);
+  F acc = fone(), vstar = fzero();
+  for (size_t i = 0; i < k; ++i) {
+    wts[i] = acc;
+    vstar = fadd(vstar, fmul(acc, vals[i]));
+    acc = fmul(acc, rho);
+  }
+  uint8_t cm_star[64];
+  host::g1::msm_small(cms, wts.data(), k, cm_star);
+  Entries e;
+  const int st = accumulate(cm_star, uu, vstar, proof, tr, e, info);
+  if (st) return st;
+  write_entries(e, sides, scalars, points);
+  tr.save(transcript);
+  return APG_OK;
+}
+
+
+// ---------------------------------------------------------------------------
 
 int mercury_open_impl(Ctx& c, const Fr* d_f, size_t nv, const uint8_t cm[64], const std::vector<F>& u,
                       host::Transcript& tr, F& v_out, uint8_t proof_out[704]) {

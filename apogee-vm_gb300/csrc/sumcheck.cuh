@@ -167,6 +167,14 @@ int verify_zerocheck_impl(size_t arity, const uint8_t* coefs, const uint32_t* ta
 
 int mercury_open_impl(Ctx& c, const Fr* d_f, size_t nv, const uint8_t cm[64], const std::vector<host::F>& u,
                       host::Transcript& tr, host::F& v_out, uint8_t proof_out[704]);
+// pcs::verify_deferred / batch_verify_deferred on the host: the twelve
+// accumulator entries (sides, scalars in memory, canonical points).
+int mercury_verify_deferred_impl(const uint8_t cm[64], const uint8_t* u, size_t u_len, const uint8_t v[32],
+                                 const uint8_t proof[704], uint8_t* transcript, uint8_t* sides, uint8_t* scalars,
+                                 uint8_t* points, uint64_t* info);
+int mercury_batch_verify_deferred_impl(const uint8_t* cms, size_t k, const uint8_t* u, size_t u_len,
+                                       const uint8_t* vs, size_t n_vs, const uint8_t proof[704], uint8_t* transcript,
+                                       uint8_t* sides, uint8_t* scalars, uint8_t* points, uint64_t* info);
 int mercury_batch_open_stacked_impl(Ctx& c, const Fr* const* d_cols, const size_t* stack_lens, size_t nstacks,
                                     size_t width, const uint8_t* cms, const std::vector<host::F>& u,
                                     const std::vector<host::F>& r, host::Transcript& tr,

@@ -535,6 +535,32 @@ int apg_server_query(apg_server* server, apg_server_stats* out);
 
 /* ---- deferred-pairing accumulator (crates/pcs/src/accumulator.rs) ------- */
 
+/* pcs::verify_deferred (crates/pcs/src/lib.rs:632): every field-side check
+ * of a Mercury verification and every point check, stopping before the
+ * pairing. Host only (no context). cm: 64 bytes; u: u_len Fr in memory;
+ * v: Fr in memory; proof: the 704-byte MercuryProof::to_bytes; the
+ * transcript (226-byte snapshot) as the prover's was before its opening,
+ * advanced in place on success, left unchanged on failure. Out: the twelve
+ * AccumulatorEntry values of one deferred check (ENTRIES_PER_CHECK,
+ * crates/pcs-verify/src/lib.rs:271-284) in apg_discharge_msms's form:
+ * sides_out[12] (0 G2One, 1 G2X), scalars_out 12 Fr in memory, points_out
+ * 12 canonical 64-byte points. Errors in the reference's order:
+ * APG_ERR_UNSUPPORTED_NUM_VARS, APG_ERR_INVALID_POINT (*info = 0..7 the
+ * proof's points h, q, g, s, d, pi_z, w, w', 8 the commitment),
+ * APG_ERR_NONCANONICAL (a proof value), APG_ERR_DEGENERATE_CHALLENGE. */
+int apg_mercury_verify_deferred(const uint8_t cm[64], const uint8_t* u, size_t u_len, const uint8_t v[32],
+                                const uint8_t proof[704], uint8_t* transcript, uint8_t sides_out[12],
+                                uint8_t* scalars_out, uint8_t* points_out, uint64_t* info);
+/* pcs::batch_verify_deferred (lib.rs:661): k commitments (k x 64 bytes,
+ * absorbed as passed) claimed to open to vs (n_vs Fr in memory) at u; the
+ * preamble draws rho, cm* = sum rho^i cm_i is summed on the host and the
+ * single-instance core runs on (cm*, u, v*). Errors add, first,
+ * APG_ERR_EMPTY_BATCH and APG_ERR_BATCH_LENGTH_MISMATCH (check_batch), and a
+ * commitment off the curve is APG_ERR_INVALID_POINT with *info = 8. */
+int apg_mercury_batch_verify_deferred(const uint8_t* cms, size_t k, const uint8_t* u, size_t u_len,
+                                      const uint8_t* vs, size_t n_vs, const uint8_t proof[704], uint8_t* transcript,
+                                      uint8_t sides_out[12], uint8_t* scalars_out, uint8_t* points_out,
+                                      uint64_t* info);
 /* The group side of pcs::discharge (crates/pcs/src/accumulator.rs:146-163),
  * everything before its pairing. The accumulator is n entries (the fields of
  * AccumulatorEntry, :37-42): sides[i] 0 = PairingSide::G2One, 1 = G2X;
