@@ -246,3 +246,32 @@ def test_batch_open_stacked_refusal_order(ctx):
     assert refused([[col] * 5, [col]], 2, cms, u, r) == "BatchLengthMismatch"
     ctx.srs_generate(7, 8)
     assert refused([[col], [col]], 2, cms, u, r) == "SrsTooSmall"
+
+
+@pytest.mark.parametrize("nv,k", [(12, 0), (18, 0), (10, 16), (6, 40)])
+def test_device_openings_pass_the_deferred_verifier(ctx, nv, k):
+    """Openings made on the device (k = 0: one column; else a batch of k)
+    through the library's deferred verifier on the host: the twelve entries
+    satisfy A = tau B under the SRS's tau, and the verifier leaves the
+    transcript where the prover left it."""
+    import apogee_gpu as A
+
+    rng = random.Random(4400 + nv * 100 + k)
+    n = 1 << nv
+    tau = rng.randrange(1, O.P_R)
+    srs = O.toy_srs(tau, n)
+    ctx.srs_upload(srs)
+    cols = [[rng.choice([0, 1, rng.getrandbits(32), rng.randrange(O.P_R)]) for _ in range(n)]
+            for _ in range(max(k, 1))]
+    u = [rng.randrange(O.P_R) for _ in range(nv)]
+    cms = [ctx.commit(A.to_mont_bytes(c), nv) for c in cols]
+    snap = A.transcript_append_scalars(A.transcript_init(), 39, [nv])
+    if k == 0:
+        v, proof, after = ctx.open(A.to_mont_bytes(cols[0]), nv, cms[0], u, snap)
+        sides, scalars, points, tr = A.mercury_verify_deferred(cms[0], u, v, proof, snap)
+    else:
+        vs, proof, after = ctx.batch_open([A.to_mont_bytes(c) for c in cols], nv, cms, u, snap)
+        sides, scalars, points, tr = A.mercury_batch_verify_deferred(cms, u, vs, proof, snap)
+    assert tr == after
+    rc, a, b, _, _ = O.accumulator_msms(sides, scalars, points, [12], weights=[1])
+    assert rc == 0 and a == O.g1_mul(b, tau)
