@@ -26,14 +26,14 @@ PROOF_BYTES = 704
 STATUS = {
     0: "Ok", 1: "LengthMismatch", 2: "UnsupportedNumVars", 3: "PointLengthMismatch", 4: "SrsTooSmall",
     5: "DegenerateChallenge", 6: "EmptyBatch", 7: "BatchLengthMismatch", 8: "MixedColumnSizes",
-    9: "InvalidPoint", 10: "MalformedAccumulator", 20: "NonCanonical", 21: "InvalidArgument", 22: "BadCircuit", 23: "NoSrs",
+    9: "InvalidPoint", 10: "MalformedAccumulator", 11: "VerificationFailed", 20: "NonCanonical", 21: "InvalidArgument", 22: "BadCircuit", 23: "NoSrs",
     24: "Internal", 25: "NoAllocTooLarge", 26: "Pending", 27: "UnknownTicket", 28: "MissingChallenge",
     29: "OutputShape", 30: "ProofShape", 31: "LayerInconsistency", 32: "RoundCountMismatch",
     33: "FinalEvalCountMismatch", 34: "RoundSumMismatch", 35: "FinalEvalMismatch", 100: "Cuda", 101: "OutOfMemory",
     103: "NoDevice",
 }
 PENDING = 26
-PCS_CODES = {2, 3, 4, 5, 6, 7, 8, 9, 10}
+PCS_CODES = {2, 3, 4, 5, 6, 7, 8, 9, 10, 11}
 
 
 class ApogeeError(RuntimeError):
@@ -254,6 +254,62 @@ def mercury_batch_verify_deferred(cms, u, vs, proof: bytes, snap: bytes):
     return _deferred_result(st, info, sides, scalars, points, tr, "apg_mercury_batch_verify_deferred")
 
 
+def pairing(p: bytes, q: bytes) -> bytes:
+    """curve::pairing::pairing of a canonical G1 (64 bytes) and G2 (128 bytes)
+    point: the Fq12 value as 384 canonical bytes."""
+    out = ctypes.create_string_buffer(384)
+    st = lib().apg_pairing(bytes(p), bytes(q), out)
+    if st:
+        raise PcsError(st, "apg_pairing") if st in PCS_CODES else ApogeeError(st, "apg_pairing")
+    return out.raw
+
+
+def pairing_check(ps, qs) -> bool:
+    """curve::pairing::pairing_check: prod_i e(ps[i], qs[i]) == 1."""
+    holds = ctypes.c_int(0)
+    st = lib().apg_pairing_check(b"".join(ps), b"".join(qs), ctypes.c_size_t(len(ps)), ctypes.byref(holds))
+    if st:
+        raise PcsError(st, "apg_pairing_check") if st in PCS_CODES else ApogeeError(st, "apg_pairing_check")
+    return bool(holds.value)
+
+
+def g2_mul(q: bytes, k: int) -> bytes:
+    out = ctypes.create_string_buffer(128)
+    st = lib().apg_g2_mul(bytes(q), int(k % (1 << 256)).to_bytes(32, "little"), out)
+    if st:
+        raise PcsError(st, "apg_g2_mul") if st in PCS_CODES else ApogeeError(st, "apg_g2_mul")
+    return out.raw
+
+
+def mercury_verify(vsrs: bytes, cm: bytes, u, v: int, proof: bytes, snap: bytes) -> bytes:
+    """pcs::verify under the SrsVerifier's 320-byte wire form: returns the
+    transcript after the verification, raises VerifyPcsError where the
+    reference returns a PcsError (VerificationFailed included)."""
+    tr = ctypes.create_string_buffer(bytes(snap), TRANSCRIPT_BYTES)
+    info = ctypes.c_uint64(0)
+    st = lib().apg_mercury_verify(bytes(vsrs), bytes(cm), to_mont_bytes(u), ctypes.c_size_t(len(u)),
+                                  to_mont_bytes([v]), bytes(proof), tr, ctypes.byref(info))
+    if st in PCS_CODES:
+        raise VerifyPcsError(st, info.value)
+    if st:
+        raise ApogeeError(st, "apg_mercury_verify")
+    return tr.raw
+
+
+def mercury_batch_verify(vsrs: bytes, cms, u, vs, proof: bytes, snap: bytes) -> bytes:
+    """pcs::batch_verify; as mercury_verify."""
+    tr = ctypes.create_string_buffer(bytes(snap), TRANSCRIPT_BYTES)
+    info = ctypes.c_uint64(0)
+    st = lib().apg_mercury_batch_verify(bytes(vsrs), b"".join(cms), ctypes.c_size_t(len(cms)), to_mont_bytes(u),
+                                        ctypes.c_size_t(len(u)), to_mont_bytes(vs), ctypes.c_size_t(len(vs)),
+                                        bytes(proof), tr, ctypes.byref(info))
+    if st in PCS_CODES:
+        raise VerifyPcsError(st, info.value)
+    if st:
+        raise ApogeeError(st, "apg_mercury_batch_verify")
+    return tr.raw
+
+
 class SumcheckError(ApogeeError):
     """sumcheck::SumcheckError: `variant` is RoundCountMismatch,
     FinalEvalCountMismatch, RoundSumMismatch or FinalEvalMismatch; `info`
@@ -403,6 +459,13 @@ class Context:
         a, b, nu = (ctypes.create_string_buffer(k) for k in (64, 64, 32))
         self._check(lib().apg_discharge_msms(self._h, sd, sc, pt, n, cs, ctypes.c_size_t(len(checks)), a, b, nu))
         return a.raw, b.raw, nu.raw
+
+    def discharge(self, vsrs: bytes, sides, scalars: bytes, points: bytes, checks):
+        """pcs::discharge (crates/pcs/src/accumulator.rs:146): the MSMs on the
+        device, the pairing on the host, under the SrsVerifier's 320-byte wire
+        form. Returns None; raises PcsError (VerificationFailed among them)."""
+        sd, sc, pt, n, cs = self._acc_args(sides, scalars, points, checks)
+        self._check(lib().apg_discharge(self._h, bytes(vsrs), sd, sc, pt, n, cs, ctypes.c_size_t(len(checks))))
 
     def pairing_msms(self, sides, scalars: bytes, points: bytes, checks, weights: bytes):
         """check_pairings' two MSMs (accumulator.rs:171-214) with one weight a

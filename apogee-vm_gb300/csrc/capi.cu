@@ -12,6 +12,19 @@ struct apg_ctx {
   Ctx c;
 };
 
+// A host-only entry point: library errors become their status, nothing
+// escapes to the caller.
+template <class Fn>
+static int host_call(Fn&& f) {
+  try {
+    return f();
+  } catch (const Error& e) {
+    return e.status;
+  } catch (...) {
+    return APG_ERR_INTERNAL;
+  }
+}
+
 extern "C" {
 static void release_lane(Ctx& c);
 }
@@ -803,6 +816,40 @@ int apg_mercury_batch_verify_deferred(const uint8_t* cms, size_t k, const uint8_
   } catch (...) {
     return APG_ERR_INTERNAL;
   }
+}
+
+int apg_pairing(const uint8_t p[64], const uint8_t q[128], uint8_t out[384]) {
+  return host_call([&] { return pairing_impl(p, q, out); });
+}
+
+int apg_g2_mul(const uint8_t q[128], const uint8_t k[32], uint8_t out[128]) {
+  return host_call([&] { return g2_mul_impl(q, k, out); });
+}
+
+int apg_pairing_check(const uint8_t* ps, const uint8_t* qs, size_t n, int* holds) {
+  return host_call([&] { return pairing_check_impl(ps, qs, n, holds); });
+}
+
+int apg_mercury_verify(const uint8_t vsrs[320], const uint8_t cm[64], const uint8_t* u, size_t u_len,
+                       const uint8_t v[32], const uint8_t proof[704], uint8_t* transcript, uint64_t* info) {
+  return host_call([&] { return mercury_verify_impl(vsrs, cm, u, u_len, v, proof, transcript, info); });
+}
+
+int apg_mercury_batch_verify(const uint8_t vsrs[320], const uint8_t* cms, size_t k, const uint8_t* u, size_t u_len,
+                             const uint8_t* vs, size_t n_vs, const uint8_t proof[704], uint8_t* transcript,
+                             uint64_t* info) {
+  return host_call(
+      [&] { return mercury_batch_verify_impl(vsrs, cms, k, u, u_len, vs, n_vs, proof, transcript, info); });
+}
+
+int apg_discharge(apg_ctx* ctx, const uint8_t vsrs[320], const uint8_t* sides, const uint8_t* scalars,
+                  const uint8_t* points, size_t n, const size_t* checks, size_t n_checks) {
+  return guarded(ctx, [&](Ctx& c) {
+    uint8_t a[64], b[64], nu[32];
+    const int st = accumulator_msms(c, sides, scalars, points, n, checks, n_checks, nullptr, a, b, nu);
+    if (st) return st;
+    return discharge_pairing_impl(vsrs, a, b);
+  });
 }
 
 int apg_verify_zerocheck(size_t arity, const uint8_t* coefs, const uint32_t* a, const uint32_t* b, size_t nterms,

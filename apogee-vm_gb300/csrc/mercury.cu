@@ -12,6 +12,7 @@
 #include <algorithm>
 
 #include "host_g1.hpp"
+#include "host_pairing.hpp"
 #include "sumcheck.cuh"
 
 namespace apg {
@@ -556,6 +557,153 @@ int mercury_batch_verify_deferred_impl(const uint8_t* cms, size_t k, const uint8
   return APG_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// The pairing step (crates/curve/src/pairing.rs, crates/pcs/src/accumulator.rs
+// check_pairings :171-214): e(A, [1]_2) e(-B, [x]_2) == 1 with A and B the
+// weighted sums of the entries on each side, over the verifier's SRS points
+// (SrsVerifier, crates/srs/src/lib.rs:279-283: [1]_1 || [1]_2 || [x]_2).
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct Vsrs {
+  host::pairing::G2 g2_gen, g2_tau;
+};
+
+int read_vsrs(const uint8_t vsrs[320], Vsrs& out) {
+  if (!host::g1::valid_encoding(vsrs)) return APG_ERR_INVALID_POINT;
+  if (!host::pairing::g2from_bytes(vsrs + 64, out.g2_gen) || !host::pairing::g2from_bytes(vsrs + 192, out.g2_tau))
+    return APG_ERR_INVALID_POINT;
+  return APG_OK;
+}
+
+// -P for a canonical encoding (infinity stays infinity).
+void g1_negate(const uint8_t p[64], uint8_t out[64]) {
+  memcpy(out, p, 64);
+  bool inf = true;
+  for (int i = 0; i < 64; ++i) inf &= p[i] == 0;
+  if (inf) return;
+  uint64_t y[4];
+  memcpy(y, p + 32, 32);
+  if ((y[0] | y[1] | y[2] | y[3]) == 0) return;
+  uint64_t br = 0;
+  for (int i = 0; i < 4; ++i) {
+    const host::u128 d = (host::u128)host::g1::kQ[i] - y[i] - br;
+    y[i] = (uint64_t)d;
+    br = (uint64_t)(d >> 127);
+  }
+  memcpy(out + 32, y, 32);
+}
+
+bool pairings_hold(const Vsrs& vk, const uint8_t a[64], const uint8_t b[64]) {
+  uint8_t nb[64];
+  g1_negate(b, nb);
+  return host::pairing::pairing_check({a, nb}, {vk.g2_gen, vk.g2_tau});
+}
+
+// One deferred check with weight one: A and B summed on the host.
+int check_entries(const Vsrs& vk, const Entries& e) {
+  std::vector<uint8_t> pa, pb;
+  std::vector<F> sa, sb;
+  for (int i = 0; i < 12; ++i) {
+    auto& pts = e.side[i] ? pb : pa;
+    pts.insert(pts.end(), e.point[i], e.point[i] + 64);
+    (e.side[i] ? sb : sa).push_back(e.scalar[i]);
+  }
+  uint8_t a[64], b[64];
+  host::g1::msm_small(pa.data(), sa.data(), sa.size(), a);
+  host::g1::msm_small(pb.data(), sb.data(), sb.size(), b);
+  return pairings_hold(vk, a, b) ? APG_OK : APG_ERR_VERIFICATION_FAILED;
+}
+
+}  // namespace
+
+int pairing_impl(const uint8_t p[64], const uint8_t q[128], uint8_t out[384]) {
+  if (!p || !q || !out) return APG_ERR_INVALID_ARGUMENT;
+  host::pairing::G2 qq;
+  if (!host::g1::valid_encoding(p) || !host::pairing::g2from_bytes(q, qq)) return APG_ERR_INVALID_POINT;
+  host::g1::Q x, y;
+  bool inf;
+  host::pairing::g1_affine(p, x, y, inf);
+  host::pairing::f12to_bytes(host::pairing::final_exponentiation(host::pairing::miller_loop(x, y, inf, qq)), out);
+  return APG_OK;
+}
+
+int g2_mul_impl(const uint8_t q[128], const uint8_t k[32], uint8_t out[128]) {
+  if (!q || !k || !out) return APG_ERR_INVALID_ARGUMENT;
+  host::pairing::G2 qq;
+  if (!host::pairing::g2from_bytes(q, qq)) return APG_ERR_INVALID_POINT;
+  host::pairing::Big kb(4);
+  memcpy(kb.data(), k, 32);
+  host::pairing::big_trim(kb);
+  host::pairing::g2to_bytes(host::pairing::g2mul(qq, kb), out);
+  return APG_OK;
+}
+
+int pairing_check_impl(const uint8_t* ps, const uint8_t* qs, size_t n, int* holds) {
+  if ((n && (!ps || !qs)) || !holds) return APG_ERR_INVALID_ARGUMENT;
+  std::vector<const uint8_t*> pp(n);
+  std::vector<host::pairing::G2> qq(n);
+  for (size_t i = 0; i < n; ++i) {
+    pp[i] = ps + 64 * i;
+    if (!host::g1::valid_encoding(pp[i]) || !host::pairing::g2from_bytes(qs + 128 * i, qq[i]))
+      return APG_ERR_INVALID_POINT;
+  }
+  *holds = host::pairing::pairing_check(pp, qq) ? 1 : 0;
+  return APG_OK;
+}
+
+// pcs::verify (crates/pcs/src/lib.rs:614-628): the deferred check, then its
+// pairing.
+int mercury_verify_impl(const uint8_t vsrs[320], const uint8_t cm[64], const uint8_t* u, size_t u_len,
+                        const uint8_t v[32], const uint8_t proof[704], uint8_t* transcript, uint64_t* info) {
+  if (!vsrs) return APG_ERR_INVALID_ARGUMENT;
+  uint8_t snap[226], sides[12], scalars[12 * 32], points[12 * 64];
+  if (!transcript) return APG_ERR_INVALID_ARGUMENT;
+  memcpy(snap, transcript, 226);
+  int st = mercury_verify_deferred_impl(cm, u, u_len, v, proof, snap, sides, scalars, points, info);
+  if (st) return st;
+  Vsrs vk;
+  if ((st = read_vsrs(vsrs, vk))) return st;
+  Entries e;
+  memcpy(e.side, sides, 12);
+  memcpy(e.scalar, scalars, sizeof(scalars));
+  memcpy(e.point, points, sizeof(points));
+  if ((st = check_entries(vk, e))) return st;
+  memcpy(transcript, snap, 226);
+  return APG_OK;
+}
+
+// pcs::batch_verify (lib.rs:648-658).
+int mercury_batch_verify_impl(const uint8_t vsrs[320], const uint8_t* cms, size_t k, const uint8_t* u, size_t u_len,
+                              const uint8_t* vs, size_t n_vs, const uint8_t proof[704], uint8_t* transcript,
+                              uint64_t* info) {
+  if (!vsrs || !transcript) return APG_ERR_INVALID_ARGUMENT;
+  uint8_t snap[226], sides[12], scalars[12 * 32], points[12 * 64];
+  memcpy(snap, transcript, 226);
+  int st = mercury_batch_verify_deferred_impl(cms, k, u, u_len, vs, n_vs, proof, snap, sides, scalars, points, info);
+  if (st) return st;
+  Vsrs vk;
+  if ((st = read_vsrs(vsrs, vk))) return st;
+  Entries e;
+  memcpy(e.side, sides, 12);
+  memcpy(e.scalar, scalars, sizeof(scalars));
+  memcpy(e.point, points, sizeof(points));
+  if ((st = check_entries(vk, e))) return st;
+  memcpy(transcript, snap, 226);
+  return APG_OK;
+}
+
+// The pairing step of pcs::discharge (accumulator.rs:146-163) over the A and B
+// its MSMs produced (apg_discharge_msms).
+int discharge_pairing_impl(const uint8_t vsrs[320], const uint8_t a[64], const uint8_t b[64]) {
+  if (!vsrs || !a || !b) return APG_ERR_INVALID_ARGUMENT;
+  Vsrs vk;
+  const int st = read_vsrs(vsrs, vk);
+  if (st) return st;
+  return pairings_hold(vk, a, b) ? APG_OK : APG_ERR_VERIFICATION_FAILED;
+}
 
 // ---------------------------------------------------------------------------
 

@@ -175,6 +175,16 @@ int mercury_verify_deferred_impl(const uint8_t cm[64], const uint8_t* u, size_t 
 int mercury_batch_verify_deferred_impl(const uint8_t* cms, size_t k, const uint8_t* u, size_t u_len,
                                        const uint8_t* vs, size_t n_vs, const uint8_t proof[704], uint8_t* transcript,
                                        uint8_t* sides, uint8_t* scalars, uint8_t* points, uint64_t* info);
+// The pairing (host): e(P, Q), a product check, and the verifiers built on it.
+int pairing_impl(const uint8_t p[64], const uint8_t q[128], uint8_t out[384]);
+int pairing_check_impl(const uint8_t* ps, const uint8_t* qs, size_t n, int* holds);
+int g2_mul_impl(const uint8_t q[128], const uint8_t k[32], uint8_t out[128]);
+int mercury_verify_impl(const uint8_t vsrs[320], const uint8_t cm[64], const uint8_t* u, size_t u_len,
+                        const uint8_t v[32], const uint8_t proof[704], uint8_t* transcript, uint64_t* info);
+int mercury_batch_verify_impl(const uint8_t vsrs[320], const uint8_t* cms, size_t k, const uint8_t* u, size_t u_len,
+                              const uint8_t* vs, size_t n_vs, const uint8_t proof[704], uint8_t* transcript,
+                              uint64_t* info);
+int discharge_pairing_impl(const uint8_t vsrs[320], const uint8_t a[64], const uint8_t b[64]);
 int mercury_batch_open_stacked_impl(Ctx& c, const Fr* const* d_cols, const size_t* stack_lens, size_t nstacks,
                                     size_t width, const uint8_t* cms, const std::vector<host::F>& u,
                                     const std::vector<host::F>& r, host::Transcript& tr,

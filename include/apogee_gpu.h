@@ -49,6 +49,7 @@ enum apg_status {
   APG_ERR_MIXED_COLUMN_SIZES = 8,     /* PcsError::MixedColumnSizes */
   APG_ERR_INVALID_POINT = 9,          /* PcsError::InvalidPoint / off-curve input */
   APG_ERR_MALFORMED_ACCUMULATOR = 10, /* PcsError::MalformedAccumulator */
+  APG_ERR_VERIFICATION_FAILED = 11,   /* PcsError::VerificationFailed: the pairing check failed */
   APG_ERR_NONCANONICAL = 20,          /* an input value is >= its modulus */
   APG_ERR_INVALID_ARGUMENT = 21,      /* null pointer, bad shape */
   APG_ERR_BAD_CIRCUIT = 22,           /* malformed circuit blob */
@@ -561,6 +562,37 @@ int apg_mercury_batch_verify_deferred(const uint8_t* cms, size_t k, const uint8_
                                       const uint8_t* vs, size_t n_vs, const uint8_t proof[704], uint8_t* transcript,
                                       uint8_t sides_out[12], uint8_t* scalars_out, uint8_t* points_out,
                                       uint64_t* info);
+/* ---- the pairing and the full verifications (host) ----------------------- */
+
+/* curve::pairing::pairing (crates/curve/src/pairing.rs): the optimal ate
+ * pairing e(P, Q) = f_{6x+2,Q}(P)^((q^12 - 1)/r) of a canonical G1 point (64
+ * bytes) and a canonical G2 point (128 bytes: x.c0 || x.c1 || y.c0 || y.c1),
+ * written as the Fq12 c0 || c1 (each Fq6 c0 || c1 || c2, each Fq2 c0 || c1,
+ * canonical Fq): 384 bytes. A point off its curve, a G2 point outside the
+ * order-r subgroup or a coordinate >= q is APG_ERR_INVALID_POINT. */
+int apg_pairing(const uint8_t p[64], const uint8_t q[128], uint8_t out[384]);
+/* k Q for a canonical G2 point Q (G2Projective * k, crates/curve/src/g2.rs),
+ * k 32 bytes little-endian (any 256-bit integer), the result canonical. */
+int apg_g2_mul(const uint8_t q[128], const uint8_t k[32], uint8_t out[128]);
+/* curve::pairing::pairing_check: prod_i e(P_i, Q_i) == 1 into *holds (1/0),
+ * n pairs as n x 64 and n x 128 bytes; points validated as for apg_pairing. */
+int apg_pairing_check(const uint8_t* ps, const uint8_t* qs, size_t n, int* holds);
+/* pcs::verify (crates/pcs/src/lib.rs:614): apg_mercury_verify_deferred, then
+ * its pairing over the SrsVerifier's wire form vsrs (320 bytes, [1]_1 ||
+ * [1]_2 || [x]_2, crates/srs/src/lib.rs:279-290). APG_OK, its errors, or
+ * APG_ERR_VERIFICATION_FAILED; the transcript advances only on APG_OK. */
+int apg_mercury_verify(const uint8_t vsrs[320], const uint8_t cm[64], const uint8_t* u, size_t u_len,
+                       const uint8_t v[32], const uint8_t proof[704], uint8_t* transcript, uint64_t* info);
+/* pcs::batch_verify (lib.rs:648): as apg_mercury_verify over a batch. */
+int apg_mercury_batch_verify(const uint8_t vsrs[320], const uint8_t* cms, size_t k, const uint8_t* u, size_t u_len,
+                             const uint8_t* vs, size_t n_vs, const uint8_t proof[704], uint8_t* transcript,
+                             uint64_t* info);
+/* pcs::discharge (crates/pcs/src/accumulator.rs:146): apg_discharge_msms on
+ * the device, then the pairing e(A, [1]_2) e(-B, [x]_2) == 1 on the host.
+ * APG_OK, the MSMs' errors, or APG_ERR_VERIFICATION_FAILED. */
+int apg_discharge(apg_ctx* ctx, const uint8_t vsrs[320], const uint8_t* sides, const uint8_t* scalars,
+                  const uint8_t* points, size_t n, const size_t* checks, size_t n_checks);
+
 /* The group side of pcs::discharge (crates/pcs/src/accumulator.rs:146-163),
  * everything before its pairing. The accumulator is n entries (the fields of
  * AccumulatorEntry, :37-42): sides[i] 0 = PairingSide::G2One, 1 = G2X;

@@ -32,6 +32,8 @@ SOURCES = {
     "mercury_proof.txt": ("crates/pcs/tests/vectors/mercury_proof.txt", None, None),
     "mercury_batch.txt": ("crates/pcs/tests/vectors/mercury_batch.txt", None, None),
     "accumulator.txt": ("crates/pcs/tests/vectors/accumulator.txt", None, None),
+    "pairing_kats.txt": ("crates/curve/tests/vectors/pairing_kats.txt", None, None),
+    "g2_kats.txt": ("crates/curve/tests/vectors/g2_kats.txt", None, 200),
 }
 
 

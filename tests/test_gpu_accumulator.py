@@ -149,3 +149,20 @@ def test_refusals_in_the_reference_order(ctx):
     # the context is clean afterwards
     a, b, _ = ctx.discharge_msms(sides, sc, good_pts, checks)
     assert O.g1_mul(b, tau) == a
+
+
+def test_discharge_with_its_pairing(ctx):
+    """pcs::discharge end to end: the golden accumulator's MSMs on the device
+    and the pairing e(A, [1]_2) e(-B, [tau]_2) on the host under the toy
+    tau's verifier points; a bumped scalar fails with VerificationFailed."""
+    import apogee_gpu as A
+    from test_host_pairing import _toy_vsrs
+
+    tau, sides, scalars, points, checks = _golden()
+    vsrs = _toy_vsrs(A)
+    ctx.discharge(vsrs, sides, _mont(scalars), b"".join(points), checks)
+    bad = list(scalars)
+    bad[3] = (bad[3] + 1) % O.P_R
+    with pytest.raises(A.PcsError) as e:
+        ctx.discharge(vsrs, sides, _mont(bad), b"".join(points), checks)
+    assert e.value.variant == "VerificationFailed"
