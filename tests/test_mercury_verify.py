@@ -185,3 +185,53 @@ def test_batches_of_many_commitments_sum_on_the_host():
     w = [pow(rho, i, P) for i in range(40)]
     want = O.msm(b"".join(cms), b"".join(O.fe(x) for x in w), 40)
     assert got[2][0] == want
+
+
+@pytest.mark.parametrize("nv,k", [(2, 0), (6, 0), (8, 0), (4, 3), (6, 9)])
+def test_oracle_openings_verify(nv, k):
+    """Openings the oracle makes on the CPU at other sizes (k = 0: one
+    column, else a batch of k) through the deferred verifier: the entries
+    satisfy A = tau B under the SRS's tau, the transcript ends where the
+    prover's did; a bumped claim breaks the relation."""
+    import ctypes
+
+    A = _A()
+    rng = random.Random(700 + 10 * nv + k)
+    tau = rng.randrange(1, P)
+    n = 1 << nv
+    srs = O.toy_srs(tau, n)
+    cols = [[rng.choice([0, 1, rng.getrandbits(32), rng.randrange(P)]) for _ in range(n)] for _ in range(max(k, 1))]
+    u = [rng.randrange(P) for _ in range(nv)]
+    cms = []
+    for c in cols:
+        out = O.buf(64)
+        assert O.lib().oracle_commit(srs, ctypes.c_size_t(n), b"".join(O.fe(x) for x in c), nv, 4, out) == 0
+        cms.append(out.raw)
+    snap = O.new_snapshot()
+    after = bytearray(snap)
+    s = (ctypes.c_uint8 * O.SNAP).from_buffer(after)
+    proof = O.buf(704)
+    if k == 0:
+        v = O.buf(32)
+        assert O.lib().oracle_mercury_open(srs, ctypes.c_size_t(n), b"".join(O.fe(x) for x in cols[0]), nv, cms[0],
+                                           b"".join(O.fe(x) for x in u), s, 4, v, proof) == 0
+        del s
+        got = A.mercury_verify_deferred(cms[0], u, O.fe_int(v.raw), proof.raw, bytes(snap))
+        bad = A.mercury_verify_deferred(cms[0], u, (O.fe_int(v.raw) + 1) % P, proof.raw, bytes(snap))
+    else:
+        vs = O.buf(32 * k)
+        assert O.lib().oracle_mercury_batch_open(srs, ctypes.c_size_t(n), b"".join(O.fe(x) for c in cols for x in c),
+                                                 ctypes.c_size_t(k), nv, b"".join(cms), b"".join(O.fe(x) for x in u),
+                                                 s, 4, vs, proof) == 0
+        del s
+        vals = [O.fe_int(vs.raw[32 * i:32 * i + 32]) for i in range(k)]
+        got = A.mercury_batch_verify_deferred(cms, u, vals, proof.raw, bytes(snap))
+        vals[-1] = (vals[-1] + 1) % P
+        bad = A.mercury_batch_verify_deferred(cms, u, vals, proof.raw, bytes(snap))
+    assert got[3] == bytes(after)
+
+    def holds(entries, t):
+        rc, a, b, _, _ = O.accumulator_msms(entries[0], entries[1], entries[2], [12], weights=[1])
+        return rc == 0 and a == O.g1_mul(b, t)
+
+    assert holds(got, tau) and not holds(bad, tau)
