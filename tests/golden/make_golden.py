@@ -18,7 +18,7 @@ import os
 import sys
 
 SOURCES = {
-    # name: (path inside the reference, line filter, max data lines or None)
+    # name: (path inside the reference, line filter, max data lines (per kind) or None)
     "fr_kats.txt": ("crates/field/tests/vectors/fr_kats.txt", None, None),
     "fq_kats.txt": ("crates/curve/tests/vectors/fq_kats.txt", ("fq_ops", "fq_pow", "fq_bytes", "fq_u64"), None),
     "g1_kats.txt": ("crates/curve/tests/vectors/g1_kats.txt", None, None),
@@ -34,6 +34,8 @@ SOURCES = {
     "accumulator.txt": ("crates/pcs/tests/vectors/accumulator.txt", None, None),
     "pairing_kats.txt": ("crates/curve/tests/vectors/pairing_kats.txt", None, None),
     "g2_kats.txt": ("crates/curve/tests/vectors/g2_kats.txt", None, 200),
+    "fq12_kats.txt": ("crates/curve/tests/vectors/fq12_kats.txt", ("fq12_ops", "fq12_final_exp"),
+                      {"fq12_ops": 68, "fq12_final_exp": 20}),
 }
 
 
@@ -70,10 +72,15 @@ def main(ref_root: str) -> None:
                 continue
             if limit is not None:
                 counts[kind] = counts.get(kind, 0) + 1
-                if counts[kind] > limit:
+                if counts[kind] > (limit[kind] if isinstance(limit, dict) else limit):
                     continue
             kept.append(line)
-        sel = "all data lines" if limit is None else f"first {limit} data lines of each record kind"
+        if limit is None:
+            sel = "all data lines"
+        elif isinstance(limit, dict):
+            sel = "first " + ", ".join(f"{v} {k}" for k, v in limit.items()) + " data lines"
+        else:
+            sel = f"first {limit} data lines of each record kind"
         if kinds is not None:
             sel += f" of kinds {', '.join(kinds)}"
         header = [f"# golden vectors from the reference's {rel}", f"# selection: {sel}"]

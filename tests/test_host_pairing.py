@@ -2,8 +2,9 @@
 it, against what the reference holds:
 
 * G2 arithmetic and decoding against g2_kats.txt (P + Q, 2P, kP, -P, the
-  rejection classes including points outside the order-r subgroup),
-  compiled for the host here from the library's header;
+  rejection classes including points outside the order-r subgroup) and the
+  Fq12 tower and exact final exponent against fq12_kats.txt, compiled for the
+  host here from the library's header;
 * apg_pairing against every pairing_kats.txt case (the exact final exponent
   (q^12 - 1)/r of the optimal ate Miller loop), and bilinearity;
 * apg_mercury_verify / apg_mercury_batch_verify on the golden proofs and the
@@ -61,6 +62,26 @@ def test_g2_arithmetic_and_decoding():
     assert r.returncode == 0, r.stdout + r.stderr
     ops, rejects, gens = map(int, r.stdout.split())
     assert ops == 200 and rejects == 14 and gens == 1
+
+
+def test_fq12_tower_and_final_exponent():
+    """The tower's Fq12 arithmetic and the exact final exponent against
+    fq12_kats.txt: 64 edge-grid and 4 random lines of a + b, a - b, ab, a^2,
+    1/a, conj a, a^q, a^(q^2), a^(q^3), and 20 final exponentiations."""
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("g++ not found")
+    exe = os.path.join(os.environ.get("TMPDIR", "/tmp"), f"fq12_check_{os.getpid()}")
+    subprocess.run([cxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "apogee-vm_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "native", "fq12_check.cpp"), "-o", exe], check=True,
+                   capture_output=True)
+    try:
+        r = subprocess.run([exe, os.path.join(O.GOLDEN, "fq12_kats.txt")], capture_output=True, text=True,
+                           timeout=300)
+    finally:
+        os.unlink(exe)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.split() == ["68", "20"]
 
 
 def test_pairing_known_answers():
